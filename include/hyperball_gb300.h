@@ -1,0 +1,218 @@
+/*
+ * hyperball_gb300.h — C ABI of the GB300 (sm_103a) HyperBall library.
+ *
+ * This is the drop-in boundary for the HyperBall path of the Rust crate
+ * webgraph-algo 0.1.0. Each entry point names the reference item it replaces
+ * (paths are relative to that crate). A Rust wrapper binds these functions
+ * with `extern "C"` and keeps the reference's builder/run/getter shape.
+ *
+ * Conventions
+ *  - Every function returns an int status (HB_OK = 0) unless stated.
+ *  - Graph inputs are host arrays; hb_create copies them to the device, so the
+ *    caller keeps ownership. Outputs go into caller-provided host buffers.
+ *  - One handle is driven by one host thread; distinct handles are independent.
+ *  - On error, hb_last_error(handle) (or hb_global_last_error() for calls that
+ *    have no handle) returns a message; the reference's anyhow errors map to
+ *    HB_ERR_NOT_RUN / HB_ERR_NOT_REQUESTED / HB_ERR_INVALID below.
+ *  - No torch or C++ types cross this boundary.
+ */
+#ifndef HYPERBALL_GB300_H
+#define HYPERBALL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define HB_OK 0
+#define HB_ERR_INVALID 1       /* bad argument (reference: builder asserts, HB:153-167, HB:211-238, HLL:379-403) */
+#define HB_ERR_NOT_RUN 2       /* accessor before run (reference: ensure_iteration, HB:624-630) */
+#define HB_ERR_NOT_REQUESTED 3 /* output not requested (reference: bail!, HB:645, HB:655, HB:669) */
+#define HB_ERR_OOM 4           /* device allocation failed */
+#define HB_ERR_CUDA 5          /* CUDA runtime error */
+#define HB_ERR_TIMEOUT 6       /* a bounded device wait gave up */
+#define HB_ERR_IO 7            /* file not readable */
+#define HB_ERR_NO_DEVICE 8     /* no CUDA device: the library has no CPU fallback */
+
+/* ---- hashers (reference: HyperLogLogBuilder::build_hasher, HLL:356-363) -- */
+#define HB_HASH_SIP13 0   /* Rust std DefaultHasher (SipHash-1-3, zero keys), the default of HyperLogLogBuilder::new (HLL:244-251) */
+#define HB_HASH_JENKINS 1 /* JenkinsHasher(seed) of tests/test_hyperball.rs:25-172 (Java dsiutils mix) */
+
+/* ---- option flags --------------------------------------------------------- */
+#define HB_SUM_OF_DISTANCES (1u << 0)         /* HyperBallBuilder::sum_of_distances(true), HB:262-265 */
+#define HB_SUM_OF_INVERSE_DISTANCES (1u << 1) /* HyperBallBuilder::sum_of_inverse_distances(true), HB:268-271 */
+#define HB_TRANSPOSE_ON_DEVICE (1u << 2)      /* build the transpose on the GPU (enables systolic iterations) */
+#define HB_NO_I32_SHIFT_QUIRK (1u << 3)       /* count() with +2^-31 for register value 31 instead of Rust's i32 wrap (HLL:178) */
+
+/* "choose automatically" value of the tuning fields of hb_options */
+#define HB_AUTO 0xffffffffu
+
+/* Which counter array hb_get_registers copies. */
+#define HB_CURRENT_STATE 0
+#define HB_NEXT_STATE 1
+
+typedef struct hb_handle hb_handle;
+typedef struct hb_graph hb_graph;
+
+/* A CSR graph held by the caller (host memory): offsets[num_nodes + 1],
+ * successors[num_arcs]; each successor list sorted ascending. This replaces
+ * the reference's `G1: RandomAccessGraph` / `G2` transpose parameters and the
+ * cumulative outdegree `D: Succ` (the offsets are that cumulative function). */
+typedef struct hb_graph_view {
+    uint64_t num_nodes;
+    uint64_t num_arcs;
+    const uint64_t* offsets;
+    const uint32_t* successors;
+} hb_graph_view;
+
+/* Builder parameters (reference: HyperBallBuilder fields, HB:26-56, and
+ * HyperLogLogBuilder, HLL:234-251). Initialise with hb_options_default. */
+typedef struct hb_options {
+    uint32_t struct_size;     /* sizeof(hb_options) */
+    int32_t log2m;            /* log2 of registers per counter, >= 4 (HLL:379-383); default 4 */
+    int32_t hash_kind;        /* HB_HASH_*; default HB_HASH_SIP13 */
+    int32_t device;           /* CUDA device ordinal; default 0 */
+    uint64_t hash_seed;       /* seed of HB_HASH_JENKINS */
+    uint64_t num_elements;    /* HLL upper bound on elements; 0 = num_nodes (or sum of weights) (HLL:346-350) */
+    uint32_t flags;           /* HB_* flags above */
+    uint32_t reserved0;
+    uint64_t arc_granularity; /* accepted for parity with HB:280-283; 0 = 16 Ki. The device balances work by degree buckets. */
+    const uint64_t* weights;  /* optional node weights, host array of num_nodes (HB:286-290); NULL = all 1 */
+    uint64_t weight_seed;     /* seeds the values added for weights (the reference uses a non-reproducible RNG, HB:1167-1174) */
+    void* stream;             /* cudaStream_t to launch on; NULL = legacy default stream */
+    uint32_t small_max_degree;  /* tuning: nodes up to this out-degree run one lane-group each; HB_AUTO = tuned default */
+    uint32_t medium_max_degree; /* tuning: nodes up to this out-degree run one warp each, above: one CTA; HB_AUTO = tuned default */
+} hb_options;
+
+/* Per-iteration statistics (reference: the progress-logger lines of
+ * iterate(), HB:782-942). */
+typedef struct hb_iter_stats {
+    uint64_t iteration;          /* 1-based */
+    uint64_t modified_counters;  /* HB:899-905 */
+    uint64_t visited_arcs;       /* arcs (u,v), u != v, v modified in the previous iteration */
+    uint64_t scanned_nodes;      /* nodes whose successors were enumerated */
+    double neighborhood_function;/* value appended to the neighbourhood function */
+    double relative_increment;   /* HB:929-941 */
+    int32_t systolic, local, pre_local, reserved;
+    double union_ms;             /* device time of the union kernels of this iteration */
+    double iteration_ms;         /* device time of the whole iteration */
+} hb_iter_stats;
+
+/* Discount function: weight of distance d >= 1 (reference: the closures of
+ * HyperBallBuilder::discount_function, HB:291-297). Called on the host once
+ * per iteration with d = iteration + 1. */
+typedef double (*hb_discount_fn)(uint64_t distance, void* ctx);
+
+/* ---- lifecycle ------------------------------------------------------------ */
+
+/* Fills defaults (log2m 4, SipHash-1-3, no optional outputs). */
+void hb_options_default(hb_options* opts);
+
+/* Builds a device-resident HyperBall instance.
+ * Replaces HyperBallBuilder::with_hyper_log_log (HB:91-133), ::new (HB:152-181),
+ * ::with_transpose (HB:204-256), the setters (HB:259-303) and ::build (HB:321-403).
+ * `transpose` may be NULL; with HB_TRANSPOSE_ON_DEVICE the transpose is built on
+ * the GPU instead. Without any transpose no systolic iteration runs (HB:795-796). */
+int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const hb_options* opts,
+              hb_handle** out);
+
+/* Adds a discount function (HB:291-297); call before the first run. */
+int hb_add_discount_function(hb_handle* h, hb_discount_fn fn, void* ctx);
+
+/* Frees every device and host resource of the handle. */
+void hb_destroy(hb_handle* h);
+
+/* ---- running (reference: HyperBall::run*, HB:534-621) --------------------- */
+
+/* HyperBall::run(upper_bound, threshold) (HB:534-583): init, then iterate until
+ * no counter changes, `upper_bound` (capped at num_nodes) iterations ran, or, when
+ * `threshold` is not NaN, the relative increment after the fifth iteration is
+ * below 1 + threshold. */
+int hb_run(hb_handle* h, uint64_t upper_bound, double threshold);
+
+/* HyperBall::run_until_stable(upper_bound) (HB:595-603). */
+int hb_run_until_stable(hb_handle* h, uint64_t upper_bound);
+
+/* HyperBall::run_until_done() (HB:614-621). */
+int hb_run_until_done(hb_handle* h);
+
+/* Step-wise driving, as the reference's in-crate test does with init() and
+ * iterate() (HB:1155-1213, HB:775-949). `out` may be NULL. */
+int hb_init(hb_handle* h);
+int hb_iterate(hb_handle* h, hb_iter_stats* out);
+
+/* Number of completed iterations and the statistics of iteration i (0-based). */
+uint64_t hb_num_iterations(const hb_handle* h);
+int hb_get_iteration_stats(const hb_handle* h, uint64_t i, hb_iter_stats* out);
+
+/* ---- results (reference: accessors, HB:633-757) ---------------------------- */
+
+/* neighborhood_function() (HB:633-636): iterations + 1 values. Writes
+ * min(capacity, len) values and stores len in *len. */
+int hb_get_neighborhood_function(const hb_handle* h, double* dst, size_t capacity, size_t* len);
+/* sum_of_distances() (HB:639-647); len must be num_nodes. */
+int hb_get_sum_of_distances(const hb_handle* h, double* dst, size_t len);
+/* harmonic_centralities() (HB:650-657). */
+int hb_get_harmonic_centralities(const hb_handle* h, double* dst, size_t len);
+/* discounted_centrality(index) (HB:663-671). */
+int hb_get_discounted_centrality(const hb_handle* h, size_t index, double* dst, size_t len);
+/* closeness_centrality() (HB:674-686): 1/d, 0 when d == 0. */
+int hb_get_closeness_centrality(const hb_handle* h, double* dst, size_t len);
+/* lin_centrality() (HB:691-712): count^2/d, 1 when d == 0. */
+int hb_get_lin_centrality(const hb_handle* h, double* dst, size_t len);
+/* nieminen_centrality() (HB:715-732): count^2 - d. */
+int hb_get_nieminen_centrality(const hb_handle* h, double* dst, size_t len);
+/* reachable_nodes() (HB:750-757). */
+int hb_get_reachable_nodes(const hb_handle* h, double* dst, size_t len);
+/* reachable_nodes_from(node) (HB:739-745). */
+int hb_reachable_nodes_from(const hb_handle* h, uint64_t node, double* out);
+
+/* Raw counter words of the current or next state, in the reference layout
+ * (SliceCounterArray, src/utils/slice_counter_array.rs:166-169: counter i at
+ * bytes [i*B, (i+1)*B), B = 2^log2m * 5 / 8, 5-bit registers packed LSB-first
+ * in little-endian words). `bytes` must be num_nodes * B. */
+int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes);
+
+/* Counter size in bytes and register width (HLL:301-303). */
+int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* register_size);
+
+/* Last error of a handle (never NULL). */
+const char* hb_last_error(const hb_handle* h);
+/* Last error of calls without a handle, per thread (never NULL). */
+const char* hb_global_last_error(void);
+
+/* ---- graphs: BVGraph input and synthetic workloads ------------------------- */
+
+/* Decodes a BVGraph (basename.graph/.properties[/.offsets]) into host CSR.
+ * Replaces webgraph's BvGraph::with_basename(..).load() as used at
+ * src/main.rs:56-58 and tests/test_hyperball.rs:226-227. */
+int hb_graph_load_bvgraph(const char* basename, hb_graph** out);
+/* Directed out-regular Erdős–Rényi: d distinct uniform non-loop successors per node. */
+int hb_graph_generate_er(uint64_t num_nodes, uint32_t d, uint64_t seed, hb_graph** out);
+/* R-MAT with 2^scale nodes and edges_per_node * 2^scale drawn arcs, deduplicated, loop free. */
+int hb_graph_generate_rmat(int scale, uint64_t edges_per_node, double a, double b, double c,
+                           uint64_t seed, hb_graph** out);
+/* Web-like: Zipf–Mandelbrot out-degrees (exponent 2.1, shift, capped), 4/5 of
+ * successors within +-window of the source, 1/5 uniform. */
+int hb_graph_generate_weblike(uint64_t num_nodes, uint64_t cap, double shift, uint64_t window,
+                              uint64_t seed, hb_graph** out);
+/* Host transpose (sorted rows). */
+int hb_graph_transpose(const hb_graph* g, hb_graph** out);
+/* Wraps caller arrays by copying them into a new graph. */
+int hb_graph_from_csr(const hb_graph_view* view, hb_graph** out);
+/* Borrowed view of a graph's arrays (valid until hb_graph_free). */
+hb_graph_view hb_graph_get_view(const hb_graph* g);
+void hb_graph_free(hb_graph* g);
+
+/* ---- introspection ---------------------------------------------------------- */
+/* Library build string, e.g. "hyperball_gb300 sm_103a". */
+const char* hb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYPERBALL_GB300_H */

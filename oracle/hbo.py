@@ -1,0 +1,241 @@
+"""ctypes wrapper of the CPU oracle library — test infrastructure only.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as
+the checker; the product never imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_P = ctypes.POINTER
+_lib = None
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("iteration", ctypes.c_uint64),
+        ("modified", ctypes.c_uint64),
+        ("visited_arcs", ctypes.c_uint64),
+        ("nf", ctypes.c_double),
+        ("relative_increment", ctypes.c_double),
+        ("systolic", ctypes.c_int32),
+        ("local", ctypes.c_int32),
+        ("pre_local", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+DISCOUNT_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle.build()
+        L = ctypes.CDLL(build_oracle.LIB)
+        V = ctypes.c_void_p
+        sig = {
+            "hbo_create": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                               _P(ctypes.c_uint64), _P(ctypes.c_uint32), ctypes.c_int,
+                               ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                               _P(ctypes.c_uint64), ctypes.c_uint64]),
+            "hbo_add_discount": (ctypes.c_int, [V, DISCOUNT_FN, V]),
+            "hbo_destroy": (None, [V]),
+            "hbo_init": (ctypes.c_int, [V]),
+            "hbo_iterate": (ctypes.c_int, [V, _P(Stats)]),
+            "hbo_run": (ctypes.c_int, [V, ctypes.c_uint64, ctypes.c_double, ctypes.c_int]),
+            "hbo_iteration": (ctypes.c_uint64, [V]),
+            "hbo_words_per_counter": (ctypes.c_uint64, [V]),
+            "hbo_word_bytes": (ctypes.c_int, [V]),
+            "hbo_last_stats": (None, [V, _P(Stats)]),
+            "hbo_get_array": (None, [V, ctypes.c_int, V]),
+            "hbo_nf_len": (ctypes.c_uint64, [V]),
+            "hbo_get_nf": (None, [V, _P(ctypes.c_double)]),
+            "hbo_get_sod": (ctypes.c_int, [V, _P(ctypes.c_double)]),
+            "hbo_get_harm": (ctypes.c_int, [V, _P(ctypes.c_double)]),
+            "hbo_get_discounted": (ctypes.c_int, [V, ctypes.c_uint64, _P(ctypes.c_double)]),
+            "hbo_get_reachable": (None, [V, ctypes.c_uint64, _P(ctypes.c_double)]),
+            "hbo_seq_create": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_int]),
+            "hbo_seq_init": (None, [V]),
+            "hbo_seq_iterate": (None, [V]),
+            "hbo_seq_get_array": (None, [V, ctypes.c_int, V]),
+            "hbo_seq_destroy": (None, [V]),
+            "hbo_hash": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64]),
+            "hbo_siphash": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                              ctypes.c_uint64, ctypes.c_char_p, ctypes.c_uint64]),
+            "hbo_register_size": (ctypes.c_int, [ctypes.c_uint64]),
+            "hbo_hll_merge": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, V, V]),
+            "hbo_hll_count": (ctypes.c_double, [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, V,
+                                                ctypes.c_int]),
+            "hbo_hll_add": (None, [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_uint64, V, ctypes.c_uint64]),
+            "hbo_hll_add_hash": (None, [ctypes.c_int, ctypes.c_uint64, V, ctypes.c_uint64]),
+            "hbo_hll_params": (None, [ctypes.c_int, ctypes.c_uint64, _P(ctypes.c_double),
+                                      _P(ctypes.c_uint64)]),
+            "hbo_last_error": (ctypes.c_char_p, []),
+            "hbo_hll_count_hashes": (ctypes.c_double, [ctypes.c_int, ctypes.c_uint64,
+                                                       _P(ctypes.c_uint64), ctypes.c_uint64,
+                                                       _P(ctypes.c_uint64), ctypes.c_uint64]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(L, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def word_bits_for(log2m):
+    """Widest word the reference's `ensure!` (HLL:399-403) accepts."""
+    bits = (1 << log2m) * 5
+    for w in (64, 32, 16):
+        if bits % w == 0:
+            return w
+    return 16
+
+
+SOD, HARM, NO_QUIRK = 1, 2, 4
+
+
+class OracleHyperBall:
+    """The reference HyperBall restated on the CPU (oracle/hyperball_oracle.cpp)."""
+
+    def __init__(self, offsets, successors, log2m, hash_kind=0, seed=0, t_offsets=None,
+                 t_successors=None, sod=False, harm=False, threads=1, granularity=0,
+                 num_elements=0, word_bits=None, quirk=True, weights=None, weight_seed=0,
+                 discounts=()):
+        L = lib()
+        self._off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._suc = np.ascontiguousarray(successors, dtype=np.uint32)
+        self.n = len(self._off) - 1
+        self._toff = None if t_offsets is None else np.ascontiguousarray(t_offsets, dtype=np.uint64)
+        self._tsuc = None if t_successors is None else np.ascontiguousarray(t_successors, dtype=np.uint32)
+        self._w = None if weights is None else np.ascontiguousarray(weights, dtype=np.uint64)
+        wb = word_bits or word_bits_for(log2m)
+        flags = (SOD if sod else 0) | (HARM if harm else 0) | (0 if quirk else NO_QUIRK)
+        p = lambda a, t: a.ctypes.data_as(_P(t)) if a is not None else None
+        self._h = L.hbo_create(self.n, p(self._off, ctypes.c_uint64), p(self._suc, ctypes.c_uint32),
+                               p(self._toff, ctypes.c_uint64), p(self._tsuc, ctypes.c_uint32),
+                               log2m, hash_kind, seed, num_elements, wb, flags, threads,
+                               granularity, p(self._w, ctypes.c_uint64), weight_seed)
+        if not self._h:
+            raise ValueError(L.hbo_last_error().decode())
+        self._cbs = []
+        for fn in discounts:
+            cb = DISCOUNT_FN(lambda d, _c, f=fn: float(f(int(d))))
+            self._cbs.append(cb)
+            L.hbo_add_discount(self._h, cb, None)
+        self.counter_bytes = (1 << log2m) * 5 // 8
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hbo_destroy(self._h)
+            self._h = None
+
+    def init(self):
+        lib().hbo_init(self._h)
+
+    def iterate(self):
+        s = Stats()
+        lib().hbo_iterate(self._h, ctypes.byref(s))
+        return s.as_dict()
+
+    def run(self, upper_bound=2**64 - 1, threshold=None):
+        lib().hbo_run(self._h, upper_bound, 0.0 if threshold is None else threshold,
+                      0 if threshold is None else 1)
+
+    def run_until_done(self):
+        self.run()
+
+    @property
+    def iteration(self):
+        return int(lib().hbo_iteration(self._h))
+
+    def registers(self, which=0):
+        out = np.zeros((self.n, self.counter_bytes), dtype=np.uint8)
+        lib().hbo_get_array(self._h, which, out.ctypes.data)
+        return out
+
+    def neighborhood_function(self):
+        k = lib().hbo_nf_len(self._h)
+        out = np.zeros(k, dtype=np.float64)
+        lib().hbo_get_nf(self._h, out.ctypes.data_as(_P(ctypes.c_double)))
+        return out
+
+    def sum_of_distances(self):
+        out = np.zeros(self.n, dtype=np.float64)
+        if lib().hbo_get_sod(self._h, out.ctypes.data_as(_P(ctypes.c_double))) != 0:
+            raise ValueError("sum of distances not requested")
+        return out
+
+    def harmonic_centralities(self):
+        out = np.zeros(self.n, dtype=np.float64)
+        if lib().hbo_get_harm(self._h, out.ctypes.data_as(_P(ctypes.c_double))) != 0:
+            raise ValueError("harmonic centralities not requested")
+        return out
+
+    def discounted_centrality(self, i):
+        out = np.zeros(self.n, dtype=np.float64)
+        if lib().hbo_get_discounted(self._h, i, out.ctypes.data_as(_P(ctypes.c_double))) != 0:
+            raise ValueError("no such discount function")
+        return out
+
+    def reachable_nodes(self):
+        out = np.zeros(self.n, dtype=np.float64)
+        lib().hbo_get_reachable(self._h, self.n, out.ctypes.data_as(_P(ctypes.c_double)))
+        return out
+
+    # derived accessors, HB:674-732
+    def closeness_centrality(self):
+        d = self.sum_of_distances()
+        with np.errstate(divide="ignore"):
+            return np.where(d == 0.0, 0.0, 1.0 / np.where(d == 0.0, 1.0, d))
+
+    def lin_centrality(self):
+        d = self.sum_of_distances()
+        c = self.reachable_nodes()
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return np.where(d == 0.0, 1.0, c * c / np.where(d == 0.0, 1.0, d))
+
+    def nieminen_centrality(self):
+        d = self.sum_of_distances()
+        c = self.reachable_nodes()
+        return (c * c) - d
+
+
+class SeqHyperBall:
+    """SeqHyperBall of HB:1230-1261 (merges every successor, no modes)."""
+
+    def __init__(self, offsets, successors, log2m, hash_kind=0, seed=0):
+        L = lib()
+        self._off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._suc = np.ascontiguousarray(successors, dtype=np.uint32)
+        self.n = len(self._off) - 1
+        self.counter_bytes = (1 << log2m) * 5 // 8
+        self._h = L.hbo_seq_create(self.n, self._off.ctypes.data_as(_P(ctypes.c_uint64)),
+                                   self._suc.ctypes.data_as(_P(ctypes.c_uint32)), log2m, hash_kind,
+                                   seed, word_bits_for(log2m))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hbo_seq_destroy(self._h)
+            self._h = None
+
+    def init(self):
+        lib().hbo_seq_init(self._h)
+
+    def iterate(self):
+        lib().hbo_seq_iterate(self._h)
+
+    def registers(self, which=0):
+        out = np.zeros((self.n, self.counter_bytes), dtype=np.uint8)
+        lib().hbo_seq_get_array(self._h, which, out.ctypes.data)
+        return out

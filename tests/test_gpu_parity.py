@@ -1,0 +1,159 @@
+"""GPU parity: the CUDA HyperBall against the CPU oracle, iteration by iteration.
+
+Bit-exact counters (both arrays), identical modified / visited counts and
+modes, neighbourhood function and per-node sums within 1e-12 relative.
+"""
+import numpy as np
+import pytest
+
+from conftest import cnr_basename, cnr_result
+from parity import assert_close, lockstep
+
+pytestmark = pytest.mark.gpu
+
+
+def test_er_1e4_log2m6_systolic(hb, oracle):
+    """The CPU-runnable config: ER n=10^4, 8 successors, SplitMix64 seed 0, log2m 6."""
+    g = hb.Graph.erdos_renyi(10_000, 8, 0)
+    t = g.transpose()
+    gpu, orc, stats = lockstep(hb, oracle, g, 6, transpose=t)
+    assert any(sg["systolic"] for sg, _ in stats), "systolic iterations expected"
+
+
+def test_er_1e4_log2m6_standard_only(hb, oracle):
+    g = hb.Graph.erdos_renyi(10_000, 8, 0)
+    gpu, orc, stats = lockstep(hb, oracle, g, 6)
+    assert not any(sg["systolic"] for sg, _ in stats)
+
+
+@pytest.mark.parametrize("log2m", [4, 5, 7, 8, 9, 10])
+def test_er_log2m(hb, oracle, log2m):
+    g = hb.Graph.erdos_renyi(3000, 5, 11 + log2m)
+    lockstep(hb, oracle, g, log2m, transpose=g.transpose())
+
+
+@pytest.mark.parametrize("log2m", [4, 6, 8])
+def test_jenkins_hash(hb, oracle, log2m):
+    g = hb.Graph.erdos_renyi(4000, 6, 3)
+    lockstep(hb, oracle, g, log2m, hash_kind=1, seed=42, transpose=g.transpose())
+
+
+def test_transpose_on_device(hb, oracle):
+    g = hb.Graph.rmat(12, 8, seed=5)
+    lockstep(hb, oracle, g, 6, transpose_on_device=True)
+
+
+@pytest.mark.parametrize("buckets", [(0, 0), (1, 2), (4, 16), (1 << 30, 1 << 30)])
+def test_degree_buckets(hb, oracle, buckets):
+    """Every node through the group, warp or CTA path gives the same counters."""
+    g = hb.Graph.weblike(20_000, cap=3000, window=64, seed=7)
+    lockstep(hb, oracle, g, 6, transpose=g.transpose(), buckets=buckets)
+
+
+def test_heavy_hub(hb, oracle):
+    """A hub with thousands of successors goes through the CTA path (log2m 8)."""
+    n = 6000
+    rng = np.random.default_rng(0)
+    rows = []
+    for v in range(n):
+        if v == 17:
+            s = np.arange(n, dtype=np.uint32)  # includes a self-loop
+        else:
+            s = np.unique(rng.integers(0, n, size=rng.integers(0, 5)).astype(np.uint32))
+        rows.append(s)
+    off = np.zeros(n + 1, dtype=np.uint64)
+    off[1:] = np.cumsum([len(r) for r in rows])
+    g = hb.Graph.from_csr(off, np.concatenate(rows))
+    lockstep(hb, oracle, g, 8, transpose=g.transpose(), buckets=(4, 64))
+
+
+def test_discount_functions(hb, oracle):
+    g = hb.Graph.erdos_renyi(2000, 4, 9)
+    lockstep(hb, oracle, g, 6, transpose=g.transpose(),
+             discounts=(lambda d: 1.0 / (d * d), lambda d: 0.5 ** d))
+
+
+def test_edge_cases(hb, oracle):
+    # one node with a self-loop
+    g = hb.Graph.from_csr(np.array([0, 1], dtype=np.uint64), np.array([0], dtype=np.uint32))
+    lockstep(hb, oracle, g, 6)
+    # no arcs at all
+    g = hb.Graph.from_csr(np.zeros(51, dtype=np.uint64), np.zeros(0, dtype=np.uint32))
+    lockstep(hb, oracle, g, 4, transpose=g.transpose())
+    # a path: many iterations, ragged sizes (n not a multiple of 32)
+    n = 77
+    off = np.concatenate([np.arange(n, dtype=np.uint64), [n - 1]]).astype(np.uint64)
+    g = hb.Graph.from_csr(off, np.arange(1, n, dtype=np.uint32))
+    lockstep(hb, oracle, g, 5, transpose=g.transpose())
+
+
+def test_run_api_matches_oracle(hb, oracle):
+    g = hb.Graph.erdos_renyi(5000, 8, 0)
+    t = g.transpose()
+    logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(6).build()
+    gpu = (hb.HyperBallBuilder.with_transpose(g, t, logic)
+           .sum_of_distances(True).sum_of_inverse_distances(True).build())
+    orc = oracle.OracleHyperBall(g.offsets, g.successors, 6, t_offsets=t.offsets,
+                                 t_successors=t.successors, sod=True, harm=True)
+    # upper bound and threshold stops (HB:541, HB:572-577)
+    for ub, thr in ((3, None), (1000, 0.01), (1000, None)):
+        gpu.run(ub, thr)
+        orc.run(ub, thr)
+        assert gpu.iteration == orc.iteration
+        np.testing.assert_array_equal(gpu.registers(), orc.registers())
+        assert_close(gpu.neighborhood_function(), orc.neighborhood_function(), 1e-12, "nf")
+        for name in ("sum_of_distances", "harmonic_centralities", "closeness_centrality",
+                     "lin_centrality", "nieminen_centrality", "reachable_nodes"):
+            assert_close(getattr(gpu, name)(), getattr(orc, name)(), 1e-12, name)
+
+
+def test_errors(hb):
+    g = hb.Graph.erdos_renyi(100, 3, 1)
+    logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(6).build()
+    h = hb.HyperBallBuilder.new(g, logic).build()
+    with pytest.raises(hb.NotRunError):
+        h.neighborhood_function()
+    h.run_until_done()
+    with pytest.raises(hb.NotRequestedError):
+        h.sum_of_distances()
+    with pytest.raises(hb.NotRequestedError):
+        h.discounted_centrality(0)
+    bad = hb.Graph.from_csr(np.array([0, 1], dtype=np.uint64), np.array([5], dtype=np.uint32))
+    with pytest.raises(hb.InvalidArgumentError):
+        hb.HyperBallBuilder.new(bad, logic).build()
+
+
+@pytest.mark.skipif(cnr_basename() is None, reason="cnr-2000 fixture not present")
+def test_cnr2000_java_goldens(hb, oracle):
+    """tests/test_hyperball.rs:221-302 on the GPU: log2m 8, Jenkins(42), to
+    stabilisation; five centralities within 1e-6 of the Java results."""
+    g = hb.Graph.load_bvgraph(cnr_basename())
+    gt = hb.Graph.load_bvgraph(cnr_basename(transpose=True))
+    logic = (hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(8)
+             .build_hasher(hb.JenkinsHasher(42)).build())
+    h = (hb.HyperBallBuilder.with_transpose(g, gt, logic)
+         .sum_of_distances(True).sum_of_inverse_distances(True).build())
+    h.run_until_done()
+    for name, fn in (("sum_of_distances", h.sum_of_distances),
+                     ("harmonic_centrality", h.harmonic_centralities),
+                     ("lin_centrality", h.lin_centrality),
+                     ("closeness_centrality", h.closeness_centrality),
+                     ("nieminen_centrality", h.nieminen_centrality)):
+        p = cnr_result(name)
+        if p is None:
+            pytest.skip("Java golden results not present")
+        exp = np.fromfile(p, dtype=">f4").astype(np.float64)
+        act = fn()
+        d = np.abs(exp - act)
+        rel = np.where(exp != 0, d / np.where(exp != 0, exp, 1.0), d)
+        assert rel.max() < 1e-6, f"{name}: max rel {rel.max()}"
+
+
+@pytest.mark.skipif(cnr_basename() is None, reason="cnr-2000 fixture not present")
+def test_cnr2000_lockstep_log2m6(hb, oracle):
+    """The reference's in-crate test (HB:1263-1322): cnr-2000, log2m 6, default
+    hasher, systolic and local modes, both arrays checked every iteration."""
+    g = hb.Graph.load_bvgraph(cnr_basename())
+    gt = hb.Graph.load_bvgraph(cnr_basename(transpose=True))
+    _, _, stats = lockstep(hb, oracle, g, 6, transpose=gt, sod=False, harm=False)
+    assert any(sg["local"] for sg, _ in stats)

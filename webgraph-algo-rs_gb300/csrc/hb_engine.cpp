@@ -1,0 +1,875 @@
+// Host engine and C ABI of the GB300 HyperBall.
+//
+// The control flow restates HyperBall::iterate / run
+// (src/algo/hyperball/hyperball_impl.rs:534-949) over device-resident state:
+//   * mode choice with the reference's integer thresholds (HB:795-810):
+//     systolic iff a transpose exists, iteration > 0 and modified < n/4;
+//     local / pre_local as in the reference (reported; on the device the
+//     local checklist is the must-be-checked bitmap);
+//   * neighbourhood function: standard iterations sum every scanned node's
+//     count, systolic ones add (post - pre) to the previous unclamped value,
+//     then the monotone clamp and relative increment (HB:916-944);
+//   * termination exactly as run() (HB:541-577).
+// Device layout (HBM): CSR offsets u64[n+1], successors u32[m], optional
+// transpose CSR, two counter arrays n*B bytes (B = 2^log2m*5/8, reference
+// layout), cached counts f64[n], the optional per-node sums f64[n], four
+// n-bit bitmaps (modified current/next, must-be-checked current/next).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "hb_internal.h"
+
+namespace {
+
+thread_local std::string g_global_err;
+
+constexpr double LN_2 = 0.693147180559945309417232121458176568;
+
+uint64_t rust_f64_to_u64(double x) {
+    if (!(x > 0.0)) return 0;
+    if (x >= 18446744073709551616.0) return UINT64_MAX;
+    return (uint64_t)x;
+}
+
+// hyper_log_log_logic.rs:301-303
+int register_size(uint64_t n) {
+    double v = std::log((std::log((double)n) / LN_2) / LN_2);
+    uint64_t c = rust_f64_to_u64(std::ceil(v));
+    return (int)std::max<uint64_t>(5, c);
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct hb_graph {
+    Csr g;
+};
+
+struct hb_handle {
+    // configuration
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t n = 0, m = 0;
+    int log2m = 4;
+    uint64_t counter_bytes = 0;
+    int hash_kind = HB_HASH_SIP13;
+    uint64_t hash_seed = 0;
+    uint64_t num_elements = 0;
+    bool do_sod = false, do_harm = false, quirk = true;
+    bool has_transpose = false;
+    uint64_t arc_granularity = 16 * 1024;
+    uint32_t small_max = 0, medium_max = 0;
+    double alpha_m_m = 0.0;
+    std::vector<hb_discount_fn> disc_fn;
+    std::vector<void*> disc_ctx;
+    uint64_t weight_seed = 0;
+    bool has_weights = false;
+
+    // device state
+    std::vector<DevBuf> bufs;
+    uint64_t* d_off = nullptr;
+    uint32_t* d_succ = nullptr;
+    uint64_t* d_toff = nullptr;
+    uint32_t* d_tsucc = nullptr;
+    uint8_t* d_cnt[2] = {nullptr, nullptr};
+    uint32_t* d_bits[4] = {nullptr, nullptr, nullptr, nullptr};  // curr_mod, next_mod, mbc, next_mbc
+    double* d_est = nullptr;
+    double* d_sod = nullptr;
+    double* d_harm = nullptr;
+    std::vector<double*> d_disc;
+    double* d_lnt = nullptr;
+    uint64_t* d_weights = nullptr;
+    uint32_t* d_medium = nullptr;
+    uint32_t* d_heavy = nullptr;
+    uint64_t n_medium = 0, n_heavy = 0;
+    unsigned long long* d_stats = nullptr;  // 4 counters
+    double* d_nf_partials = nullptr;
+    double* d_nf_out = nullptr;
+    int grid_group = 1, grid_warp = 1, grid_cta = 1;
+    int nf_slots = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    // reference state (IterationContext + HyperBall fields)
+    int cur = 0;         // index of the current counter array
+    int mod_cur = 0;     // d_bits[mod_cur] = curr_mod, d_bits[mod_cur ^ 1] = next_mod
+    int mbc_cur = 2;     // d_bits[mbc_cur] = mbc, d_bits[mbc_cur ^ 1] = next_mbc
+    uint64_t iteration = 0;
+    bool systolic = false, local = false, pre_local = false;
+    uint64_t modified_counters = 0;
+    double last = 0.0, relative_increment = 0.0;
+    std::vector<double> nf;
+    std::vector<hb_iter_stats> stats;
+    bool initialised = false;
+
+    std::string err;
+};
+
+namespace {
+
+int set_err(hb_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    g_global_err = msg;
+    return code;
+}
+
+int cuda_err(hb_handle* h, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return HB_OK;
+    int code = (e == cudaErrorMemoryAllocation) ? HB_ERR_OOM
+               : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? HB_ERR_NO_DEVICE
+                                                                               : HB_ERR_CUDA;
+    return set_err(h, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define HB_CUDA(h, call)                                          \
+    do {                                                          \
+        cudaError_t _e = (call);                                  \
+        if (_e != cudaSuccess) return cuda_err((h), _e, #call);   \
+    } while (0)
+
+#define HB_LAUNCH(h, call)                                                    \
+    do {                                                                      \
+        int _e = (call);                                                      \
+        if (_e != 0) return cuda_err((h), (cudaError_t)_e, #call);            \
+    } while (0)
+
+template <class T>
+int dalloc(hb_handle* h, T** out, size_t count) {
+    *out = nullptr;
+    size_t bytes = std::max<size_t>(count * sizeof(T), 256);
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_err(h, e, "cudaMalloc");
+    }
+    h->bufs.push_back({p, bytes});
+    *out = (T*)p;
+    return HB_OK;
+}
+
+void release(hb_handle* h) {
+    if (!h) return;
+    for (auto& b : h->bufs) cudaFree(b.p);
+    h->bufs.clear();
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+}
+
+bool check_view(const hb_graph_view* g, std::string& why) {
+    if (!g) {
+        why = "graph is NULL";
+        return false;
+    }
+    if (g->num_nodes > 0xffffffffull) {
+        why = "more than 2^32 nodes do not fit u32 successors";
+        return false;
+    }
+    if (!g->offsets) {
+        why = "offsets is NULL";
+        return false;
+    }
+    if (g->num_arcs > 0 && !g->successors) {
+        why = "successors is NULL";
+        return false;
+    }
+    if (g->offsets[0] != 0 || g->offsets[g->num_nodes] != g->num_arcs) {
+        why = "offsets[0] must be 0 and offsets[num_nodes] must equal num_arcs";
+        return false;
+    }
+    return true;
+}
+
+int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t** d_succ) {
+    int r;
+    if ((r = dalloc(h, d_off, g->num_nodes + 1))) return r;
+    if ((r = dalloc(h, d_succ, g->num_arcs))) return r;
+    HB_CUDA(h, cudaMemcpyAsync(*d_off, g->offsets, (g->num_nodes + 1) * 8, cudaMemcpyHostToDevice,
+                               h->stream));
+    if (g->num_arcs)
+        HB_CUDA(h, cudaMemcpyAsync(*d_succ, g->successors, g->num_arcs * 4, cudaMemcpyHostToDevice,
+                                   h->stream));
+    // reject out-of-range successors before any kernel indexes with them
+    int* d_bad = nullptr;
+    if ((r = dalloc(h, &d_bad, 1))) return r;
+    HB_CUDA(h, cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream));
+    HB_LAUNCH(h, hbk::launch_validate(*d_off, *d_succ, g->num_nodes, g->num_arcs, d_bad, h->stream));
+    int bad = 0;
+    HB_CUDA(h, cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (bad) return set_err(h, HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
+    return HB_OK;
+}
+
+int build_transpose_on_device(hb_handle* h) {
+    const uint64_t n = h->n, m = h->m;
+    int r;
+    unsigned long long* indeg = nullptr;
+    if ((r = dalloc(h, &indeg, n + 1))) return r;
+    if ((r = dalloc(h, &h->d_toff, n + 1))) return r;
+    if ((r = dalloc(h, &h->d_tsucc, m))) return r;
+    const uint64_t sl = hbk::scan_scratch_len(n + 1);
+    unsigned long long* scratch = nullptr;
+    if ((r = dalloc(h, &scratch, sl))) return r;
+    HB_CUDA(h, cudaMemsetAsync(indeg, 0, (n + 1) * 8, h->stream));
+    HB_LAUNCH(h, hbk::launch_transpose_count(h->d_succ, m, indeg, h->stream));
+    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(indeg, h->d_toff, n + 1, scratch, sl, h->stream));
+    // reuse indeg as the scatter cursor
+    HB_CUDA(h, cudaMemcpyAsync(indeg, h->d_toff, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    HB_LAUNCH(h, hbk::launch_transpose_scatter(h->d_off, h->d_succ, n, indeg, h->d_tsucc, h->stream));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    // temporaries are released right away
+    for (auto it = h->bufs.begin(); it != h->bufs.end();) {
+        if (it->p == (void*)indeg || it->p == (void*)scratch) {
+            cudaFree(it->p);
+            it = h->bufs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    h->has_transpose = true;
+    return HB_OK;
+}
+
+hbk::UnionArgs union_args(hb_handle* h) {
+    hbk::UnionArgs a{};
+    a.off = h->d_off;
+    a.succ = h->d_succ;
+    a.curr = h->d_cnt[h->cur];
+    a.next = h->d_cnt[h->cur ^ 1];
+    a.curr_mod = h->d_bits[h->mod_cur];
+    a.next_mod = h->d_bits[h->mod_cur ^ 1];
+    a.mbc = h->d_bits[h->mbc_cur];
+    a.est = h->d_est;
+    a.sod = h->d_sod;
+    a.harm = h->d_harm;
+    a.ndisc = (int)h->d_disc.size();
+    for (int k = 0; k < a.ndisc; k++) {
+        a.disc[k] = h->d_disc[k];
+        a.disc_factor[k] = h->disc_fn[k](h->iteration + 1, h->disc_ctx[k]);
+    }
+    a.systolic = h->systolic ? 1 : 0;
+    a.quirk = h->quirk ? 1 : 0;
+    a.iter = (uint32_t)h->iteration;
+    a.n = h->n;
+    a.alpha_m_m = h->alpha_m_m;
+    a.ln_table = h->d_lnt;
+    a.small_max_degree = h->small_max;
+    a.stats_out = h->d_stats;
+    return a;
+}
+
+int do_init(hb_handle* h) {
+    const uint64_t n = h->n;
+    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[0], 0, n * h->counter_bytes, h->stream));
+    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[1], 0, n * h->counter_bytes, h->stream));
+    h->cur = 0;
+    h->mod_cur = 0;
+    h->mbc_cur = 2;
+    hbk::InitArgs ia{};
+    ia.curr = h->d_cnt[0];
+    ia.est = h->d_est;
+    ia.n = n;
+    ia.hash_kind = h->hash_kind;
+    ia.seed = h->hash_seed;
+    ia.weights = h->d_weights;
+    ia.weight_seed = h->weight_seed;
+    ia.alpha_m_m = h->alpha_m_m;
+    ia.ln_table = h->d_lnt;
+    ia.quirk = h->quirk ? 1 : 0;
+    if (n) HB_LAUNCH(h, hbk::launch_init(h->log2m, ia, h->stream));
+    if (h->d_sod) HB_CUDA(h, cudaMemsetAsync(h->d_sod, 0, n * 8, h->stream));
+    if (h->d_harm) HB_CUDA(h, cudaMemsetAsync(h->d_harm, 0, n * 8, h->stream));
+    for (double* d : h->d_disc) HB_CUDA(h, cudaMemsetAsync(d, 0, n * 8, h->stream));
+    const uint64_t words = (n + 31) / 32;
+    // curr_modified = all ones (HB:1208); bits beyond n stay zero
+    HB_LAUNCH(h, hbk::launch_fill_u32(h->d_bits[0], 0xffffffffu, words, h->stream));
+    if (n % 32) {
+        uint32_t last = (1u << (n % 32)) - 1u;
+        HB_CUDA(h, cudaMemcpyAsync(h->d_bits[0] + words - 1, &last, 4, cudaMemcpyHostToDevice,
+                                   h->stream));
+    }
+    for (int b = 1; b < 4; b++) HB_CUDA(h, cudaMemsetAsync(h->d_bits[b], 0, words * 4, h->stream));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->iteration = 0;
+    h->systolic = h->local = h->pre_local = false;
+    h->modified_counters = 0;
+    h->last = (double)n;
+    h->relative_increment = 0.0;
+    h->nf.assign(1, h->last);
+    h->stats.clear();
+    h->initialised = true;
+    return HB_OK;
+}
+
+int do_iterate(hb_handle* h, hb_iter_stats* out) {
+    const uint64_t n = h->n, m = h->m;
+    const uint64_t prev_mod = h->modified_counters;
+    const bool prev_was_systolic = h->systolic;
+    // HB:795-810
+    h->systolic = h->has_transpose && h->iteration > 0 && prev_mod < n / 4;
+    double current_nf = h->systolic ? h->last : 0.0;
+    h->local = h->pre_local;
+    h->pre_local = h->systolic && m > 0 && prev_mod < (n * n) / (m * 10);
+
+    const uint64_t words = (n + 31) / 32;
+    cudaStream_t s = h->stream;
+    HB_CUDA(h, cudaEventRecord(h->ev[0], s));
+    HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mod_cur ^ 1], 0, words * 4, s));
+    if (h->systolic) {
+        HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mbc_cur ^ 1], 0, words * 4, s));
+        if (!prev_was_systolic) {
+            // The reference scans every node in the first systolic iteration
+            // (HB:853-857); scanning the predecessors of the nodes modified in
+            // the previous iteration gives the same counters.
+            HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mbc_cur], 0, words * 4, s));
+            HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur], h->d_toff, h->d_tsucc,
+                                                h->d_bits[h->mbc_cur], n, h->grid_group, s));
+        }
+    }
+    HB_CUDA(h, cudaMemsetAsync(h->d_stats, 0, 4 * sizeof(unsigned long long), s));
+    HB_CUDA(h, cudaEventRecord(h->ev[1], s));
+
+    hbk::UnionArgs a = union_args(h);
+    int slots = 0;
+    a.nf_partials = h->d_nf_partials;
+    a.list = nullptr;
+    a.list_len = 0;
+    if (n) {
+        HB_LAUNCH(h, hbk::launch_union_group(h->log2m, a, h->grid_group, 256, s));
+        slots += h->grid_group;
+    }
+    if (h->n_medium) {
+        a.list = h->d_medium;
+        a.list_len = h->n_medium;
+        a.nf_partials = h->d_nf_partials + slots;
+        HB_LAUNCH(h, hbk::launch_union_team(h->log2m, 32, a, h->grid_warp, s));
+        slots += h->grid_warp;
+    }
+    if (h->n_heavy) {
+        a.list = h->d_heavy;
+        a.list_len = h->n_heavy;
+        a.nf_partials = h->d_nf_partials + slots;
+        HB_LAUNCH(h, hbk::launch_union_team(h->log2m, 256, a, h->grid_cta, s));
+        slots += h->grid_cta;
+    }
+    HB_CUDA(h, cudaEventRecord(h->ev[2], s));
+    if (h->systolic)
+        HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
+                                            h->d_bits[h->mbc_cur ^ 1], n, h->grid_group, s));
+    HB_LAUNCH(h, hbk::launch_reduce_nf(h->d_nf_partials, slots, h->d_nf_out, s));
+    struct {
+        unsigned long long st[4];
+        double nf;
+    } host{};
+    HB_CUDA(h, cudaMemcpyAsync(host.st, h->d_stats, sizeof(host.st), cudaMemcpyDeviceToHost, s));
+    HB_CUDA(h, cudaMemcpyAsync(&host.nf, h->d_nf_out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    HB_CUDA(h, cudaEventRecord(h->ev[3], s));
+    HB_CUDA(h, cudaStreamSynchronize(s));
+
+    // swap states (HB:909-914)
+    h->cur ^= 1;
+    h->mod_cur ^= 1;
+    if (h->systolic) h->mbc_cur ^= 1;
+
+    h->modified_counters = host.st[1];
+    current_nf += host.nf;
+    h->last = current_nf;
+    const double last_output = h->nf.back();
+    if (current_nf < last_output) current_nf = last_output;
+    h->relative_increment = current_nf / last_output;
+    h->nf.push_back(current_nf);
+    h->iteration += 1;
+
+    hb_iter_stats st{};
+    st.iteration = h->iteration;
+    st.modified_counters = host.st[1];
+    st.visited_arcs = host.st[0];
+    st.scanned_nodes = host.st[2];
+    st.neighborhood_function = current_nf;
+    st.relative_increment = h->relative_increment;
+    st.systolic = h->systolic;
+    st.local = h->local;
+    st.pre_local = h->pre_local;
+    float ms_union = 0.f, ms_all = 0.f;
+    cudaEventElapsedTime(&ms_union, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&ms_all, h->ev[0], h->ev[3]);
+    st.union_ms = ms_union;
+    st.iteration_ms = ms_all;
+    h->stats.push_back(st);
+    if (out) *out = st;
+    return HB_OK;
+}
+
+int ensure_iteration(const hb_handle* h) {
+    if (!h || h->iteration == 0)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_RUN,
+                       "HyperBall was not run. Please call hb_run before accessing computed fields");
+    return HB_OK;
+}
+
+int copy_d2h(const hb_handle* h, const void* src, void* dst, size_t bytes) {
+    hb_handle* hh = const_cast<hb_handle*>(h);
+    HB_CUDA(hh, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    HB_CUDA(hh, cudaStreamSynchronize(h->stream));
+    return HB_OK;
+}
+
+int check_len(const hb_handle* h, size_t len) {
+    if (len != h->n)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID,
+                       "output length must equal num_nodes (" + std::to_string(h->n) + ")");
+    return HB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void hb_options_default(hb_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->struct_size = sizeof(hb_options);
+    o->log2m = 4;
+    o->hash_kind = HB_HASH_SIP13;
+    o->small_max_degree = HB_AUTO;
+    o->medium_max_degree = HB_AUTO;
+}
+
+const char* hb_version(void) { return "hyperball_gb300 0.1 sm_103a"; }
+const char* hb_global_last_error(void) { return g_global_err.c_str(); }
+const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_global_err.c_str(); }
+
+int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const hb_options* opts,
+              hb_handle** out) {
+    if (!out) return set_err(nullptr, HB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    hb_options o;
+    hb_options_default(&o);
+    if (opts) {
+        if (opts->struct_size != sizeof(hb_options))
+            return set_err(nullptr, HB_ERR_INVALID, "hb_options.struct_size mismatch");
+        o = *opts;
+    }
+    std::string why;
+    if (!check_view(graph, why)) return set_err(nullptr, HB_ERR_INVALID, why);
+    if (transpose) {
+        if (!check_view(transpose, why)) return set_err(nullptr, HB_ERR_INVALID, "transpose: " + why);
+        // HB:230-238
+        if (transpose->num_nodes != graph->num_nodes)
+            return set_err(nullptr, HB_ERR_INVALID,
+                           "the transpose should have same number of nodes of the graph");
+        if (transpose->num_arcs != graph->num_arcs)
+            return set_err(nullptr, HB_ERR_INVALID,
+                           "the transpose should have same number of arcs of the graph");
+    }
+    // HLL:379-383
+    if (o.log2m < 4)
+        return set_err(nullptr, HB_ERR_INVALID,
+                       "the logarithm of the number of registers per counter should be at least 4; got " +
+                           std::to_string(o.log2m));
+    if (o.log2m > 10)
+        return set_err(nullptr, HB_ERR_INVALID,
+                       "log2m above 10 is not supported by the device kernels; got " +
+                           std::to_string(o.log2m));
+    if (o.hash_kind != HB_HASH_SIP13 && o.hash_kind != HB_HASH_JENKINS)
+        return set_err(nullptr, HB_ERR_INVALID, "unknown hash_kind");
+
+    std::unique_ptr<hb_handle> h(new hb_handle());
+    h->device = o.device;
+    h->stream = (cudaStream_t)o.stream;
+    h->n = graph->num_nodes;
+    h->m = graph->num_arcs;
+    h->log2m = o.log2m;
+    h->counter_bytes = ((uint64_t)1 << o.log2m) * 5 / 8;
+    h->hash_kind = o.hash_kind;
+    h->hash_seed = o.hash_seed;
+    h->do_sod = o.flags & HB_SUM_OF_DISTANCES;
+    h->do_harm = o.flags & HB_SUM_OF_INVERSE_DISTANCES;
+    h->quirk = !(o.flags & HB_NO_I32_SHIFT_QUIRK);
+    h->arc_granularity = o.arc_granularity ? o.arc_granularity : 16 * 1024;
+    h->weight_seed = o.weight_seed;
+    h->has_weights = o.weights != nullptr;
+    uint64_t ne = o.num_elements;
+    if (ne == 0) {
+        if (o.weights) {
+            for (uint64_t i = 0; i < h->n; i++) ne += o.weights[i];
+        } else {
+            ne = h->n;
+        }
+    }
+    h->num_elements = ne;
+    if (register_size(ne) != 5)
+        return set_err(nullptr, HB_ERR_INVALID, "register size other than 5 is not supported");
+    {
+        // HLL:388-393, 420
+        const double mf = (double)(1ull << o.log2m);
+        double alpha;
+        switch (o.log2m) {
+            case 4: alpha = 0.673; break;
+            case 5: alpha = 0.697; break;
+            case 6: alpha = 0.709; break;
+            default: alpha = 0.7213 / (1.0 + 1.079 / mf); break;
+        }
+        h->alpha_m_m = alpha * (mf * mf);
+    }
+
+    hb_handle* hp = h.get();
+    int r;
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_NO_DEVICE, "no CUDA device available (this library has no CPU path)");
+    }
+    if ((r = cuda_err(hp, cudaSetDevice(h->device), "cudaSetDevice"))) return r;
+    for (auto& e : h->ev)
+        if ((r = cuda_err(hp, cudaEventCreate(&e), "cudaEventCreate"))) {
+            release(hp);
+            return r;
+        }
+
+    auto fail = [&](int code) {
+        g_global_err = hp->err;
+        release(hp);
+        return code;
+    };
+    if ((r = upload_csr(hp, graph, &h->d_off, &h->d_succ))) return fail(r);
+    if (transpose) {
+        if ((r = upload_csr(hp, transpose, &h->d_toff, &h->d_tsucc))) return fail(r);
+        h->has_transpose = true;
+    } else if (o.flags & HB_TRANSPOSE_ON_DEVICE) {
+        if ((r = build_transpose_on_device(hp))) return fail(r);
+    }
+    const uint64_t n = h->n;
+    if ((r = dalloc(hp, &h->d_cnt[0], n * h->counter_bytes))) return fail(r);
+    if ((r = dalloc(hp, &h->d_cnt[1], n * h->counter_bytes))) return fail(r);
+    const uint64_t words = (n + 31) / 32;
+    for (int b = 0; b < 4; b++)
+        if ((r = dalloc(hp, &h->d_bits[b], words))) return fail(r);
+    if ((r = dalloc(hp, &h->d_est, n))) return fail(r);
+    if (h->do_sod && (r = dalloc(hp, &h->d_sod, n))) return fail(r);
+    if (h->do_harm && (r = dalloc(hp, &h->d_harm, n))) return fail(r);
+    {
+        const uint64_t mm = 1ull << o.log2m;
+        std::vector<double> lnt(mm + 1, 0.0);
+        const double mf = (double)mm;
+        for (uint64_t z = 1; z <= mm; z++) lnt[z] = mf * std::log(mf / (double)z);
+        if ((r = dalloc(hp, &h->d_lnt, mm + 1))) return fail(r);
+        if ((r = cuda_err(hp, cudaMemcpy(h->d_lnt, lnt.data(), (mm + 1) * 8, cudaMemcpyHostToDevice),
+                          "cudaMemcpy")))
+            return fail(r);
+    }
+    if (o.weights) {
+        if ((r = dalloc(hp, &h->d_weights, n))) return fail(r);
+        if ((r = cuda_err(hp, cudaMemcpy(h->d_weights, o.weights, n * 8, cudaMemcpyHostToDevice),
+                          "cudaMemcpy")))
+            return fail(r);
+    }
+    // degree buckets (static: the graph does not change)
+    h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
+    h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
+    if (h->medium_max < h->small_max) h->medium_max = h->small_max;
+    {
+        std::vector<uint32_t> med, hvy;
+        for (uint64_t v = 0; v < n; v++) {
+            const uint64_t d = graph->offsets[v + 1] - graph->offsets[v];
+            if (d > h->medium_max)
+                hvy.push_back((uint32_t)v);
+            else if (d > h->small_max)
+                med.push_back((uint32_t)v);
+        }
+        // heaviest first so the long CTA teams start early
+        std::stable_sort(hvy.begin(), hvy.end(), [&](uint32_t x, uint32_t y) {
+            return graph->offsets[x + 1] - graph->offsets[x] > graph->offsets[y + 1] - graph->offsets[y];
+        });
+        h->n_medium = med.size();
+        h->n_heavy = hvy.size();
+        if (h->n_medium) {
+            if ((r = dalloc(hp, &h->d_medium, h->n_medium))) return fail(r);
+            if ((r = cuda_err(hp, cudaMemcpy(h->d_medium, med.data(), h->n_medium * 4, cudaMemcpyHostToDevice),
+                              "cudaMemcpy")))
+                return fail(r);
+        }
+        if (h->n_heavy) {
+            if ((r = dalloc(hp, &h->d_heavy, h->n_heavy))) return fail(r);
+            if ((r = cuda_err(hp, cudaMemcpy(h->d_heavy, hvy.data(), h->n_heavy * 4, cudaMemcpyHostToDevice),
+                              "cudaMemcpy")))
+                return fail(r);
+        }
+    }
+    h->grid_group = hbk::union_grid(h->log2m, 0, h->device);
+    {
+        const uint64_t need = (n + 255) / 256 + 1;
+        if ((uint64_t)h->grid_group > need) h->grid_group = (int)need;
+    }
+    h->grid_warp = hbk::union_grid(h->log2m, 1, h->device);
+    {
+        const uint64_t need = (h->n_medium * 32 + 255) / 256 + 1;
+        if ((uint64_t)h->grid_warp > need) h->grid_warp = (int)need;
+    }
+    h->grid_cta = hbk::union_grid(h->log2m, 2, h->device);
+    if ((uint64_t)h->grid_cta > h->n_heavy + 1) h->grid_cta = (int)(h->n_heavy + 1);
+    h->nf_slots = h->grid_group + h->grid_warp + h->grid_cta;
+    if ((r = dalloc(hp, &h->d_nf_partials, h->nf_slots))) return fail(r);
+    if ((r = dalloc(hp, &h->d_nf_out, 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_stats, 4))) return fail(r);
+    if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
+    *out = h.release();
+    return HB_OK;
+}
+
+int hb_add_discount_function(hb_handle* h, hb_discount_fn fn, void* ctx) {
+    if (!h || !fn) return set_err(h, HB_ERR_INVALID, "handle or function is NULL");
+    if ((int)h->disc_fn.size() >= hbk::MAX_DISCOUNT)
+        return set_err(h, HB_ERR_INVALID, "at most 8 discount functions");
+    double* d = nullptr;
+    int r = dalloc(h, &d, h->n);
+    if (r) return r;
+    h->disc_fn.push_back(fn);
+    h->disc_ctx.push_back(ctx);
+    h->d_disc.push_back(d);
+    return HB_OK;
+}
+
+void hb_destroy(hb_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release(h);
+    delete h;
+}
+
+int hb_init(hb_handle* h) {
+    if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    HB_CUDA(h, cudaSetDevice(h->device));
+    return do_init(h);
+}
+
+int hb_iterate(hb_handle* h, hb_iter_stats* out) {
+    if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    if (!h->initialised) return set_err(h, HB_ERR_NOT_RUN, "hb_init must precede hb_iterate");
+    HB_CUDA(h, cudaSetDevice(h->device));
+    return do_iterate(h, out);
+}
+
+int hb_run(hb_handle* h, uint64_t upper_bound, double threshold) {
+    if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    HB_CUDA(h, cudaSetDevice(h->device));
+    upper_bound = std::min<uint64_t>(upper_bound, h->n);  // HB:541
+    int r = do_init(h);
+    if (r) return r;
+    for (uint64_t i = 0; i < upper_bound; i++) {
+        if ((r = do_iterate(h, nullptr))) return r;
+        if (h->modified_counters == 0) break;  // HB:559-570
+        if (!std::isnan(threshold) && i > 3 && h->relative_increment < 1.0 + threshold) break;
+    }
+    return HB_OK;
+}
+
+int hb_run_until_stable(hb_handle* h, uint64_t upper_bound) { return hb_run(h, upper_bound, NAN); }
+int hb_run_until_done(hb_handle* h) { return hb_run(h, UINT64_MAX, NAN); }
+
+uint64_t hb_num_iterations(const hb_handle* h) { return h ? h->iteration : 0; }
+
+int hb_get_iteration_stats(const hb_handle* h, uint64_t i, hb_iter_stats* out) {
+    if (!h || !out) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    if (i >= h->stats.size()) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "no such iteration");
+    *out = h->stats[i];
+    return HB_OK;
+}
+
+int hb_get_neighborhood_function(const hb_handle* h, double* dst, size_t capacity, size_t* len) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if (len) *len = h->nf.size();
+    if (dst) std::memcpy(dst, h->nf.data(), std::min(capacity, h->nf.size()) * sizeof(double));
+    return HB_OK;
+}
+
+int hb_get_sum_of_distances(const hb_handle* h, double* dst, size_t len) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if (!h->d_sod)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
+                       "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building HyperBall to compute them");
+    if ((r = check_len(h, len))) return r;
+    return copy_d2h(h, h->d_sod, dst, len * 8);
+}
+
+int hb_get_harmonic_centralities(const hb_handle* h, double* dst, size_t len) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if (!h->d_harm)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
+                       "Sum of inverse distances were not requested. Set HB_SUM_OF_INVERSE_DISTANCES while building HyperBall to compute them");
+    if ((r = check_len(h, len))) return r;
+    return copy_d2h(h, h->d_harm, dst, len * 8);
+}
+
+int hb_get_discounted_centrality(const hb_handle* h, size_t index, double* dst, size_t len) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if (index >= h->d_disc.size())
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
+                       "Discount centrality of index " + std::to_string(index) + " does not exist");
+    if ((r = check_len(h, len))) return r;
+    return copy_d2h(h, h->d_disc[index], dst, len * 8);
+}
+
+int hb_get_closeness_centrality(const hb_handle* h, double* dst, size_t len) {
+    int r = hb_get_sum_of_distances(h, dst, len);
+    if (r) {
+        if (r == HB_ERR_NOT_REQUESTED)
+            const_cast<hb_handle*>(h)->err =
+                "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building HyperBall to compute closeness centrality";
+        return r;
+    }
+    for (size_t i = 0; i < len; i++) dst[i] = dst[i] == 0.0 ? 0.0 : 1.0 / dst[i];
+    return HB_OK;
+}
+
+int hb_get_reachable_nodes(const hb_handle* h, double* dst, size_t len) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if ((r = check_len(h, len))) return r;
+    return copy_d2h(h, h->d_est, dst, len * 8);
+}
+
+int hb_reachable_nodes_from(const hb_handle* h, uint64_t node, double* out) {
+    int r = ensure_iteration(h);
+    if (r) return r;
+    if (node >= h->n || !out) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "node out of range");
+    return copy_d2h(h, h->d_est + node, out, 8);
+}
+
+static int lin_or_nieminen(const hb_handle* h, double* dst, size_t len, bool lin) {
+    int r = hb_get_sum_of_distances(h, dst, len);
+    if (r) {
+        if (r == HB_ERR_NOT_REQUESTED)
+            const_cast<hb_handle*>(h)->err =
+                lin ? "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building HyperBall to compute lin centrality"
+                    : "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building HyperBall to compute nieminen centrality";
+        return r;
+    }
+    std::vector<double> cnt(len);
+    if ((r = copy_d2h(h, h->d_est, cnt.data(), len * 8))) return r;
+    for (size_t i = 0; i < len; i++) {
+        const double d = dst[i];
+        if (lin) {
+            dst[i] = d == 0.0 ? 1.0 : cnt[i] * cnt[i] / d;
+        } else {
+            dst[i] = (cnt[i] * cnt[i]) - d;
+        }
+    }
+    return HB_OK;
+}
+
+int hb_get_lin_centrality(const hb_handle* h, double* dst, size_t len) {
+    return lin_or_nieminen(h, dst, len, true);
+}
+int hb_get_nieminen_centrality(const hb_handle* h, double* dst, size_t len) {
+    return lin_or_nieminen(h, dst, len, false);
+}
+
+int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes) {
+    if (!h || !dst) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    if (bytes != h->n * h->counter_bytes)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "bytes must be num_nodes * counter bytes");
+    if (which != HB_CURRENT_STATE && which != HB_NEXT_STATE)
+        return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "which must be HB_CURRENT_STATE or HB_NEXT_STATE");
+    const int idx = which == HB_CURRENT_STATE ? h->cur : (h->cur ^ 1);
+    return copy_d2h(h, h->d_cnt[idx], dst, bytes);
+}
+
+int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* reg_size) {
+    if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    if (counter_bytes) *counter_bytes = h->counter_bytes;
+    if (reg_size) *reg_size = register_size(h->num_elements);
+    return HB_OK;
+}
+
+// ---- graphs -----------------------------------------------------------------
+int hb_graph_load_bvgraph(const char* basename, hb_graph** out) {
+    if (!basename || !out) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    std::unique_ptr<hb_graph> g(new hb_graph());
+    std::string err;
+    uint64_t checked = 0;
+    int r = hbg::load_bvgraph(basename, g->g, err, &checked);
+    if (r) return set_err(nullptr, r, err);
+    *out = g.release();
+    return HB_OK;
+}
+
+int hb_graph_generate_er(uint64_t n, uint32_t d, uint64_t seed, hb_graph** out) {
+    if (!out) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    if (n > 0xffffffffull) return set_err(nullptr, HB_ERR_INVALID, "too many nodes");
+    std::unique_ptr<hb_graph> g(new hb_graph());
+    hbg::gen_er(n, d, seed, g->g);
+    *out = g.release();
+    return HB_OK;
+}
+
+int hb_graph_generate_rmat(int scale, uint64_t epn, double a, double b, double c, uint64_t seed,
+                           hb_graph** out) {
+    if (!out || scale < 1 || scale > 31 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0)
+        return set_err(nullptr, HB_ERR_INVALID, "invalid R-MAT parameters");
+    std::unique_ptr<hb_graph> g(new hb_graph());
+    hbg::gen_rmat(scale, epn, a, b, c, seed, g->g);
+    *out = g.release();
+    return HB_OK;
+}
+
+int hb_graph_generate_weblike(uint64_t n, uint64_t cap, double shift, uint64_t window, uint64_t seed,
+                              hb_graph** out) {
+    if (!out || n == 0 || n > 0xffffffffull || cap == 0 || !(shift >= 0.0))
+        return set_err(nullptr, HB_ERR_INVALID, "invalid web-like parameters");
+    std::unique_ptr<hb_graph> g(new hb_graph());
+    hbg::gen_weblike(n, cap, shift, window, seed, g->g);
+    *out = g.release();
+    return HB_OK;
+}
+
+int hb_graph_transpose(const hb_graph* g, hb_graph** out) {
+    if (!g || !out) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    std::unique_ptr<hb_graph> t(new hb_graph());
+    hbg::transpose(g->g, t->g);
+    *out = t.release();
+    return HB_OK;
+}
+
+int hb_graph_from_csr(const hb_graph_view* v, hb_graph** out) {
+    std::string why;
+    if (!out) return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    if (!check_view(v, why)) return set_err(nullptr, HB_ERR_INVALID, why);
+    std::unique_ptr<hb_graph> g(new hb_graph());
+    g->g.n = v->num_nodes;
+    g->g.m = v->num_arcs;
+    g->g.offsets.assign(v->offsets, v->offsets + v->num_nodes + 1);
+    g->g.successors.assign(v->successors, v->successors + v->num_arcs);
+    *out = g.release();
+    return HB_OK;
+}
+
+hb_graph_view hb_graph_get_view(const hb_graph* g) {
+    hb_graph_view v{};
+    if (!g) return v;
+    v.num_nodes = g->g.n;
+    v.num_arcs = g->g.m;
+    v.offsets = g->g.offsets.data();
+    v.successors = g->g.successors.data();
+    return v;
+}
+
+void hb_graph_free(hb_graph* g) { delete g; }
+
+}  // extern "C"

@@ -1,0 +1,614 @@
+"""Python mirror of the reference HyperBall API over the GB300 C ABI.
+
+The reference (Rust crate webgraph-algo 0.1.0) drives HyperBall as
+
+    let logic = HyperLogLogBuilder::new(n).log_2_num_reg(8)
+        .build_hasher(JenkinsHasherBuilder::new(42)).build()?;     // HLL:234-428
+    let mut hb = HyperBallBuilder::with_transpose(&g, &gt, &dcf, a0, a1)
+        .sum_of_distances(true).sum_of_inverse_distances(true)
+        .build(pl);                                                 // HB:204-403
+    hb.run_until_done(&threads, pl)?;                               // HB:614-621
+    let sod = hb.sum_of_distances()?;                               // HB:639-647
+
+and this module keeps that shape, names and error behaviour:
+
+    logic = HyperLogLogBuilder(n).log_2_num_reg(8).build_hasher(JenkinsHasher(42)).build()
+    hb = (HyperBallBuilder.with_transpose(g, gt, logic)
+          .sum_of_distances(True).sum_of_inverse_distances(True).build())
+    hb.run_until_done()
+    sod = hb.sum_of_distances()
+
+Counters live on the GPU; there is no CPU path. Loading the library never
+needs a GPU, but building a HyperBall without one raises NoDeviceError.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(_PKG, "lib", "libhyperball_gb300.so")
+
+HB_OK = 0
+HB_ERR_INVALID = 1
+HB_ERR_NOT_RUN = 2
+HB_ERR_NOT_REQUESTED = 3
+HB_ERR_OOM = 4
+HB_ERR_CUDA = 5
+HB_ERR_TIMEOUT = 6
+HB_ERR_IO = 7
+HB_ERR_NO_DEVICE = 8
+
+HB_HASH_SIP13 = 0
+HB_HASH_JENKINS = 1
+
+HB_SUM_OF_DISTANCES = 1 << 0
+HB_SUM_OF_INVERSE_DISTANCES = 1 << 1
+HB_TRANSPOSE_ON_DEVICE = 1 << 2
+HB_NO_I32_SHIFT_QUIRK = 1 << 3
+
+HB_CURRENT_STATE = 0
+HB_NEXT_STATE = 1
+
+
+class HyperBallError(RuntimeError):
+    """Base error; `code` is the C status."""
+
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class InvalidArgumentError(HyperBallError, ValueError):
+    pass
+
+
+class NotRunError(HyperBallError):
+    pass
+
+
+class NotRequestedError(HyperBallError):
+    pass
+
+
+class NoDeviceError(HyperBallError):
+    pass
+
+
+_ERRORS = {
+    HB_ERR_INVALID: InvalidArgumentError,
+    HB_ERR_NOT_RUN: NotRunError,
+    HB_ERR_NOT_REQUESTED: NotRequestedError,
+    HB_ERR_NO_DEVICE: NoDeviceError,
+}
+
+
+class GraphView(ctypes.Structure):
+    _fields_ = [
+        ("num_nodes", ctypes.c_uint64),
+        ("num_arcs", ctypes.c_uint64),
+        ("offsets", ctypes.POINTER(ctypes.c_uint64)),
+        ("successors", ctypes.POINTER(ctypes.c_uint32)),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("log2m", ctypes.c_int32),
+        ("hash_kind", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("hash_seed", ctypes.c_uint64),
+        ("num_elements", ctypes.c_uint64),
+        ("flags", ctypes.c_uint32),
+        ("reserved0", ctypes.c_uint32),
+        ("arc_granularity", ctypes.c_uint64),
+        ("weights", ctypes.POINTER(ctypes.c_uint64)),
+        ("weight_seed", ctypes.c_uint64),
+        ("stream", ctypes.c_void_p),
+        ("small_max_degree", ctypes.c_uint32),
+        ("medium_max_degree", ctypes.c_uint32),
+    ]
+
+
+class IterStats(ctypes.Structure):
+    _fields_ = [
+        ("iteration", ctypes.c_uint64),
+        ("modified_counters", ctypes.c_uint64),
+        ("visited_arcs", ctypes.c_uint64),
+        ("scanned_nodes", ctypes.c_uint64),
+        ("neighborhood_function", ctypes.c_double),
+        ("relative_increment", ctypes.c_double),
+        ("systolic", ctypes.c_int32),
+        ("local", ctypes.c_int32),
+        ("pre_local", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("union_ms", ctypes.c_double),
+        ("iteration_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+DISCOUNT_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p)
+
+# (name, restype, argtypes) of every exported entry point of include/hyperball_gb300.h
+_P = ctypes.POINTER
+_H = ctypes.c_void_p
+EXPORTS = [
+    ("hb_options_default", None, [_P(Options)]),
+    ("hb_create", ctypes.c_int, [_P(GraphView), _P(GraphView), _P(Options), _P(_H)]),
+    ("hb_add_discount_function", ctypes.c_int, [_H, DISCOUNT_FN, ctypes.c_void_p]),
+    ("hb_destroy", None, [_H]),
+    ("hb_run", ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double]),
+    ("hb_run_until_stable", ctypes.c_int, [_H, ctypes.c_uint64]),
+    ("hb_run_until_done", ctypes.c_int, [_H]),
+    ("hb_init", ctypes.c_int, [_H]),
+    ("hb_iterate", ctypes.c_int, [_H, _P(IterStats)]),
+    ("hb_num_iterations", ctypes.c_uint64, [_H]),
+    ("hb_get_iteration_stats", ctypes.c_int, [_H, ctypes.c_uint64, _P(IterStats)]),
+    ("hb_get_neighborhood_function", ctypes.c_int,
+     [_H, _P(ctypes.c_double), ctypes.c_size_t, _P(ctypes.c_size_t)]),
+    ("hb_get_sum_of_distances", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_harmonic_centralities", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_discounted_centrality", ctypes.c_int,
+     [_H, ctypes.c_size_t, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_closeness_centrality", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_lin_centrality", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_nieminen_centrality", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_get_reachable_nodes", ctypes.c_int, [_H, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_reachable_nodes_from", ctypes.c_int, [_H, ctypes.c_uint64, _P(ctypes.c_double)]),
+    ("hb_get_registers", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
+    ("hb_counter_layout", ctypes.c_int, [_H, _P(ctypes.c_uint64), _P(ctypes.c_int)]),
+    ("hb_last_error", ctypes.c_char_p, [_H]),
+    ("hb_global_last_error", ctypes.c_char_p, []),
+    ("hb_graph_load_bvgraph", ctypes.c_int, [ctypes.c_char_p, _P(_H)]),
+    ("hb_graph_generate_er", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, _P(_H)]),
+    ("hb_graph_generate_rmat", ctypes.c_int,
+     [ctypes.c_int, ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+      ctypes.c_uint64, _P(_H)]),
+    ("hb_graph_generate_weblike", ctypes.c_int,
+     [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, _P(_H)]),
+    ("hb_graph_transpose", ctypes.c_int, [_H, _P(_H)]),
+    ("hb_graph_from_csr", ctypes.c_int, [_P(GraphView), _P(_H)]),
+    ("hb_graph_get_view", GraphView, [_H]),
+    ("hb_graph_free", None, [_H]),
+    ("hb_version", ctypes.c_char_p, []),
+]
+
+_lib = None
+
+
+def load_library(path=None):
+    """Loads the in-tree shared library (building nothing). Raises if missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(
+            "libhyperball_gb300.so not built (run __graft_entry__.build()); "
+            "there is no CPU fallback")
+    lib = ctypes.CDLL(p)
+    for name, res, args in EXPORTS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(code, handle=None):
+    if code == HB_OK:
+        return
+    lib = load_library()
+    msg = (lib.hb_last_error(handle) if handle else lib.hb_global_last_error()) or b""
+    raise _ERRORS.get(code, HyperBallError)(code, msg.decode(errors="replace"))
+
+
+# ---------------------------------------------------------------------------
+# graphs
+# ---------------------------------------------------------------------------
+class _Owned:
+    """Array-interface holder that keeps the owner of the memory alive."""
+
+    def __init__(self, owner, ptr, n, typestr):
+        self.owner = owner
+        self.__array_interface__ = {"data": (ptr, True), "shape": (n,), "typestr": typestr,
+                                    "version": 3}
+
+
+class Graph:
+    """Host CSR graph (u64 offsets, u32 successors) owned by the library.
+
+    Stands in for webgraph's RandomAccessGraph; `offsets` is also the
+    cumulative outdegree function the reference passes as `D: Succ`."""
+
+    def __init__(self, handle):
+        self._h = ctypes.c_void_p(handle) if not isinstance(handle, ctypes.c_void_p) else handle
+        lib = load_library()
+        v = lib.hb_graph_get_view(self._h)
+        self.num_nodes = int(v.num_nodes)
+        self.num_arcs = int(v.num_arcs)
+        self._off_ptr = ctypes.cast(v.offsets, ctypes.c_void_p).value
+        self._suc_ptr = ctypes.cast(v.successors, ctypes.c_void_p).value
+
+    # Views keep the graph alive through their base object, so an array taken
+    # from a temporary Graph never outlives the memory it points to.
+    @property
+    def offsets(self):
+        return np.asarray(_Owned(self, self._off_ptr, self.num_nodes + 1, "<u8"))
+
+    @property
+    def successors(self):
+        if self.num_arcs == 0:
+            return np.zeros(0, dtype=np.uint32)
+        return np.asarray(_Owned(self, self._suc_ptr, self.num_arcs, "<u4"))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            load_library().hb_graph_free(h)
+            self._h = None
+
+    def view(self):
+        return GraphView(self.num_nodes, self.num_arcs,
+                         self.offsets.ctypes.data_as(_P(ctypes.c_uint64)),
+                         self.successors.ctypes.data_as(_P(ctypes.c_uint32)))
+
+    def outdegree(self, node):
+        return int(self.offsets[node + 1] - self.offsets[node])
+
+    def successors_of(self, node):
+        return self.successors[self.offsets[node]:self.offsets[node + 1]]
+
+    @staticmethod
+    def _make(fn, *args):
+        h = ctypes.c_void_p()
+        _check(fn(*args, ctypes.byref(h)))
+        return Graph(h)
+
+    @staticmethod
+    def load_bvgraph(basename):
+        return Graph._make(load_library().hb_graph_load_bvgraph, os.fsencode(basename))
+
+    @staticmethod
+    def erdos_renyi(n, d, seed):
+        return Graph._make(load_library().hb_graph_generate_er, n, d, seed)
+
+    @staticmethod
+    def rmat(scale, edges_per_node, a=0.57, b=0.19, c=0.19, seed=1):
+        return Graph._make(load_library().hb_graph_generate_rmat, scale, edges_per_node, a, b, c, seed)
+
+    @staticmethod
+    def weblike(n, cap=100_000, shift=1.266, window=1024, seed=2):
+        return Graph._make(load_library().hb_graph_generate_weblike, n, cap, shift, window, seed)
+
+    @staticmethod
+    def from_csr(offsets, successors):
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        suc = np.ascontiguousarray(successors, dtype=np.uint32)
+        v = GraphView(len(off) - 1, len(suc), off.ctypes.data_as(_P(ctypes.c_uint64)),
+                      suc.ctypes.data_as(_P(ctypes.c_uint32)))
+        return Graph._make(load_library().hb_graph_from_csr, ctypes.byref(v))
+
+    def transpose(self):
+        return Graph._make(load_library().hb_graph_transpose, self._h)
+
+
+# ---------------------------------------------------------------------------
+# HyperLogLog logic descriptor (HyperLogLogBuilder, HLL:234-428)
+# ---------------------------------------------------------------------------
+class DefaultHasher:
+    """Rust std DefaultHasher (SipHash-1-3, zero keys)."""
+    kind = HB_HASH_SIP13
+    seed = 0
+
+
+class JenkinsHasher:
+    """JenkinsHasherBuilder::new(seed) of the reference's tests."""
+    kind = HB_HASH_JENKINS
+
+    def __init__(self, seed):
+        self.seed = seed
+
+
+class HyperLogLog:
+    def __init__(self, log2m, hasher, num_elements):
+        self.log2m = log2m
+        self.hasher = hasher
+        self.num_elements = num_elements
+
+    @property
+    def num_registers(self):
+        return 1 << self.log2m
+
+    @property
+    def counter_bytes(self):
+        return (1 << self.log2m) * 5 // 8
+
+
+class HyperLogLogBuilder:
+    def __init__(self, n):
+        self._n = n
+        self._log2m = 4
+        self._hasher = DefaultHasher()
+
+    def log_2_num_reg(self, log2m):
+        self._log2m = log2m
+        return self
+
+    def rsd(self, rsd):
+        return self.log_2_num_reg(math.ceil(math.log2((1.106 / rsd) ** 2)))
+
+    def num_elements(self, n):
+        self._n = n
+        return self
+
+    def build_hasher(self, hasher):
+        self._hasher = hasher
+        return self
+
+    def word_type(self, _dtype):
+        # The device layout is byte-identical for every word type.
+        return self
+
+    def build(self):
+        if self._log2m < 4:
+            raise InvalidArgumentError(
+                HB_ERR_INVALID,
+                "the logarithm of the number of registers per counter should be at least 4; "
+                f"got {self._log2m}")
+        return HyperLogLog(self._log2m, self._hasher, self._n)
+
+
+# ---------------------------------------------------------------------------
+# HyperBallBuilder / HyperBall (HB:26-757)
+# ---------------------------------------------------------------------------
+class HyperBallBuilder:
+    DEFAULT_GRANULARITY = 16 * 1024
+
+    def __init__(self, graph, transpose, logic):
+        self._graph = graph
+        self._transpose = transpose
+        self._logic = logic
+        self._sod = False
+        self._harm = False
+        self._disc = []
+        self._gran = self.DEFAULT_GRANULARITY
+        self._weights = None
+        self._weight_seed = 0
+        self._transpose_on_device = False
+        self._stream = None
+        self._device = 0
+        self._small = None
+        self._medium = None
+        self._quirk = True
+
+    @staticmethod
+    def new(graph, logic):
+        """HyperBallBuilder::new (HB:152-181): no transpose, no systolic iterations."""
+        return HyperBallBuilder(graph, None, logic)
+
+    @staticmethod
+    def with_transpose(graph, transpose, logic):
+        """HyperBallBuilder::with_transpose (HB:204-256)."""
+        if transpose.num_nodes != graph.num_nodes:
+            raise InvalidArgumentError(
+                HB_ERR_INVALID, "the transpose should have same number of nodes of the graph")
+        if transpose.num_arcs != graph.num_arcs:
+            raise InvalidArgumentError(
+                HB_ERR_INVALID, "the transpose should have same number of arcs of the graph")
+        return HyperBallBuilder(graph, transpose, logic)
+
+    @staticmethod
+    def with_hyper_log_log(graph, transpose, log2m, weights=None):
+        """HyperBallBuilder::with_hyper_log_log (HB:91-133), default hasher."""
+        if weights is not None and len(weights) != graph.num_nodes:
+            raise InvalidArgumentError(
+                HB_ERR_INVALID, "weights should have length equal to the graph's number of nodes")
+        n = int(np.sum(weights)) if weights is not None else graph.num_nodes
+        logic = HyperLogLogBuilder(n).log_2_num_reg(log2m).build()
+        b = HyperBallBuilder(graph, transpose, logic)
+        return b.weights(weights)
+
+    def sum_of_distances(self, flag):
+        self._sod = bool(flag)
+        return self
+
+    def sum_of_inverse_distances(self, flag):
+        self._harm = bool(flag)
+        return self
+
+    def arc_granularity(self, g):
+        self._gran = int(g)
+        return self
+
+    def weights(self, weights, seed=0):
+        if weights is not None:
+            w = np.ascontiguousarray(weights, dtype=np.uint64)
+            if len(w) != self._graph.num_nodes:
+                raise InvalidArgumentError(HB_ERR_INVALID, "weights length mismatch")
+            self._weights = w
+        else:
+            self._weights = None
+        self._weight_seed = seed
+        return self
+
+    def discount_function(self, fn):
+        self._disc.append(fn)
+        return self
+
+    def no_discount_function(self):
+        self._disc = []
+        return self
+
+    # GB300 extensions (no reference counterpart)
+    def transpose_on_device(self, flag=True):
+        self._transpose_on_device = bool(flag)
+        return self
+
+    def stream(self, cuda_stream_ptr):
+        self._stream = cuda_stream_ptr
+        return self
+
+    def device(self, ordinal):
+        self._device = int(ordinal)
+        return self
+
+    def degree_buckets(self, small_max, medium_max):
+        self._small, self._medium = int(small_max), int(medium_max)
+        return self
+
+    def i32_shift_quirk(self, flag):
+        self._quirk = bool(flag)
+        return self
+
+    def build(self):
+        return HyperBall(self)
+
+
+class HyperBall:
+    def __init__(self, b):
+        lib = load_library()
+        self._lib = lib
+        self._b = b
+        self.num_nodes = b._graph.num_nodes
+        o = Options()
+        lib.hb_options_default(ctypes.byref(o))
+        o.log2m = b._logic.log2m
+        o.hash_kind = b._logic.hasher.kind
+        o.hash_seed = b._logic.hasher.seed
+        o.num_elements = b._logic.num_elements
+        flags = 0
+        if b._sod:
+            flags |= HB_SUM_OF_DISTANCES
+        if b._harm:
+            flags |= HB_SUM_OF_INVERSE_DISTANCES
+        if b._transpose is None and b._transpose_on_device:
+            flags |= HB_TRANSPOSE_ON_DEVICE
+        if not b._quirk:
+            flags |= HB_NO_I32_SHIFT_QUIRK
+        o.flags = flags
+        o.arc_granularity = b._gran
+        o.device = b._device
+        o.stream = b._stream
+        if b._small is not None:
+            o.small_max_degree = b._small
+        if b._medium is not None:
+            o.medium_max_degree = b._medium
+        if b._weights is not None:
+            o.weights = b._weights.ctypes.data_as(_P(ctypes.c_uint64))
+            o.weight_seed = b._weight_seed
+        self._gv = b._graph.view()
+        self._tv = b._transpose.view() if b._transpose is not None else None
+        h = ctypes.c_void_p()
+        _check(lib.hb_create(ctypes.byref(self._gv),
+                             ctypes.byref(self._tv) if self._tv is not None else None,
+                             ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._disc_refs = []
+        for fn in b._disc:
+            cb = DISCOUNT_FN(lambda d, _ctx, f=fn: float(f(int(d))))
+            self._disc_refs.append(cb)
+            _check(lib.hb_add_discount_function(h, cb, None), h)
+        cb = ctypes.c_uint64()
+        rs = ctypes.c_int()
+        _check(lib.hb_counter_layout(h, ctypes.byref(cb), ctypes.byref(rs)), h)
+        self.counter_bytes = int(cb.value)
+        self.register_size = int(rs.value)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.hb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- running ---------------------------------------------------------
+    def run(self, upper_bound, threshold=None):
+        t = float("nan") if threshold is None else float(threshold)
+        _check(self._lib.hb_run(self._h, min(int(upper_bound), 2**64 - 1), t), self._h)
+
+    def run_until_stable(self, upper_bound):
+        _check(self._lib.hb_run_until_stable(self._h, min(int(upper_bound), 2**64 - 1)), self._h)
+
+    def run_until_done(self):
+        _check(self._lib.hb_run_until_done(self._h), self._h)
+
+    def init(self):
+        _check(self._lib.hb_init(self._h), self._h)
+
+    def iterate(self):
+        s = IterStats()
+        _check(self._lib.hb_iterate(self._h, ctypes.byref(s)), self._h)
+        return s.as_dict()
+
+    @property
+    def iteration(self):
+        return int(self._lib.hb_num_iterations(self._h))
+
+    def iteration_stats(self):
+        out = []
+        for i in range(self.iteration):
+            s = IterStats()
+            _check(self._lib.hb_get_iteration_stats(self._h, i, ctypes.byref(s)), self._h)
+            out.append(s.as_dict())
+        return out
+
+    # -- results ---------------------------------------------------------
+    def neighborhood_function(self):
+        ln = ctypes.c_size_t()
+        _check(self._lib.hb_get_neighborhood_function(self._h, None, 0, ctypes.byref(ln)), self._h)
+        out = np.zeros(ln.value, dtype=np.float64)
+        _check(self._lib.hb_get_neighborhood_function(
+            self._h, out.ctypes.data_as(_P(ctypes.c_double)), ln.value, ctypes.byref(ln)), self._h)
+        return out
+
+    def _vec(self, fn, *pre):
+        out = np.zeros(self.num_nodes, dtype=np.float64)
+        _check(fn(self._h, *pre, out.ctypes.data_as(_P(ctypes.c_double)), self.num_nodes), self._h)
+        return out
+
+    def sum_of_distances(self):
+        return self._vec(self._lib.hb_get_sum_of_distances)
+
+    def harmonic_centralities(self):
+        return self._vec(self._lib.hb_get_harmonic_centralities)
+
+    def discounted_centrality(self, index):
+        return self._vec(self._lib.hb_get_discounted_centrality, index)
+
+    def closeness_centrality(self):
+        return self._vec(self._lib.hb_get_closeness_centrality)
+
+    def lin_centrality(self):
+        return self._vec(self._lib.hb_get_lin_centrality)
+
+    def nieminen_centrality(self):
+        return self._vec(self._lib.hb_get_nieminen_centrality)
+
+    def reachable_nodes(self):
+        return self._vec(self._lib.hb_get_reachable_nodes)
+
+    def reachable_nodes_from(self, node):
+        v = ctypes.c_double()
+        _check(self._lib.hb_reachable_nodes_from(self._h, node, ctypes.byref(v)), self._h)
+        return v.value
+
+    def registers(self, which=HB_CURRENT_STATE):
+        """Raw counter bytes (num_nodes x counter_bytes), reference layout."""
+        out = np.zeros((self.num_nodes, self.counter_bytes), dtype=np.uint8)
+        _check(self._lib.hb_get_registers(self._h, which, out.ctypes.data, out.nbytes), self._h)
+        return out
