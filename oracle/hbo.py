@@ -81,6 +81,8 @@ def lib():
             "hbo_hll_params": (None, [ctypes.c_int, ctypes.c_uint64, _P(ctypes.c_double),
                                       _P(ctypes.c_uint64)]),
             "hbo_last_error": (ctypes.c_char_p, []),
+            "hbo_check_div_small_int": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64,
+                                                          ctypes.c_uint64]),
             "hbo_hll_count_hashes": (ctypes.c_double, [ctypes.c_int, ctypes.c_uint64,
                                                        _P(ctypes.c_uint64), ctypes.c_uint64,
                                                        _P(ctypes.c_uint64), ctypes.c_uint64]),

@@ -707,6 +707,38 @@ double hbo_hll_count_hashes(int log2m, uint64_t n, const uint64_t* hashes, uint6
     return lg.count(a.data());
 }
 
+// Checks the device's division by the iteration number: for d = 1..d_max and
+// `samples` random positive doubles a (exponents spread over +-2^40, plus
+// near-power-of-two cases), q0 = RN(a*rd), r = fma(-q0, d, a),
+// q1 = fma(r, rd, q0) with rd = RN(1/d) must equal a / d. Returns mismatches.
+uint64_t hbo_check_div_small_int(uint64_t d_max, uint64_t samples, uint64_t seed) {
+    uint64_t bad = 0, s = seed;
+    auto next = [&s]() {
+        s += 0x9e3779b97f4a7c15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    };
+    for (uint64_t di = 1; di <= d_max; di++) {
+        const double d = (double)di, rd = 1.0 / d;
+        for (uint64_t k = 0; k < samples; k++) {
+            const uint64_t r = next();
+            double a;
+            const uint64_t mant = r & ((1ull << 52) - 1);
+            const uint64_t ex = 1023 - 40 + ((r >> 52) % 81);
+            uint64_t bits = (ex << 52) | mant;
+            if (k % 8 == 0) bits = (ex << 52) | (r % 4 == 0 ? 0 : ((1ull << 52) - 1 - (r >> 60)));
+            std::memcpy(&a, &bits, 8);
+            const double q0 = a * rd;
+            const double rr = std::fma(-q0, d, a);
+            const double q1 = std::fma(rr, rd, q0);
+            if (q1 != a / d) bad++;
+        }
+    }
+    return bad;
+}
+
 // Per-counter parameters for the tests.
 void hbo_hll_params(int log2m, uint64_t n, double* alpha_m_m, uint64_t* words16) {
     HllLogic<uint16_t> lg(log2m, n, 0, 0);

@@ -214,6 +214,13 @@ def test_siphash_paper_vector(oracle):
     assert L.hbo_siphash(2, 4, k0, k1, msg, 15) == 0xa129ca6149be45e5
 
 
+def test_division_by_iteration_number_is_correctly_rounded(oracle):
+    """The device computes delta / (t+1) as Markstein's corrected product
+    q0 = RN(a*rd), q1 = RN(q0 + fma(-q0, d, a)*rd); it must equal IEEE a/d
+    for every divisor up to 4096 (far above any iteration count reached)."""
+    assert oracle.lib().hbo_check_div_small_int(4096, 20000, 7) == 0
+
+
 def test_sip13_is_siphash13_of_le_bytes(oracle):
     L = oracle.lib()
     for x in (0, 1, 12345, 2**63 + 7):

@@ -90,14 +90,21 @@ struct hb_handle {
     std::vector<double*> d_disc;
     double* d_lnt = nullptr;
     uint64_t* d_weights = nullptr;
-    uint32_t* d_medium = nullptr;
+    uint32_t* d_tiles = nullptr;  // window boundaries
+    uint64_t n_tiles = 0;         // number of windows
+    uint32_t* d_perm = nullptr;     // per window: medium then light nodes, by degree
+    uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
+    uint64_t n_chunks = 0;
+    uint8_t* d_win_flags = nullptr; // systolic: windows with work
     uint32_t* d_heavy = nullptr;
-    uint64_t n_medium = 0, n_heavy = 0;
-    unsigned long long* d_stats = nullptr;  // 4 counters
-    double* d_nf_partials = nullptr;
-    double* d_nf_out = nullptr;
-    int grid_group = 1, grid_warp = 1, grid_cta = 1;
-    int nf_slots = 0;
+    uint64_t n_heavy = 0;
+    hbk::TilePartial* d_partials = nullptr;  // one per tile, then one per heavy block
+    uint64_t n_partials = 0;
+    hbk::TilePartial* d_partial_scratch = nullptr;
+    hbk::TilePartial* d_partial_out = nullptr;
+    int* d_any31 = nullptr;
+    bool any31 = false;
+    int grid_tile = 1, grid_heavy = 1, grid_mark = 1, grid_fin = 1;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // reference state (IterationContext + HyperBall fields)
@@ -260,12 +267,29 @@ hbk::UnionArgs union_args(hb_handle* h) {
     }
     a.systolic = h->systolic ? 1 : 0;
     a.quirk = h->quirk ? 1 : 0;
+    a.any31 = h->any31 ? 1 : 0;
     a.iter = (uint32_t)h->iteration;
     a.n = h->n;
     a.alpha_m_m = h->alpha_m_m;
+    a.a_scaled = h->alpha_m_m * 2147483648.0;  // exact: power-of-two scaling
+    {
+        const double small = 2.5 * (double)(1ull << h->log2m);
+        long long bits;
+        std::memcpy(&bits, &small, sizeof bits);
+        a.small_bits = bits;
+    }
+    a.d1 = (double)(h->iteration + 1);
+    a.rd1 = 1.0 / a.d1;
     a.ln_table = h->d_lnt;
-    a.small_max_degree = h->small_max;
-    a.stats_out = h->d_stats;
+    a.tiles = h->d_tiles;
+    a.n_tiles = (uint32_t)h->n_tiles;
+    a.win_flags = h->d_win_flags;
+    a.perm = h->d_perm;
+    a.chunks = h->d_chunks;
+    a.n_chunks = h->n_chunks;
+    a.tile_max_degree = h->medium_max;
+    a.acc_slot = (uint32_t)(h->n_partials - 1);
+    a.partials = h->d_partials;
     return a;
 }
 
@@ -287,7 +311,11 @@ int do_init(hb_handle* h) {
     ia.alpha_m_m = h->alpha_m_m;
     ia.ln_table = h->d_lnt;
     ia.quirk = h->quirk ? 1 : 0;
+    ia.any31 = h->d_any31;
+    HB_CUDA(h, cudaMemsetAsync(h->d_any31, 0, sizeof(int), h->stream));
     if (n) HB_LAUNCH(h, hbk::launch_init(h->log2m, ia, h->stream));
+    int any31 = 0;
+    HB_CUDA(h, cudaMemcpyAsync(&any31, h->d_any31, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     if (h->d_sod) HB_CUDA(h, cudaMemsetAsync(h->d_sod, 0, n * 8, h->stream));
     if (h->d_harm) HB_CUDA(h, cudaMemsetAsync(h->d_harm, 0, n * 8, h->stream));
     for (double* d : h->d_disc) HB_CUDA(h, cudaMemsetAsync(d, 0, n * 8, h->stream));
@@ -301,6 +329,7 @@ int do_init(hb_handle* h) {
     }
     for (int b = 1; b < 4; b++) HB_CUDA(h, cudaMemsetAsync(h->d_bits[b], 0, words * 4, h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->any31 = any31 != 0;
     h->iteration = 0;
     h->systolic = h->local = h->pre_local = false;
     h->modified_counters = 0;
@@ -334,48 +363,38 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
             // the previous iteration gives the same counters.
             HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mbc_cur], 0, words * 4, s));
             HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur], h->d_toff, h->d_tsucc,
-                                                h->d_bits[h->mbc_cur], n, h->grid_group, s));
+                                                h->d_bits[h->mbc_cur], n, h->grid_mark, s));
         }
     }
-    HB_CUDA(h, cudaMemsetAsync(h->d_stats, 0, 4 * sizeof(unsigned long long), s));
-    HB_CUDA(h, cudaEventRecord(h->ev[1], s));
-
+    HB_CUDA(h, cudaMemsetAsync(h->d_partials, 0, h->n_partials * sizeof(hbk::TilePartial), s));
     hbk::UnionArgs a = union_args(h);
-    int slots = 0;
-    a.nf_partials = h->d_nf_partials;
-    a.list = nullptr;
-    a.list_len = 0;
-    if (n) {
-        HB_LAUNCH(h, hbk::launch_union_group(h->log2m, a, h->grid_group, 256, s));
-        slots += h->grid_group;
+    if (h->systolic && h->n_tiles) {
+        // windows holding a node to check or to copy
+        HB_LAUNCH(h, hbk::launch_window_flags(h->d_tiles, (uint32_t)h->n_tiles, a.mbc, a.curr_mod,
+                                              h->d_win_flags, s));
     }
-    if (h->n_medium) {
-        a.list = h->d_medium;
-        a.list_len = h->n_medium;
-        a.nf_partials = h->d_nf_partials + slots;
-        HB_LAUNCH(h, hbk::launch_union_team(h->log2m, 32, a, h->grid_warp, s));
-        slots += h->grid_warp;
-    }
+    HB_CUDA(h, cudaEventRecord(h->ev[1], s));
+    if (h->n_tiles) HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, h->grid_tile, s));
     if (h->n_heavy) {
         a.list = h->d_heavy;
         a.list_len = h->n_heavy;
-        a.nf_partials = h->d_nf_partials + slots;
-        HB_LAUNCH(h, hbk::launch_union_team(h->log2m, 256, a, h->grid_cta, s));
-        slots += h->grid_cta;
+        HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, a, h->grid_heavy, s));
     }
     HB_CUDA(h, cudaEventRecord(h->ev[2], s));
+    if (n) HB_LAUNCH(h, hbk::launch_finalize(h->log2m, a, h->grid_fin, s));
     if (h->systolic)
         HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
-                                            h->d_bits[h->mbc_cur ^ 1], n, h->grid_group, s));
-    HB_LAUNCH(h, hbk::launch_reduce_nf(h->d_nf_partials, slots, h->d_nf_out, s));
+                                            h->d_bits[h->mbc_cur ^ 1], n, h->grid_mark, s));
+    HB_LAUNCH(h, hbk::launch_reduce_partials(h->d_partials, h->n_partials, h->d_partial_scratch,
+                                             h->d_partial_out, s));
+    hbk::TilePartial tot{};
+    HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partial_out, sizeof(tot), cudaMemcpyDeviceToHost, s));
+    HB_CUDA(h, cudaEventRecord(h->ev[3], s));
+    HB_CUDA(h, cudaStreamSynchronize(s));
     struct {
         unsigned long long st[4];
         double nf;
-    } host{};
-    HB_CUDA(h, cudaMemcpyAsync(host.st, h->d_stats, sizeof(host.st), cudaMemcpyDeviceToHost, s));
-    HB_CUDA(h, cudaMemcpyAsync(&host.nf, h->d_nf_out, sizeof(double), cudaMemcpyDeviceToHost, s));
-    HB_CUDA(h, cudaEventRecord(h->ev[3], s));
-    HB_CUDA(h, cudaStreamSynchronize(s));
+    } host{{tot.vis, tot.mod, tot.scanned, 0}, tot.nf};
 
     // swap states (HB:909-914)
     h->cur ^= 1;
@@ -575,54 +594,90 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
                           "cudaMemcpy")))
             return fail(r);
     }
-    // degree buckets (static: the graph does not change)
+    // Work partition (static: the graph does not change). Nodes are cut into
+    // windows of consecutive ids; inside a window, light (out-degree <=
+    // small_max) and medium (up to medium_max) nodes are listed by decreasing
+    // out-degree so that neighbouring lanes walk equally long lists. Nodes
+    // above medium_max run one CTA each, heaviest first.
     h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
     h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
     if (h->medium_max < h->small_max) h->medium_max = h->small_max;
     {
-        std::vector<uint32_t> med, hvy;
-        for (uint64_t v = 0; v < n; v++) {
-            const uint64_t d = graph->offsets[v + 1] - graph->offsets[v];
-            if (d > h->medium_max)
-                hvy.push_back((uint32_t)v);
-            else if (d > h->small_max)
-                med.push_back((uint32_t)v);
+        uint32_t win_nodes = 0, win_arcs = 0, per_light = 0, per_medium = 0;
+        hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
+        hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
+        std::vector<uint32_t> hvy, tiles, perm, light, medium;
+        std::vector<uint2> chunks;
+        auto deg = [&](uint32_t x) { return graph->offsets[x + 1] - graph->offsets[x]; };
+        auto by_degree = [&](uint32_t x, uint32_t y) { return deg(x) > deg(y); };
+        perm.reserve(n);
+        for (uint64_t w0 = 0; w0 < n; w0 += win_nodes) {
+            const uint64_t w1 = std::min<uint64_t>(n, w0 + win_nodes);
+            tiles.push_back((uint32_t)w0);
+            light.clear();
+            medium.clear();
+            for (uint64_t v = w0; v < w1; v++) {
+                const uint64_t d = deg((uint32_t)v);
+                if (d > h->medium_max)
+                    hvy.push_back((uint32_t)v);
+                else if (d > h->small_max)
+                    medium.push_back((uint32_t)v);
+                else
+                    light.push_back((uint32_t)v);
+            }
+            std::stable_sort(light.begin(), light.end(), by_degree);
+            std::stable_sort(medium.begin(), medium.end(), by_degree);
+            for (size_t i = 0; i < medium.size(); i += per_medium) {
+                const uint32_t c = (uint32_t)std::min<size_t>(per_medium, medium.size() - i);
+                chunks.push_back(make_uint2((uint32_t)(perm.size() + i), c | 0x80000000u));
+            }
+            perm.insert(perm.end(), medium.begin(), medium.end());
+            for (size_t i = 0; i < light.size(); i += per_light) {
+                const uint32_t c = (uint32_t)std::min<size_t>(per_light, light.size() - i);
+                chunks.push_back(make_uint2((uint32_t)(perm.size() + i), c));
+            }
+            perm.insert(perm.end(), light.begin(), light.end());
         }
-        // heaviest first so the long CTA teams start early
-        std::stable_sort(hvy.begin(), hvy.end(), [&](uint32_t x, uint32_t y) {
-            return graph->offsets[x + 1] - graph->offsets[x] > graph->offsets[y + 1] - graph->offsets[y];
-        });
-        h->n_medium = med.size();
+        if (n) tiles.push_back((uint32_t)n);
+        h->n_tiles = n ? tiles.size() - 1 : 0;
+        h->n_chunks = chunks.size();
+        std::stable_sort(hvy.begin(), hvy.end(), by_degree);
         h->n_heavy = hvy.size();
-        if (h->n_medium) {
-            if ((r = dalloc(hp, &h->d_medium, h->n_medium))) return fail(r);
-            if ((r = cuda_err(hp, cudaMemcpy(h->d_medium, med.data(), h->n_medium * 4, cudaMemcpyHostToDevice),
-                              "cudaMemcpy")))
-                return fail(r);
-        }
-        if (h->n_heavy) {
-            if ((r = dalloc(hp, &h->d_heavy, h->n_heavy))) return fail(r);
-            if ((r = cuda_err(hp, cudaMemcpy(h->d_heavy, hvy.data(), h->n_heavy * 4, cudaMemcpyHostToDevice),
-                              "cudaMemcpy")))
-                return fail(r);
-        }
+        auto upload = [&](auto** dst, const auto& src) {
+            int rr = dalloc(hp, dst, src.size());
+            if (rr) return rr;
+            if (src.empty()) return (int)HB_OK;
+            return cuda_err(hp,
+                            cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice),
+                            "cudaMemcpy");
+        };
+        if ((r = upload(&h->d_tiles, tiles))) return fail(r);
+        if ((r = upload(&h->d_perm, perm))) return fail(r);
+        if ((r = upload(&h->d_chunks, chunks))) return fail(r);
+        if (h->n_heavy && (r = upload(&h->d_heavy, hvy))) return fail(r);
+        if ((r = dalloc(hp, &h->d_win_flags, h->n_tiles + 1))) return fail(r);
     }
-    h->grid_group = hbk::union_grid(h->log2m, 0, h->device);
+    h->grid_tile = hbk::tile_grid(h->log2m, h->device);
+    {
+        // one warp per chunk, 8 warps per block
+        const uint64_t need = (h->n_chunks + 7) / 8 + 1;
+        if ((uint64_t)h->grid_tile > need) h->grid_tile = (int)need;
+    }
+    h->grid_heavy = hbk::heavy_grid(h->log2m, h->device);
+    if ((uint64_t)h->grid_heavy > h->n_heavy + 1) h->grid_heavy = (int)(h->n_heavy + 1);
+    h->grid_mark = 8 * hbk::num_sms(h->device);
+    h->grid_fin = hbk::finalize_grid(h->log2m, h->device);
     {
         const uint64_t need = (n + 255) / 256 + 1;
-        if ((uint64_t)h->grid_group > need) h->grid_group = (int)need;
+        if ((uint64_t)h->grid_fin > need) h->grid_fin = (int)need;
     }
-    h->grid_warp = hbk::union_grid(h->log2m, 1, h->device);
-    {
-        const uint64_t need = (h->n_medium * 32 + 255) / 256 + 1;
-        if ((uint64_t)h->grid_warp > need) h->grid_warp = (int)need;
-    }
-    h->grid_cta = hbk::union_grid(h->log2m, 2, h->device);
-    if ((uint64_t)h->grid_cta > h->n_heavy + 1) h->grid_cta = (int)(h->n_heavy + 1);
-    h->nf_slots = h->grid_group + h->grid_warp + h->grid_cta;
-    if ((r = dalloc(hp, &h->d_nf_partials, h->nf_slots))) return fail(r);
-    if ((r = dalloc(hp, &h->d_nf_out, 1))) return fail(r);
-    if ((r = dalloc(hp, &h->d_stats, 4))) return fail(r);
+    // partial slots: one per finalize block (neighbourhood function), then one
+    // accumulating the union kernels' integer totals
+    h->n_partials = (uint64_t)h->grid_fin + 1;
+    if ((r = dalloc(hp, &h->d_partials, h->n_partials))) return fail(r);
+    if ((r = dalloc(hp, &h->d_partial_scratch, 256))) return fail(r);
+    if ((r = dalloc(hp, &h->d_partial_out, 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_any31, 1))) return fail(r);
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     *out = h.release();
     return HB_OK;

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include <vector_types.h>
+
 #include "../../include/hyperball_gb300.h"
 
 // Host CSR graph: offsets[n+1] (u64), successors[m] (u32), rows sorted.
@@ -31,6 +33,15 @@ namespace hbk {
 
 constexpr int MAX_DISCOUNT = 8;
 
+// What one tile (or one block of the heavy-node kernel) contributes to an
+// iteration; summed in a fixed order after the union kernels.
+struct TilePartial {
+    double nf;                    // neighbourhood-function contribution
+    unsigned long long vis;       // visited arcs
+    unsigned long long mod;       // modified counters
+    unsigned long long scanned;   // scanned nodes
+};
+
 // Everything the union kernels read or write in one iteration.
 struct UnionArgs {
     const uint64_t* off;      // CSR offsets, n+1
@@ -48,15 +59,25 @@ struct UnionArgs {
     int ndisc;
     int systolic;             // 1: scan only must-be-checked nodes
     int quirk;                // Rust i32-shift count semantics
+    int any31;                // some register may hold 31 (only then count looks for it)
     uint32_t iter;            // 0-based iteration number
     uint64_t n;
     double alpha_m_m;
+    double a_scaled;          // alpha_m_m * 2^31
+    long long small_bits;     // bit pattern of 2.5 * m
+    double d1, rd1;           // iteration + 1 and RN(1 / (iteration + 1))
     const double* ln_table;   // m * ln(m / z), z = 0..m
-    const uint32_t* list;     // node list (team kernels) or null
+    const uint32_t* list;     // heavy node list
     uint64_t list_len;
-    uint32_t small_max_degree;// group kernel skips nodes above this degree
-    unsigned long long* stats_out; // [visited arcs, modified counters, scanned nodes]
-    double* nf_partials;      // one slot per block of this launch
+    const uint32_t* tiles;    // window k = nodes [tiles[k], tiles[k+1])
+    uint32_t n_tiles;         // number of windows
+    const uint8_t* win_flags; // systolic: window holds a node to check or copy
+    const uint32_t* perm;     // per window: medium nodes then light nodes, largest degree first
+    const uint2* chunks;      // {first perm index, count | medium << 31}, in node order
+    uint64_t n_chunks;
+    uint32_t tile_max_degree; // nodes above this out-degree are listed as heavy
+    uint32_t acc_slot;        // partial slot accumulating the union kernels' integer totals
+    TilePartial* partials;    // one per finalize block, then acc_slot
 };
 
 struct InitArgs {
@@ -70,15 +91,33 @@ struct InitArgs {
     double alpha_m_m;
     const double* ln_table;
     int quirk;
+    int* any31;               // set to 1 when an initial register holds 31
 };
 
 // Launchers (hb_kernels.cu). All return cudaError_t as int.
 int launch_init(int log2m, const InitArgs& a, void* stream);
-int launch_union_group(int log2m, const UnionArgs& a, int grid, int block, void* stream);
-int launch_union_team(int log2m, int team, const UnionArgs& a, int grid, void* stream);
+// persistent tile kernel over the worklist (or all tiles)
+int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream);
+int tile_grid(int log2m, int device);
+// nodes and staged arcs one tile holds at this log2m
+int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);
+// heavy nodes, one CTA each
+int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream);
+int heavy_grid(int log2m, int device);
+// counts, neighbourhood function and per-node sums of the changed nodes;
+// writes partials[0 .. grid)
+int launch_finalize(int log2m, const UnionArgs& a, int grid, void* stream);
+int finalize_grid(int log2m, int device);
+int launch_window_flags(const uint32_t* tiles, uint32_t n_tiles, const uint32_t* mbc,
+                        const uint32_t* curr_mod, uint8_t* flags, void* stream);
+// nodes per chunk of the union kernel: light nodes (lane-group each) and
+// medium nodes (team each)
+int chunk_nodes(int log2m, uint32_t* light, uint32_t* medium);
+// fixed-order sum of `count` partials; scratch holds 256 partials
+int launch_reduce_partials(const TilePartial* in, uint64_t count, TilePartial* scratch,
+                           TilePartial* out, void* stream);
 int launch_mark_preds(const uint32_t* next_mod, const uint64_t* toff, const uint32_t* tsucc,
                       uint32_t* next_mbc, uint64_t n, int grid, void* stream);
-int launch_reduce_nf(const double* partials, int count, double* out, void* stream);
 int launch_fill_u32(uint32_t* p, uint32_t v, uint64_t count, void* stream);
 int launch_transpose_count(const uint32_t* succ, uint64_t m, unsigned long long* indeg,
                            void* stream);
@@ -89,8 +128,6 @@ int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t
                              unsigned long long* cursor, uint32_t* tsucc, void* stream);
 int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m, int* bad,
                     void* stream);
-// Occupancy-derived grid (blocks) for union kernel kind 0 group, 1 warp team, 2 CTA team.
-int union_grid(int log2m, int kind, int device);
 
 int num_sms(int device);
 

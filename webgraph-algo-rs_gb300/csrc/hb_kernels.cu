@@ -2,20 +2,30 @@
 //
 // One HyperBall iteration (reference: HyperBall::iterate / parallel_task,
 // src/algo/hyperball/hyperball_impl.rs:775-1152) runs as
-//   1. k_union_group  — nodes of out-degree <= small_max_degree, one lane-group
-//                       (one lane per 64-register chunk) per node, walking the
-//                       node's successors sequentially;
-//   2. k_union_team<32>  — listed medium nodes, one warp per node;
-//   3. k_union_team<256> — listed heavy nodes, one CTA per node;
-//   4. k_mark_preds   — systolic iterations: predecessors of modified nodes
-//                       (through the transpose) into next-must-be-checked;
-//   5. k_reduce_nf    — neighbourhood-function block partials summed in a
-//                       fixed order (deterministic).
-// All three union kernels share the per-node epilogue (finalize_node):
-// modified test, exact count, neighbourhood-function contribution, per-node
-// f64 sums, next-state store. Only successors flagged in the previous
-// iteration's modified bitmap are merged (HB:1038), so later iterations read
-// little counter data.
+//   1. k_window_flags    — systolic iterations only: one byte per window of
+//                          consecutive nodes, set when the window holds a node
+//                          to check or to copy;
+//   2. k_union_window    — grid-stride sweep, one warp per chunk of nodes in
+//                          node order; every node of out-degree up to
+//                          tile_max_degree: merge of the modified successors'
+//                          counters, modified test, next-state store;
+//   3. k_union_heavy     — the remaining (heavy) nodes, one CTA per node;
+//   4. k_finalize        — warp per word of the new modified bitmap: exact
+//                          count of every changed counter, neighbourhood-
+//                          function contribution, per-node f64 sums;
+//   5. k_mark_preds      — systolic iterations: predecessors of modified nodes
+//                          (through the transpose) into next-must-be-checked;
+//   6. k_reduce_partials — per-block partials (neighbourhood function, visited
+//                          arcs, modified and scanned nodes) summed in a fixed
+//                          order.
+// Only successors flagged in the previous iteration's modified bitmap are
+// merged (HB:1038). The count of an unchanged counter is the cached estimate
+// of the previous iteration, so k_finalize touches changed nodes only.
+//
+// GB300's f64 pipe issues 2 lane-operations per cycle per SM (1/64 of fp32),
+// so the epilogue keeps f64 instructions to the reference's own operations:
+// one division for the estimate, the subtraction, the per-node sums, and a
+// three-instruction correctly rounded division by the iteration number.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,19 +38,17 @@ using namespace hbd;
 
 namespace hbk {
 
-constexpr int STAT_VISITED = 0, STAT_MODIFIED = 1, STAT_SCANNED = 2;
-
 // ---------------------------------------------------------------------------
-// block-level publish of per-thread statistics
+// block-level publish of per-thread statistics into one partial slot
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void publish(double nf, unsigned long long vis, unsigned long long modc,
-                                        unsigned long long scanned, const UnionArgs& a) {
+                                        unsigned long long scanned, TilePartial* slot) {
     __shared__ double s_nf[32];
     __shared__ unsigned long long s_v[32], s_m[32], s_s[32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        nf += __shfl_xor_sync(0xffffffffu, nf, off);
+        nf = __dadd_rn(nf, __shfl_xor_sync(0xffffffffu, nf, off));
         vis += __shfl_xor_sync(0xffffffffu, vis, off);
         modc += __shfl_xor_sync(0xffffffffu, modc, off);
         scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
@@ -57,158 +65,348 @@ __device__ __forceinline__ void publish(double nf, unsigned long long vis, unsig
         unsigned long long tv = 0, tm = 0, ts = 0;
         const int nwarps = (blockDim.x + 31) >> 5;
         for (int w = 0; w < nwarps; w++) {
-            t += s_nf[w];
+            t = __dadd_rn(t, s_nf[w]);
             tv += s_v[w];
             tm += s_m[w];
             ts += s_s[w];
         }
-        a.nf_partials[blockIdx.x] = t;
-        if (tv) atomicAdd(a.stats_out + STAT_VISITED, tv);
-        if (tm) atomicAdd(a.stats_out + STAT_MODIFIED, tm);
-        if (ts) atomicAdd(a.stats_out + STAT_SCANNED, ts);
+        *slot = TilePartial{t, tv, tm, ts};
     }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
-// per-node epilogue, run by the G lanes (one per chunk) of a team
+// end of a node's union, run by the G lanes (one per chunk) of a team: store
+// the merged counter into the next state; true when it differs from the
+// previous one (HB:1052). Counting is left to k_finalize.
 // ---------------------------------------------------------------------------
 template <int LOG2M>
-__device__ __forceinline__ bool finalize_node(const UnionArgs& a, uint64_t v, int c,
-                                              unsigned team_mask,
-                                              const uint32_t (&prev)[Geo<LOG2M>::NW],
-                                              const uint32_t (&acc)[Geo<LOG2M>::NW],
-                                              double& nf_acc) {
+__device__ __forceinline__ bool commit_node(const UnionArgs& a, uint64_t v, int c,
+                                            unsigned team_mask,
+                                            const uint32_t (&prev)[Geo<LOG2M>::NW],
+                                            const uint32_t (&acc)[Geo<LOG2M>::NW]) {
     using Gm = Geo<LOG2M>;
-    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW;
     uint32_t diff = 0;
 #pragma unroll
     for (int i = 0; i < NW; i++) diff |= prev[i] ^ acc[i];
     bool changed = diff != 0u;
     if constexpr (G > 1) changed = __any_sync(team_mask, changed);
     store_chunk<LOG2M>(a.next, v, c, acc);
-    if (changed) {
-        uint64_t hs = 0;
-        uint32_t z = 0, c31 = 0;
-        count_chunk<REGS>(acc, hs, z, c31);
-        if constexpr (G > 1) {
-#pragma unroll
-            for (int off = 1; off < G; off <<= 1) {
-                hs += __shfl_xor_sync(team_mask, hs, off);
-                z += __shfl_xor_sync(team_mask, z, off);
-                c31 += __shfl_xor_sync(team_mask, c31, off);
-            }
-        }
-        if (c == 0) {
-            const double post =
-                estimate(signed_hsum(hs, c31, a.quirk), z, a.alpha_m_m, (double)Gm::M, a.ln_table);
-            const double pre = a.est[v];
-            a.est[v] = post;
-            if (a.systolic) {
-                nf_acc = __dadd_rn(nf_acc, -pre);
-                nf_acc = __dadd_rn(nf_acc, post);
-            } else {
-                nf_acc = __dadd_rn(nf_acc, post);
-            }
-            const double delta = __dsub_rn(post, pre);
-            if (delta > 0.0) {
-                const double d1 = (double)(a.iter + 1);
-                if (a.sod) a.sod[v] = __dadd_rn(a.sod[v], __dmul_rn(delta, d1));
-                if (a.harm) a.harm[v] = __dadd_rn(a.harm[v], __ddiv_rn(delta, d1));
-                for (int k = 0; k < a.ndisc; k++)
-                    a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, a.disc_factor[k]));
-            }
-        }
-    } else if (!a.systolic && c == 0) {
-        nf_acc = __dadd_rn(nf_acc, a.est[v]);
-    }
     return changed;
 }
 
 // ---------------------------------------------------------------------------
-// light nodes: one team of G lanes per node, nodes in index order
+// k_finalize: the per-node arithmetic of HB:1052-1093 for every node whose
+// counter changed (and, in standard iterations, the count of every node for
+// the neighbourhood function). One warp per 32 consecutive nodes, so loads
+// are coalesced and all lanes run the f64 instructions together:
+//   post = count(next counter)  (exact integer harmonic sum, one division)
+//   pre  = cached count of the previous counter
+//   NF  += post (standard) or post - pre (systolic)
+//   delta = post - pre; if delta > 0: sod += delta*(t+1), harm += delta/(t+1),
+//   discounted sums += delta*f(t+1)
+// Partial NF sums per block (fixed grid and assignment: reproducible).
 // ---------------------------------------------------------------------------
 template <int LOG2M>
-__global__ void __launch_bounds__(256) k_union_group(UnionArgs a) {
+__global__ void __launch_bounds__(256) k_finalize(UnionArgs a) {
     using Gm = Geo<LOG2M>;
-    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS, NPW = 32 / G;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
     const int lane = threadIdx.x & 31;
-    const int c = lane % G, slot = lane / G;
-    const unsigned team_mask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * G));
+    const uint64_t nwords = (a.n + 31) >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    double nf_acc = 0.0;
-    unsigned long long vis = 0, modc = 0, scanned = 0;
-    for (uint64_t wb = gw * NPW; wb < a.n; wb += nw * NPW) {
-        const uint64_t v = wb + slot;
-        bool scan = false, copy = false;
-        uint64_t s0 = 0, s1 = 0;
-        if (v < a.n) {
-            s0 = __ldg(a.off + v);
-            s1 = __ldg(a.off + v + 1);
-            if (s1 - s0 <= a.small_max_degree) {
-                if (!a.systolic || test_bit(a.mbc, v))
-                    scan = true;
-                else if (test_bit(a.curr_mod, v))
-                    copy = true;
+    double nf = 0.0;
+    for (uint64_t w = gw; w < nwords; w += nw) {
+        const uint32_t bits = __ldg(a.next_mod + w);
+        if (a.systolic && bits == 0u) continue;
+        const uint64_t v = (w << 5) + lane;
+        if (v >= a.n) continue;
+        if ((bits >> lane) & 1u) {
+            uint64_t hs = 0;
+            uint32_t z = 0, c31 = 0;
+#pragma unroll 1
+            for (int c = 0; c < G; c++) {
+                uint32_t x[NW];
+                load_chunk<LOG2M>(a.next, v, c, x);
+                count_chunk<REGS>(x, hs, z, c31, a.any31 != 0);
             }
-        }
-        bool changed = false;
-        if (scan) {
-            uint32_t prev[NW], acc[NW];
-            load_chunk<LOG2M>(a.curr, v, c, prev);
-#pragma unroll
-            for (int i = 0; i < NW; i++) acc[i] = prev[i];
-            for (uint64_t e = s0; e < s1; e++) {
-                const uint32_t s = __ldg(a.succ + e);
-                if (s != v && test_bit(a.curr_mod, s)) {
-                    vis += (c == 0);
-                    uint32_t y[NW];
-                    load_chunk<LOG2M>(a.curr, s, c, y);
-                    merge_chunk<REGS>(acc, y);
-                }
+            const double pre = a.est[v];
+            const double post = estimate_fast(signed_hsum(hs, c31, a.quirk), z, a.alpha_m_m,
+                                              a.a_scaled, a.small_bits, (double)Gm::M, a.ln_table);
+            a.est[v] = post;
+            if (a.systolic) {
+                nf = __dadd_rn(nf, -pre);
+                nf = __dadd_rn(nf, post);
+            } else {
+                nf = __dadd_rn(nf, post);
             }
-            changed = finalize_node<LOG2M>(a, v, c, team_mask, prev, acc, nf_acc);
-            scanned += (c == 0);
-        } else if (copy) {
-            uint32_t prev[NW];
-            load_chunk<LOG2M>(a.curr, v, c, prev);
-            store_chunk<LOG2M>(a.next, v, c, prev);
-        }
-        __syncwarp();
-        const unsigned bits =
-            __reduce_or_sync(0xffffffffu, (changed && c == 0) ? (1u << slot) : 0u);
-        if (lane == 0 && bits) {
-            atomicOr(a.next_mod + (wb >> 5), bits << (wb & 31));
-            modc += __popc(bits);
+            const double delta = __dsub_rn(post, pre);
+            // delta > 0.0 as an integer test: positive, not NaN
+            const long long db = __double_as_longlong(delta);
+            if (db > 0 && db <= 0x7ff0000000000000ll) {
+                if (a.sod) a.sod[v] = __dadd_rn(a.sod[v], __dmul_rn(delta, a.d1));
+                if (a.harm) a.harm[v] = __dadd_rn(a.harm[v], div_by_small_int(delta, a.d1, a.rd1));
+                for (int k = 0; k < a.ndisc; k++)
+                    a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, a.disc_factor[k]));
+            }
+        } else if (!a.systolic) {
+            nf = __dadd_rn(nf, a.est[v]);
         }
     }
-    publish(nf_acc, vis, modc, scanned, a);
+    publish(nf, 0, 0, 0, a.partials + blockIdx.x);
+}
+
+// Merges into acc (chunk c) the counters of the successors in [e, e1) of node v
+// that were modified in the previous iteration; `stride` arcs apart. Two
+// successors per step keep two counter gathers in flight per lane.
+template <int LOG2M>
+__device__ __forceinline__ void gather_successors(const UnionArgs& a, uint64_t v, int c,
+                                                  uint64_t e, uint64_t e1, uint64_t stride,
+                                                  uint32_t (&acc)[Geo<LOG2M>::NW],
+                                                  unsigned long long& vis) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    for (; e + stride < e1; e += 2 * stride) {
+        const uint32_t sa = __ldg(a.succ + e), sb = __ldg(a.succ + e + stride);
+        const bool ma = sa != v && test_bit(a.curr_mod, sa);
+        const bool mb = sb != v && test_bit(a.curr_mod, sb);
+        uint32_t ya[NW], yb[NW];
+        if (ma) load_chunk<LOG2M>(a.curr, sa, c, ya);
+        if (mb) load_chunk<LOG2M>(a.curr, sb, c, yb);
+        if (ma) merge_chunk<REGS>(acc, ya);
+        if (mb) merge_chunk<REGS>(acc, yb);
+        vis += (unsigned long long)ma + (unsigned long long)mb;
+    }
+    if (e < e1) {
+        const uint32_t s = __ldg(a.succ + e);
+        if (s != v && test_bit(a.curr_mod, s)) {
+            uint32_t y[NW];
+            load_chunk<LOG2M>(a.curr, s, c, y);
+            merge_chunk<REGS>(acc, y);
+            vis++;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
-// listed nodes: one team of TEAM threads (warp or CTA) per node
+// windows and chunks: every node up to tile_max_degree
+//
+// The graph never changes, so the work order is fixed once at build time:
+// nodes are cut into windows of WINDOW consecutive ids; inside a window the
+// medium nodes (out-degree above the light bound, up to tile_max_degree) and
+// then the light nodes are listed by decreasing out-degree in one host-built
+// permutation. The permutation is cut into chunks of one warp-step each
+// (32/G light nodes, one lane-group each, or 32/TB_MED medium nodes, one
+// team each), and the chunk table follows node order. Nodes above
+// tile_max_degree go to k_union_heavy.
+//
+// k_union_window sweeps the chunk table with a grid stride, so the warps in
+// flight at any moment work on a narrow band of consecutive node ids; with
+// URL-order locality their successors cluster around that band and its
+// counters stay L2-resident while the band passes. Systolic iterations skip
+// the chunks of windows without work. Neighbouring lanes walk successor
+// lists of equal length; each lane keeps PIPE counter gathers in flight while
+// the ids and modified bits of the next PIPE successors load.
 // ---------------------------------------------------------------------------
-template <int LOG2M, int TEAM>
-__global__ void __launch_bounds__(256) k_union_team(UnionArgs a) {
+constexpr int WINDOW = 1024;
+constexpr int PIPE = 2;
+
+template <int LOG2M>
+struct TileGeo {
+    static constexpr int NODES = WINDOW;
+    static constexpr int ARCS = 1 << 30;  // no per-window arc limit
+};
+
+// Merges into acc (chunk c) the counters of the successors e0, e0+stride, ...
+// (< e1) of node v modified in the previous iteration; returns how many were
+// merged (self-loops excluded).
+template <int LOG2M>
+__device__ __forceinline__ uint32_t gather_pipelined(const UnionArgs& a, uint64_t v, int c,
+                                                     uint64_t e0, uint64_t e1, uint32_t stride,
+                                                     uint32_t (&acc)[Geo<LOG2M>::NW],
+                                                     uint32_t& grew) {
     using Gm = Geo<LOG2M>;
-    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS, P = TEAM / G;
-    constexpr int WARPS = TEAM / 32;
-    __shared__ uint32_t red[WARPS > 1 ? WARPS : 1][G][NW];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int tid = TEAM == 32 ? lane : (int)threadIdx.x;
-    const int p = tid / G, c = tid % G;
-    uint64_t team_id, nteams;
-    if (TEAM == 32) {
-        team_id = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-        nteams = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    } else {
-        team_id = blockIdx.x;
-        nteams = gridDim.x;
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    const uint32_t vv = (uint32_t)v;
+    uint32_t cnt = 0;
+    uint32_t s[PIPE];
+    bool m[PIPE];
+#pragma unroll
+    for (int k = 0; k < PIPE; k++) {
+        const uint64_t e = e0 + (uint64_t)k * stride;
+        s[k] = e < e1 ? __ldg(a.succ + e) : vv;
     }
-    const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
-    double nf_acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < PIPE; k++) m[k] = s[k] != vv && test_bit(a.curr_mod, s[k]);
+    for (uint64_t e = e0; e < e1; e += (uint64_t)PIPE * stride) {
+        uint32_t y[PIPE][NW];
+#pragma unroll
+        for (int k = 0; k < PIPE; k++)
+            if (m[k]) load_chunk<LOG2M>(a.curr, s[k], c, y[k]);
+        uint32_t ns[PIPE];
+#pragma unroll
+        for (int k = 0; k < PIPE; k++) {
+            const uint64_t en = e + (uint64_t)(PIPE + k) * stride;
+            ns[k] = en < e1 ? __ldg(a.succ + en) : vv;
+        }
+        bool nm[PIPE];
+#pragma unroll
+        for (int k = 0; k < PIPE; k++) nm[k] = ns[k] != vv && test_bit(a.curr_mod, ns[k]);
+#pragma unroll
+        for (int k = 0; k < PIPE; k++) {
+            if (m[k]) {
+                merge_chunk<REGS>(acc, y[k], grew);
+                cnt++;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PIPE; k++) {
+            s[k] = ns[k];
+            m[k] = nm[k];
+        }
+    }
+    return cnt;
+}
+
+// One warp-step over up to 32/G nodes of a list: scan, copy or nothing.
+// Returns through the accumulators; sets the modified bits.
+template <int LOG2M, int TB>
+__device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ perm,
+                                          uint32_t b, uint32_t e, unsigned long long& vis,
+                                          unsigned long long& modc, unsigned long long& scanned) {
+    using Gm = Geo<LOG2M>;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    constexpr int PB = TB / G;   // arc lanes per node
+    constexpr int NPW = 32 / TB; // nodes per warp-step
+    const int lane = threadIdx.x & 31;
+    const int slot = lane / TB, tl = lane % TB, p = tl / G, c = tl % G;
+    const unsigned tmask = TB == 32 ? 0xffffffffu : (((1u << TB) - 1u) << (slot * TB));
+    const unsigned lmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * TB));
+    for (uint32_t base = b; base < e; base += NPW) {
+        const uint32_t idx = base + slot;
+        bool scan = false, copy = false;
+        uint64_t v = 0;
+        if (idx < e) {
+            v = __ldg(perm + idx);
+            if (!a.systolic || test_bit(a.mbc, v))
+                scan = true;
+            else if (test_bit(a.curr_mod, v))
+                copy = true;
+        }
+        bool changed = false;
+        if (scan) {
+            const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
+            uint32_t acc[NW];
+            if (PB == 1 || p == 0) {
+                load_chunk<LOG2M>(a.curr, v, c, acc);
+            } else {
+#pragma unroll
+                for (int k = 0; k < NW; k++) acc[k] = 0u;
+            }
+            uint32_t grew = 0;
+            uint32_t w = gather_pipelined<LOG2M>(a, v, c, s0 + p, s1, PB, acc, grew);
+            if constexpr (PB > 1) {
+                __syncwarp(tmask);
+#pragma unroll
+                for (int off = G; off < TB; off <<= 1) {
+                    uint32_t y[NW];
+#pragma unroll
+                    for (int k = 0; k < NW; k++) y[k] = __shfl_xor_sync(tmask, acc[k], off);
+                    merge_chunk<REGS>(acc, y);
+                }
+                if (c != 0) w = 0;
+#pragma unroll
+                for (int off = G; off < TB; off <<= 1) w += __shfl_xor_sync(tmask, w, off);
+                if (p == 0) {
+                    // partial counters started empty: compare with the previous counter
+                    uint32_t prev[NW];
+                    load_chunk<LOG2M>(a.curr, v, c, prev);
+                    grew = 0;
+#pragma unroll
+                    for (int k = 0; k < NW; k++) grew |= prev[k] ^ acc[k];
+                }
+            }
+            if (p == 0) {
+                changed = grew != 0u;
+                if constexpr (G > 1) changed = __any_sync(lmask, changed);
+                store_chunk<LOG2M>(a.next, v, c, acc);
+                if (c == 0) {
+                    scanned++;
+                    vis += w;
+                }
+            }
+        } else if (copy && p == 0) {
+            uint32_t w[NW];
+            load_chunk<LOG2M>(a.curr, v, c, w);
+            store_chunk<LOG2M>(a.next, v, c, w);
+        }
+        // modified bits, aggregated over the lanes that hit the same word
+        const bool flag = changed && p == 0 && c == 0;
+        const unsigned want = __ballot_sync(0xffffffffu, flag);
+        if (want) {
+            const uint32_t word = flag ? (uint32_t)(v >> 5) : 0xffffffffu;
+            const unsigned peers = __match_any_sync(0xffffffffu, word);
+            // each group of lanes on one word reduces with its own mask
+            const uint32_t bits = __reduce_or_sync(peers, flag ? (1u << (v & 31)) : 0u);
+            if (flag && lane == __ffs(peers) - 1) atomicOr(a.next_mod + word, bits);
+            modc += flag;
+        }
+    }
+}
+
+template <int LOG2M>
+__global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
+    using Gm = Geo<LOG2M>;
+    constexpr int G = Gm::CHUNKS;
+    constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long vis = 0, modc = 0, scanned = 0;
-    for (uint64_t idx = team_id; idx < a.list_len; idx += nteams) {
+    // Warp w takes chunks w, w+W, ...: all warps sweep the node range
+    // together, so the counters of nearby successors stay in L2.
+    for (uint64_t k = gw; k < a.n_chunks; k += nw) {
+        const uint2 d = __ldg(a.chunks + k);
+        const uint32_t cnt = d.y & 0x7fffffffu;
+        if (a.systolic && !__ldg(a.win_flags + __ldg(a.perm + d.x) / WINDOW)) continue;
+        if (d.y >> 31)
+            run_nodes<LOG2M, TB_MED>(a, a.perm, d.x, d.x + cnt, vis, modc, scanned);
+        else
+            run_nodes<LOG2M, G>(a, a.perm, d.x, d.x + cnt, vis, modc, scanned);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
+        modc += __shfl_xor_sync(0xffffffffu, modc, off);
+        scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+    }
+    if (lane == 0) {
+        // integer totals are order independent
+        TilePartial* t = a.partials + a.acc_slot;
+        if (vis) atomicAdd(&t->vis, vis);
+        if (modc) atomicAdd(&t->mod, modc);
+        if (scanned) atomicAdd(&t->scanned, scanned);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// heavy nodes: one CTA per node. Lanes split the successors (G lanes per
+// counter), the per-lane partial counters are merged by a butterfly of
+// shuffles and then across warps through shared memory.
+// ---------------------------------------------------------------------------
+template <int LOG2M>
+__global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
+    using Gm = Geo<LOG2M>;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    constexpr int TEAM = 256, P = TEAM / G, WARPS = TEAM / 32;
+    __shared__ uint32_t red[WARPS][G][NW];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int tid = threadIdx.x;
+    const int p = tid / G, c = tid % G;
+    const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
+    unsigned long long vis = 0, modc = 0, scanned = 0;
+    for (uint64_t idx = blockIdx.x; idx < a.list_len; idx += gridDim.x) {
         const uint64_t v = __ldg(a.list + idx);
         const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
         const bool scan = !a.systolic || test_bit(a.mbc, v);
@@ -222,15 +420,9 @@ __global__ void __launch_bounds__(256) k_union_team(UnionArgs a) {
 #pragma unroll
                 for (int i = 0; i < NW; i++) acc[i] = prev[i] = 0u;
             }
-            for (uint64_t e = s0 + p; e < s1; e += P) {
-                const uint32_t s = __ldg(a.succ + e);
-                if (s != v && test_bit(a.curr_mod, s)) {
-                    vis += (c == 0);
-                    uint32_t y[NW];
-                    load_chunk<LOG2M>(a.curr, s, c, y);
-                    merge_chunk<REGS>(acc, y);
-                }
-            }
+            unsigned long long my_vis = 0;
+            gather_successors<LOG2M>(a, v, c, s0 + p, s1, P, acc, my_vis);
+            if (c == 0) vis += my_vis;
             __syncwarp();
 #pragma unroll
             for (int off = G; off < 32; off <<= 1) {
@@ -239,23 +431,19 @@ __global__ void __launch_bounds__(256) k_union_team(UnionArgs a) {
                 for (int i = 0; i < NW; i++) y[i] = __shfl_xor_sync(0xffffffffu, acc[i], off);
                 merge_chunk<REGS>(acc, y);
             }
-            if constexpr (WARPS > 1) {
-                if (lane < G) {
+            if (lane < G) {
 #pragma unroll
-                    for (int i = 0; i < NW; i++) red[warp][c][i] = acc[i];
-                }
-                __syncthreads();
-                if (warp == 0 && lane < G) {
-                    for (int w = 1; w < WARPS; w++) {
-                        uint32_t y[NW];
-#pragma unroll
-                        for (int i = 0; i < NW; i++) y[i] = red[w][c][i];
-                        merge_chunk<REGS>(acc, y);
-                    }
-                }
+                for (int i = 0; i < NW; i++) red[warp][c][i] = acc[i];
             }
+            __syncthreads();
             if (warp == 0 && lane < G) {
-                const bool changed = finalize_node<LOG2M>(a, v, c, leader_mask, prev, acc, nf_acc);
+                for (int w = 1; w < WARPS; w++) {
+                    uint32_t y[NW];
+#pragma unroll
+                    for (int i = 0; i < NW; i++) y[i] = red[w][c][i];
+                    merge_chunk<REGS>(acc, y);
+                }
+                const bool changed = commit_node<LOG2M>(a, v, c, leader_mask, prev, acc);
                 if (c == 0) {
                     scanned++;
                     if (changed) {
@@ -271,9 +459,21 @@ __global__ void __launch_bounds__(256) k_union_team(UnionArgs a) {
                 store_chunk<LOG2M>(a.next, v, c, prev);
             }
         }
-        if constexpr (WARPS > 1) __syncthreads();
+        __syncthreads();
     }
-    publish(nf_acc, vis, modc, scanned, a);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
+        modc += __shfl_xor_sync(0xffffffffu, modc, off);
+        scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+    }
+    if (lane == 0) {
+        // integer totals are order independent
+        TilePartial* t = a.partials + a.acc_slot;
+        if (vis) atomicAdd(&t->vis, vis);
+        if (modc) atomicAdd(&t->mod, modc);
+        if (scanned) atomicAdd(&t->scanned, scanned);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -293,24 +493,25 @@ __device__ __forceinline__ void set_reg(uint8_t* c, uint32_t j, uint32_t val) {
 }
 
 template <int LOG2M>
-__device__ __forceinline__ void add_hash(uint8_t* counter, uint64_t x) {
+__device__ __forceinline__ uint32_t add_hash(uint8_t* counter, uint64_t x) {
     const uint32_t j = (uint32_t)(x & ((1ull << LOG2M) - 1ull));
     const uint64_t y = (x >> LOG2M) | (1ull << 30);
-    const uint32_t r = (uint32_t)(__ffsll((long long)y) - 1);
-    const uint32_t cand = r + 1u;
+    const uint32_t cand = (uint32_t)__ffsll((long long)y);  // trailing zeros + 1
     if (get_reg(counter, j) < cand) set_reg(counter, j, cand);
+    return cand;
 }
 
 template <int LOG2M>
 __global__ void __launch_bounds__(256) k_init(InitArgs a) {
     using Gm = Geo<LOG2M>;
+    bool saw31 = false;
     for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < a.n;
          v += (uint64_t)gridDim.x * blockDim.x) {
         uint8_t* counter = a.curr + v * (uint64_t)Gm::COUNTER_BYTES;
         if (a.weights == nullptr) {
             const uint64_t x = a.hash_kind == 1 ? hash_jenkins(v, a.seed) : hash_sip13(v);
-            add_hash<LOG2M>(counter, x);
-            const uint32_t val = (uint32_t)__ffsll((long long)((x >> LOG2M) | (1ull << 30)));
+            const uint32_t val = add_hash<LOG2M>(counter, x);
+            saw31 |= val == 31u;
             // one register holds val, the other m-1 are zero
             const uint64_t hs = (uint64_t)(Gm::M - 1) * 0x80000000ull + (uint64_t)(0x80000000u >> val);
             const uint32_t c31 = val == 31u;
@@ -328,7 +529,7 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
                 z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
                 z ^= z >> 31;
                 const uint64_t x = a.hash_kind == 1 ? hash_jenkins(z, a.seed) : hash_sip13(z);
-                add_hash<LOG2M>(counter, x);
+                saw31 |= add_hash<LOG2M>(counter, x) == 31u;
             }
             uint64_t hs = 0;
             uint32_t z = 0, c31 = 0;
@@ -342,6 +543,9 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
                                 a.ln_table);
         }
     }
+    // Registers only ever take values some initial register had; remember
+    // whether 31 occurs so counts can skip looking for it.
+    if (__syncthreads_or(saw31) && threadIdx.x == 0) atomicOr(a.any31, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -370,18 +574,60 @@ __global__ void __launch_bounds__(256) k_mark_preds(const uint32_t* __restrict__
     }
 }
 
-// fixed-order sum of block partials (one block)
-__global__ void k_reduce_nf(const double* __restrict__ partials, int count, double* out) {
-    __shared__ double s[256];
-    double t = 0.0;
-    for (int i = threadIdx.x; i < count; i += blockDim.x) t = __dadd_rn(t, partials[i]);
-    s[threadIdx.x] = t;
+// Fixed-order reduction of the per-tile / per-block partials: stage 1 sums
+// contiguous ranges (one block each), stage 2 sums the stage-1 results, so
+// the neighbourhood function is reproducible run to run.
+constexpr int REDUCE_BLOCKS = 256;
+
+__global__ void k_reduce_partials(const TilePartial* __restrict__ in, uint64_t count,
+                                  TilePartial* __restrict__ out) {
+    __shared__ double s_nf[256];
+    __shared__ unsigned long long s_v[256], s_m[256], s_s[256];
+    const uint64_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint64_t b = (uint64_t)blockIdx.x * per, e = min(count, b + per);
+    double nf = 0.0;
+    unsigned long long v = 0, mo = 0, sc = 0;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        nf = __dadd_rn(nf, in[i].nf);
+        v += in[i].vis;
+        mo += in[i].mod;
+        sc += in[i].scanned;
+    }
+    s_nf[threadIdx.x] = nf;
+    s_v[threadIdx.x] = v;
+    s_m[threadIdx.x] = mo;
+    s_s[threadIdx.x] = sc;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) s[threadIdx.x] = __dadd_rn(s[threadIdx.x], s[threadIdx.x + w]);
+        if ((int)threadIdx.x < w) {
+            s_nf[threadIdx.x] = __dadd_rn(s_nf[threadIdx.x], s_nf[threadIdx.x + w]);
+            s_v[threadIdx.x] += s_v[threadIdx.x + w];
+            s_m[threadIdx.x] += s_m[threadIdx.x + w];
+            s_s[threadIdx.x] += s_s[threadIdx.x + w];
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = s[0];
+    if (threadIdx.x == 0) out[blockIdx.x] = TilePartial{s_nf[0], s_v[0], s_m[0], s_s[0]};
+}
+
+// Systolic iterations: flags the windows holding a node that must be checked
+// or copied; the union kernel skips the chunks of the other windows.
+__global__ void k_window_flags(const uint32_t* __restrict__ tiles, uint32_t n_tiles,
+                               const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
+                               uint8_t* flags) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_tiles; k += gridDim.x * blockDim.x) {
+        const uint64_t r0 = __ldg(tiles + k), r1 = __ldg(tiles + k + 1);
+        bool any = false;
+        for (uint64_t w = r0 >> 5; w <= ((r1 - 1) >> 5) && !any; w++) {
+            uint32_t bits = __ldg(mbc + w) | __ldg(curr_mod + w);
+            // keep only the bits of this window's nodes
+            const uint64_t lo = w << 5;
+            if (r0 > lo) bits &= ~0u << (uint32_t)(r0 - lo);
+            if (r1 < lo + 32) bits &= (1u << (uint32_t)(r1 - lo)) - 1u;
+            any = bits != 0u;
+        }
+        flags[k] = any ? 1 : 0;
+    }
 }
 
 __global__ void k_fill_u32(uint32_t* p, uint32_t v, uint64_t count) {
@@ -414,7 +660,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const unsigned long 
         v[i] = (base + i < count) ? in[base + i] : 0ull;
         t += v[i];
     }
-    // inclusive scan of thread totals across the block
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long x = t;
 #pragma unroll
@@ -477,34 +722,13 @@ __global__ void k_validate(const uint64_t* __restrict__ off, const uint32_t* __r
 }
 
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 int num_sms(int device) {
     int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
     return v > 0 ? v : 1;
-}
-
-template <int LOG2M>
-static int init_impl(const InitArgs& a, cudaStream_t s) {
-    const int grid = (int)std::min<uint64_t>((a.n + 255) / 256 + 1, 65535);
-    k_init<LOG2M><<<grid, 256, 0, s>>>(a);
-    return (int)cudaGetLastError();
-}
-
-template <int LOG2M>
-static int group_impl(const UnionArgs& a, int grid, int block, cudaStream_t s) {
-    k_union_group<LOG2M><<<grid, block, 0, s>>>(a);
-    return (int)cudaGetLastError();
-}
-
-template <int LOG2M>
-static int team_impl(int team, const UnionArgs& a, int grid, cudaStream_t s) {
-    if (team == 32)
-        k_union_team<LOG2M, 32><<<grid, 256, 0, s>>>(a);
-    else
-        k_union_team<LOG2M, 256><<<grid, 256, 0, s>>>(a);
-    return (int)cudaGetLastError();
 }
 
 #define HB_DISPATCH_LOG2M(l, CALL) \
@@ -519,32 +743,141 @@ static int team_impl(int team, const UnionArgs& a, int grid, cudaStream_t s) {
         default: return (int)cudaErrorInvalidValue; \
     }
 
+template <int LOG2M>
+static int init_impl(const InitArgs& a, cudaStream_t s) {
+    const int grid = (int)std::min<uint64_t>((a.n + 255) / 256 + 1, 65535);
+    k_init<LOG2M><<<grid, 256, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int LOG2M>
+static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    k_union_window<LOG2M><<<grid, 256, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int LOG2M>
+static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    k_union_heavy<LOG2M><<<grid, 256, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int LOG2M>
+static int finalize_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    k_finalize<LOG2M><<<grid, 256, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+template <int LOG2M>
+static int finalize_grid_impl(int device) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_finalize<LOG2M>, 256, 0);
+    return std::max(1, per_sm) * num_sms(device);
+}
+
+int launch_finalize(int log2m, const UnionArgs& a, int grid, void* stream) {
+#define CALL(L) finalize_impl<L>(a, grid, (cudaStream_t)stream)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int finalize_grid(int log2m, int device) {
+#define CALL(L) finalize_grid_impl<L>(device)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+template <int LOG2M>
+static int tile_grid_impl(int device) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M>, 256, 0);
+    return std::max(1, per_sm) * num_sms(device);
+}
+
+template <int LOG2M>
+static int heavy_grid_impl(int device) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_heavy<LOG2M>, 256, 0);
+    return std::max(1, per_sm) * num_sms(device);
+}
+
+template <int L>
+static int tile_caps(uint32_t* nodes, uint32_t* arcs) {
+    *nodes = TileGeo<L>::NODES;
+    *arcs = TileGeo<L>::ARCS;
+    return 0;
+}
+
 int launch_init(int log2m, const InitArgs& a, void* stream) {
 #define CALL(L) init_impl<L>(a, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
 }
 
-int launch_union_group(int log2m, const UnionArgs& a, int grid, int block, void* stream) {
-#define CALL(L) group_impl<L>(a, grid, block, (cudaStream_t)stream)
+int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream) {
+#define CALL(L) tile_impl<L>(a, grid, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
 }
 
-int launch_union_team(int log2m, int team, const UnionArgs& a, int grid, void* stream) {
-#define CALL(L) team_impl<L>(team, a, grid, (cudaStream_t)stream)
+int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream) {
+#define CALL(L) heavy_impl<L>(a, grid, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
+}
+
+int tile_grid(int log2m, int device) {
+#define CALL(L) tile_grid_impl<L>(device)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int heavy_grid(int log2m, int device) {
+#define CALL(L) heavy_grid_impl<L>(device)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs) {
+#define CALL(L) tile_caps<L>(nodes, arcs)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+template <int L>
+static int chunk_nodes_impl(uint32_t* light, uint32_t* medium) {
+    constexpr int G = Geo<L>::CHUNKS;
+    constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
+    *light = 32 / G;
+    *medium = 32 / TB_MED;
+    return 0;
+}
+
+int chunk_nodes(int log2m, uint32_t* light, uint32_t* medium) {
+#define CALL(L) chunk_nodes_impl<L>(light, medium)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int launch_window_flags(const uint32_t* tiles, uint32_t n_tiles, const uint32_t* mbc,
+                        const uint32_t* curr_mod, uint8_t* flags, void* stream) {
+    if (n_tiles == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n_tiles + 255) / 256, 4096);
+    k_window_flags<<<grid, 256, 0, (cudaStream_t)stream>>>(tiles, n_tiles, mbc, curr_mod, flags);
+    return (int)cudaGetLastError();
+}
+
+int launch_reduce_partials(const TilePartial* in, uint64_t count, TilePartial* scratch,
+                           TilePartial* out, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    k_reduce_partials<<<REDUCE_BLOCKS, 256, 0, s>>>(in, count, scratch);
+    k_reduce_partials<<<1, 256, 0, s>>>(scratch, REDUCE_BLOCKS, out);
+    return (int)cudaGetLastError();
 }
 
 int launch_mark_preds(const uint32_t* next_mod, const uint64_t* toff, const uint32_t* tsucc,
                       uint32_t* next_mbc, uint64_t n, int grid, void* stream) {
     k_mark_preds<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, toff, tsucc, next_mbc, n);
-    return (int)cudaGetLastError();
-}
-
-int launch_reduce_nf(const double* partials, int count, double* out, void* stream) {
-    k_reduce_nf<<<1, 256, 0, (cudaStream_t)stream>>>(partials, count, out);
     return (int)cudaGetLastError();
 }
 
@@ -608,29 +941,6 @@ int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint6
     const int grid = (int)std::min<uint64_t>((std::max(n, m) + 255) / 256 + 1, 8192);
     k_validate<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, m, bad);
     return (int)cudaGetLastError();
-}
-
-// Occupancy-derived grid for the union kernels.
-int union_grid(int log2m, int kind, int device) {
-    int per_sm = 1;
-    const void* fn = nullptr;
-#define FN(L)                                                                              \
-    (kind == 0 ? (const void*)k_union_group<L>                                            \
-               : (kind == 1 ? (const void*)k_union_team<L, 32> : (const void*)k_union_team<L, 256>))
-    switch (log2m) {
-        case 4: fn = FN(4); break;
-        case 5: fn = FN(5); break;
-        case 6: fn = FN(6); break;
-        case 7: fn = FN(7); break;
-        case 8: fn = FN(8); break;
-        case 9: fn = FN(9); break;
-        case 10: fn = FN(10); break;
-        default: return 1;
-    }
-#undef FN
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
-    if (per_sm < 1) per_sm = 1;
-    return per_sm * num_sms(device);
 }
 
 }  // namespace hbk

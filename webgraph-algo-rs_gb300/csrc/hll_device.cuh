@@ -106,10 +106,12 @@ struct SubChain<10> {
     }
 };
 
-// x = register-wise max(x, y) over one chunk of REGS registers.
+// x = register-wise max(x, y) over one chunk of REGS registers; ORs into
+// `grew` the bits of x that took y's value and changed.
 template <int REGS>
 __device__ __forceinline__ void merge_chunk(uint32_t (&x)[(REGS * 5 + 31) / 32],
-                                            const uint32_t (&y)[(REGS * 5 + 31) / 32]) {
+                                            const uint32_t (&y)[(REGS * 5 + 31) / 32],
+                                            uint32_t& grew) {
     constexpr int NW = (REGS * 5 + 31) / 32;
     uint32_t a[NW], b[NW], z[NW];
 #pragma unroll
@@ -138,37 +140,160 @@ __device__ __forceinline__ void merge_chunk(uint32_t (&x)[(REGS * 5 + 31) / 32],
     for (int i = 0; i < NW; i++) {
         const uint32_t H = mask_word(REGS, i, 4);
         const uint32_t m = (mk[i] | H) ^ z[i];
-        x[i] = x[i] ^ ((x[i] ^ y[i]) & m);
+        const uint32_t d = (x[i] ^ y[i]) & m;
+        grew |= d;
+        x[i] = x[i] ^ d;
     }
 }
 
-// Partial count of one chunk: hsum += sum 2^(31-v), zeroes += #(v==0),
-// c31 += #(v==31).
+template <int REGS>
+__device__ __forceinline__ void merge_chunk(uint32_t (&x)[(REGS * 5 + 31) / 32],
+                                            const uint32_t (&y)[(REGS * 5 + 31) / 32]) {
+    uint32_t unused = 0;
+    merge_chunk<REGS>(x, y, unused);
+}
+
+template <int NW>
+struct AddChain;
+template <>
+struct AddChain<3> {
+    static __device__ __forceinline__ void run(uint32_t (&r)[3], const uint32_t (&a)[3],
+                                               const uint32_t (&b)[3]) {
+        asm("add.cc.u32 %0, %3, %6;\n\t"
+            "addc.cc.u32 %1, %4, %7;\n\t"
+            "addc.u32 %2, %5, %8;"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
+    }
+};
+template <>
+struct AddChain<5> {
+    static __device__ __forceinline__ void run(uint32_t (&r)[5], const uint32_t (&a)[5],
+                                               const uint32_t (&b)[5]) {
+        asm("add.cc.u32 %0, %5, %10;\n\t"
+            "addc.cc.u32 %1, %6, %11;\n\t"
+            "addc.cc.u32 %2, %7, %12;\n\t"
+            "addc.cc.u32 %3, %8, %13;\n\t"
+            "addc.u32 %4, %9, %14;"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(b[0]), "r"(b[1]),
+              "r"(b[2]), "r"(b[3]), "r"(b[4]));
+    }
+};
+template <>
+struct AddChain<10> {
+    static __device__ __forceinline__ void run(uint32_t (&r)[10], const uint32_t (&a)[10],
+                                               const uint32_t (&b)[10]) {
+        asm("add.cc.u32 %0, %10, %20;\n\t"
+            "addc.cc.u32 %1, %11, %21;\n\t"
+            "addc.cc.u32 %2, %12, %22;\n\t"
+            "addc.cc.u32 %3, %13, %23;\n\t"
+            "addc.cc.u32 %4, %14, %24;\n\t"
+            "addc.cc.u32 %5, %15, %25;\n\t"
+            "addc.cc.u32 %6, %16, %26;\n\t"
+            "addc.cc.u32 %7, %17, %27;\n\t"
+            "addc.cc.u32 %8, %18, %28;\n\t"
+            "addc.u32 %9, %19, %29;"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]),
+              "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]),
+              "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]));
+    }
+};
+
+// Partial count of one chunk: hsum += sum over registers of 2^(31-v),
+// zeroes += #(v == 0), and, only when `with31`, c31 += #(v == 31).
+//  * 2^(31-v): funnel-shifting 0x80000000 right by the raw extracted field
+//    uses the shift amount mod 32, so the unmasked field gives the term in
+//    one instruction.
+//  * zero registers, broadword: ((x & ~H) + low4) | x has bit 4 of a
+//    register set iff the register is non-zero (low4 = bits 0-3 of every
+//    register; the add never carries out of a register).
 template <int REGS>
 __device__ __forceinline__ void count_chunk(const uint32_t (&w)[(REGS * 5 + 31) / 32],
-                                            uint64_t& hsum, uint32_t& zeroes, uint32_t& c31) {
+                                            uint64_t& hsum, uint32_t& zeroes, uint32_t& c31,
+                                            bool with31) {
+    constexpr int NW = (REGS * 5 + 31) / 32;
+    uint32_t lo = 0, hi = 0;
 #pragma unroll
     for (int k = 0; k < REGS; k++) {
         const int p = 5 * k;
         const int i = p / 32, s = p % 32;
-        uint32_t v;
-        if (s + 5 <= 32)
-            v = (w[i] >> s) & 31u;
-        else
-            v = __funnelshift_r(w[i], w[(i + 1) < (REGS * 5 + 31) / 32 ? i + 1 : i], s) & 31u;
-        hsum += (uint64_t)(0x80000000u >> v);
-        zeroes += (v == 0u);
-        c31 += (v == 31u);
+        const uint32_t raw =
+            (s + 5 <= 32) ? (w[i] >> s) : __funnelshift_r(w[i], w[(i + 1) < NW ? i + 1 : i], s);
+        const uint32_t term = __funnelshift_r(0x80000000u, 0u, raw);
+        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, 0;" : "+r"(lo), "+r"(hi) : "r"(term));
+    }
+    hsum += ((uint64_t)hi << 32) | lo;
+    uint32_t t[NW], low4[NW], sum[NW];
+#pragma unroll
+    for (int i = 0; i < NW; i++) {
+        const uint32_t H = mask_word(REGS, i, 4);
+        low4[i] = mask_word(REGS, i, 0) | mask_word(REGS, i, 1) | mask_word(REGS, i, 2) |
+                  mask_word(REGS, i, 3);
+        t[i] = w[i] & ~H;
+    }
+    AddChain<NW>::run(sum, t, low4);
+    uint32_t nz = 0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) nz += __popc((sum[i] | w[i]) & mask_word(REGS, i, 4));
+    zeroes += (uint32_t)REGS - nz;
+    if (with31) {
+#pragma unroll
+        for (int k = 0; k < REGS; k++) {
+            const int p = 5 * k;
+            const int i = p / 32, s = p % 32;
+            const uint32_t raw = (s + 5 <= 32) ? (w[i] >> s)
+                                               : __funnelshift_r(w[i], w[(i + 1) < NW ? i + 1 : i], s);
+            c31 += ((raw & 31u) == 31u);
+        }
     }
 }
 
-// HLL:181-185 from the exact integer harmonic sum.
+// HLL:181-185 from the exact integer harmonic sum (reference arithmetic, f64
+// pipe). Used where counts are rare (init, weighted init).
 __device__ __forceinline__ double estimate(int64_t hsum, uint32_t zeroes, double alpha_m_m,
                                            double m, const double* __restrict__ ln_table) {
     const double hm = (double)hsum * 0x1p-31;
     double e = __ddiv_rn(alpha_m_m, hm);
     if (zeroes != 0u && e < 2.5 * m) e = __ldg(ln_table + zeroes);
     return e;
+}
+
+// |x| < 2^53 converted to double by bit assembly (exact; no f64 instruction).
+__device__ __forceinline__ double exact_u64_to_double(uint64_t u) {
+    if (u == 0) return 0.0;
+    const int lz = __clzll((long long)u);
+    const uint64_t e = (uint64_t)(63 - lz + 1023);
+    const uint64_t mant = (u << lz) >> 11;  // 53 bits, leading one at bit 52
+    return __longlong_as_double((long long)((e << 52) | (mant & ((1ull << 52) - 1))));
+}
+
+// The same estimate with one f64 instruction (the division) on the hot path:
+//   alpha*m^2 / (H * 2^-31) == (alpha*m^2*2^31) / H exactly (power-of-two
+//   scaling), so a_scaled = alpha*m^2*2^31 is precomputed; H > 0 converts
+//   exactly; `e < 2.5m` between positive finite doubles is an integer compare
+//   of their bit patterns. H <= 0 (only reachable through the i32 quirk)
+//   takes the reference arithmetic.
+__device__ __forceinline__ double estimate_fast(int64_t hsum, uint32_t zeroes, double alpha_m_m,
+                                                double a_scaled, long long small_bits, double m,
+                                                const double* __restrict__ ln_table) {
+    if (hsum <= 0) return estimate(hsum, zeroes, alpha_m_m, m, ln_table);
+    const double e = __ddiv_rn(a_scaled, exact_u64_to_double((uint64_t)hsum));
+    if (zeroes != 0u && __double_as_longlong(e) < small_bits) return __ldg(ln_table + zeroes);
+    return e;
+}
+
+// delta / d correctly rounded, for a positive integer-valued d with
+// rd = RN(1/d): q0 = RN(delta*rd), r = delta - d*q0 (exact by fma),
+// q1 = RN(q0 + r*rd). Markstein's correction step (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990); checked against true division in the tests.
+__device__ __forceinline__ double div_by_small_int(double delta, double d, double rd) {
+    const double q0 = __dmul_rn(delta, rd);
+    const double r = __fma_rn(-q0, d, delta);
+    return __fma_rn(r, rd, q0);
 }
 
 __device__ __forceinline__ int64_t signed_hsum(uint64_t hsum, uint32_t c31, int quirk) {
