@@ -1,0 +1,423 @@
+#!/usr/bin/env python3
+"""HyperBall benchmark on one GB300: arc-register updates per second.
+
+Workload: the synthetic web-like graph with 2^26 nodes (out-degrees Zipf with
+exponent 2.1 and mean 12, capped at 10^5; 80% of the successors uniform
+within +/-1024 of the source id, 20% uniform over all nodes; seed 2), HyperLogLog
+counters with 2^6 registers (SipHash-1-3 node hash, seed 0), systolic
+iterations with the transpose built on the device, sum of distances and
+harmonic centrality, run until no counter changes.
+
+A step is one complete HyperBall run (hb_run_until_done: init plus every
+iteration). The work unit is the arc-register update: visited_arcs_t * 2^log2m
+summed over the iterations (the visited arcs are deterministic). `value` is
+measured with the graph resident in HBM; `e2e` goes through the public API
+from pinned host buffers (hb_create copies the CSR in and builds the transpose
+on the device, then the run, then the neighbourhood function, sums of
+distances and harmonic centralities are read back).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the CPU restatement of the reference algorithm (the
+oracle's threaded engine, one thread per host core) on the same workload; each
+step is one standard iteration of the same run.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "webgraph-algo-rs_gb300"))
+
+METRIC = "HyperBall arc-register updates/s"
+UNIT = "arc-register updates/s"
+LOG2M = 6
+COUNTER_BYTES = (1 << LOG2M) * 5 // 8
+PROFILE = os.path.join(ROOT, "profiles", "union_weblike.md")
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--log2n", type=int, default=26, help="graph size (2^log2n nodes)")
+    p.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: --steps)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(log2n):
+    return {
+        "workload": f"weblike-2^{log2n} HyperBall to stabilisation",
+        "nodes": 1 << log2n,
+        "graph": "web-like: Zipf(2.1) out-degree, mean 12, cap 1e5; 80% of successors within "
+                 "+/-1024 of the source, 20% uniform; seed 2",
+        "log2m": LOG2M,
+        "hash": "SipHash-1-3, seed 0",
+        "mode": "systolic, transpose built on device",
+        "outputs": "neighbourhood function, sum of distances, harmonic centrality",
+        "l2": "inputs larger than L2 (two 2^n x 40 B counter arrays, CSR 4 B/arc)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# replicas: one process per GPU, independent instances, no data-path collective
+# ---------------------------------------------------------------------------
+class Ranks:
+    """Barrier and max-over-ranks for `world` replicas (torchrun env); a
+    no-op for one process."""
+
+    def __init__(self, world, backend, device=None):
+        import torch
+        self.world, self.dist, self.device = world, None, device
+        if world > 1:
+            import torch.distributed as dist
+            kw = {"device_id": device} if backend == "nccl" else {}
+            dist.init_process_group(backend, **kw)
+            self.dist = dist
+        self.torch = torch
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.dist is None:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64,
+                              device=self.device if self.device is not None else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+
+
+def job_value(world, steps, units_per_step, seconds):
+    """Whole-job throughput: every replica did `steps` steps of `units_per_step`
+    units; `seconds` is the max over replicas."""
+    return world * steps * units_per_step / seconds
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.samples = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-i", str(gpu_id), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.samples.append(f)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        return self.summarise(self.samples)
+
+    @classmethod
+    def summarise(cls, samples):
+        """Median SM clock, max clock and the throttle reasons seen in
+        `nvidia-smi --format=csv,noheader,nounits` rows of FIELDS."""
+        sm, mx, reasons = [], None, set()
+        for f in samples:
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(cls.NAMES, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# roofline model of the union kernels (k_union_window + k_union_heavy)
+# ---------------------------------------------------------------------------
+def union_model_bytes(stats, n):
+    """Compulsory HBM bytes of the union kernels of each iteration:
+    8 B offsets per scanned node, 4 B per successor id read, one counter read
+    per distinct modified successor (bounded by min(previously modified,
+    visited arcs)), prev read + next write of every scanned node, and the
+    modified / must-be-checked bitmaps."""
+    out = []
+    prev_mod = n  # init marks every counter modified
+    for s in stats:
+        S, A, V = s["scanned_nodes"], s["scanned_arcs"], s["visited_arcs"]
+        U = min(prev_mod, V)
+        out.append(8 * S + 4 * A + COUNTER_BYTES * U + 2 * COUNTER_BYTES * S + n // 4)
+        prev_mod = s["modified_counters"]
+    return out
+
+
+def profiled_traffic_ratio():
+    """DRAM bytes per model byte of the union kernel, from the committed ncu
+    summary (None when there is none)."""
+    try:
+        text = open(PROFILE).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_model_byte:\s*([0-9.]+)", text)
+    return float(m.group(1)) if m else None
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (oracle) sample: standard iterations of the same workload
+# ---------------------------------------------------------------------------
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+class CpuSample:
+    """The oracle's threaded engine (one thread per host core) on the same graph;
+    each sample is one iteration of the run (the first ones are standard
+    iterations over every arc)."""
+
+    def __init__(self, graph):
+        import numpy as np
+        from oracle import hbo
+        self.cores = host_cores()
+        self.off = np.array(graph.offsets)
+        self.suc = np.array(graph.successors)
+        self.o = hbo.OracleHyperBall(self.off, self.suc, LOG2M, 0, 0, sod=True, harm=True,
+                                     threads=self.cores)
+        t = time.perf_counter()
+        self.o.init()
+        self.init_s = time.perf_counter() - t
+
+    def step(self):
+        t = time.perf_counter()
+        s = self.o.iterate()
+        dt = time.perf_counter() - t
+        return s["visited_arcs"] << LOG2M, dt, s["iteration"]
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import hyperball_gb300 as hb
+    g = hb.Graph.weblike(1 << args.log2n)
+    cpu = CpuSample(g)
+    for _ in range(args.warmup):
+        cpu.step()
+    units, secs, its = 0, 0.0, []
+    for _ in range(args.steps):
+        u, dt, it = cpu.step()
+        units += u
+        secs += dt
+        its.append(it)
+    value = units / secs
+    sample = (f"iterations {its[0]}-{its[-1]} of the run (after {args.warmup} warm-up "
+              f"iterations), {units >> LOG2M} visited arcs, {secs:.1f} s")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": workload(args.log2n),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": "port",
+                         "sample": "C++ restatement of the reference algorithm (oracle), "
+                                   "threaded engine; " + sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import hyperball_gb300 as hb
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device (there is no CPU path)")
+    torch.cuda.set_device(local)
+    ranks = Ranks(world, "nccl", torch.device("cuda", local))
+    barrier, max_over_ranks = ranks.barrier, ranks.max
+
+    n = 1 << args.log2n
+    g = hb.Graph.weblike(n)
+    m = g.num_arcs
+    stream = torch.cuda.Stream()
+    logic = hb.HyperLogLogBuilder(n).log_2_num_reg(LOG2M).build()
+    h = (hb.HyperBallBuilder.new(g, logic).transpose_on_device(True)
+         .sum_of_distances(True).sum_of_inverse_distances(True)
+         .stream(stream.cuda_stream).device(local).build())
+
+    for _ in range(args.warmup):
+        h.run_until_done()
+    ref_stats = [dict(s) for s in h.iteration_stats()]
+    units_per_step = sum(s["visited_arcs"] for s in ref_stats) << LOG2M
+
+    # --- device-resident timed region -------------------------------------
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(gpu_id)
+    launches0 = h.kernel_launches()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    # the timed region is the profiled range (ncu --profile-from-start off)
+    torch.cuda.profiler.start()
+    ev0.record(stream)
+    union_ms, model_bytes, iters = 0.0, 0, 0
+    for _ in range(args.steps):
+        h.run_until_done()
+        st = h.iteration_stats()
+        if [s["visited_arcs"] for s in st] != [s["visited_arcs"] for s in ref_stats]:
+            raise RuntimeError("visited arcs differ between runs")
+        union_ms += sum(s["union_ms"] for s in st)
+        model_bytes += sum(union_model_bytes(st, n))
+        iters += len(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    barrier()
+    clk = clocks.stop()
+    launches = h.kernel_launches() - launches0
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    value = job_value(world, args.steps, units_per_step, elapsed_ms / 1e3)
+
+    achieved = model_bytes / (union_ms / 1e3) / 1e9
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        peak_src = "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    ratio = profiled_traffic_ratio()
+    per_launch_model = model_bytes / iters
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_src,
+        "traffic": ratio * per_launch_model if ratio else None,
+        "kernel": "union (k_union_window + k_union_heavy), one launch each per iteration",
+        "model_bytes_per_launch": per_launch_model,
+        "union_ms_per_step": union_ms / args.steps,
+    }
+
+    # --- end to end through the public API from pinned host buffers ---------
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    off_pin = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    suc_pin = torch.empty(m, dtype=torch.int32).pin_memory()
+    off_pin.numpy()[:] = np.asarray(g.offsets).view(np.int64)
+    suc_pin.numpy()[:] = np.asarray(g.successors).view(np.int32)
+    view = hb.CsrView(n, m, off_pin.data_ptr(), suc_pin.data_ptr(), owner=(off_pin, suc_pin))
+    h.close()
+    del h
+    nf_len = len(ref_stats) + 1
+
+    def e2e_step():
+        hh = (hb.HyperBallBuilder.new(view, logic).transpose_on_device(True)
+              .sum_of_distances(True).sum_of_inverse_distances(True)
+              .stream(stream.cuda_stream).device(local).build())
+        hh.run_until_done()
+        nf = hh.neighborhood_function()
+        hh.sum_of_distances()
+        hh.harmonic_centralities()
+        k = hh.kernel_launches()
+        hh.close()
+        return len(nf), k
+
+    e2e_step()  # warm-up
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_launches = 0
+    for _ in range(e2e_steps):
+        got, k = e2e_step()
+        e2e_launches += k
+        if got != nf_len:
+            raise RuntimeError("end-to-end run took a different number of iterations")
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {
+        "value": job_value(world, e2e_steps, units_per_step, e2e_s), "unit": UNIT,
+        "h2d_bytes_per_step": 8 * (n + 1) + 4 * m,
+        "d2h_bytes_per_step": 16 * n + 8 * nf_len,
+        "ms_per_step": 1e3 * e2e_s / e2e_steps,
+        "gpu_launches_per_step": e2e_launches // max(e2e_steps, 1),
+    }
+
+    cpu_baseline = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = CpuSample(g)
+        u, dt, it = cpu.step()
+        cpu_baseline = {
+            "value": u / dt, "unit": UNIT, "cores": cpu.cores, "kind": "port",
+            "sample": f"C++ restatement of the reference algorithm (oracle), threaded engine: "
+                      f"iteration {it} of the same run (standard, {u >> LOG2M} visited arcs) "
+                      f"in {dt:.1f} s",
+        }
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": dict(workload(args.log2n), arcs=m, iterations=len(ref_stats),
+                           parallelism=f"replicas x{world}"),
+            "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
+            "clocks": clk, "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    ranks.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -99,6 +99,8 @@ typedef struct hb_iter_stats {
     int32_t systolic, local, pre_local, reserved;
     double union_ms;             /* device time of the union kernels of this iteration */
     double iteration_ms;         /* device time of the whole iteration */
+    uint64_t scanned_arcs;       /* arcs of the scanned nodes (successor ids read) */
+    uint64_t kernel_launches;    /* CUDA kernels this library launched for the iteration */
 } hb_iter_stats;
 
 /* Discount function: weight of distance d >= 1 (reference: the closures of
@@ -210,6 +212,9 @@ void hb_graph_free(hb_graph* g);
 /* ---- introspection ---------------------------------------------------------- */
 /* Library build string, e.g. "hyperball_gb300 sm_103a". */
 const char* hb_version(void);
+/* CUDA kernels this library launched for the handle so far (creation, init and
+ * every iteration). No reference counterpart: a diagnostic for benchmarks. */
+uint64_t hb_kernel_launches(const hb_handle* h);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "hb_internal.h"
@@ -62,7 +63,8 @@ struct hb_handle {
     cudaStream_t stream = nullptr;
     uint64_t n = 0, m = 0;
     int log2m = 4;
-    uint64_t counter_bytes = 0;
+    uint64_t counter_bytes = 0;   // the reference's packed counter size, 2^log2m * 5 / 8
+    uint64_t stride = 0;          // device bytes per counter: one byte per register
     int hash_kind = HB_HASH_SIP13;
     uint64_t hash_seed = 0;
     uint64_t num_elements = 0;
@@ -92,16 +94,26 @@ struct hb_handle {
     uint64_t* d_weights = nullptr;
     uint32_t* d_tiles = nullptr;  // window boundaries
     uint64_t n_tiles = 0;         // number of windows
-    uint32_t* d_perm = nullptr;     // per window: medium then light nodes, by degree
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
+    uint32_t* d_perm = nullptr;     // device node -> caller node
+    uint32_t* d_inv = nullptr;      // caller node -> device node
+    std::vector<uint32_t> inv_host;
     uint64_t n_chunks = 0;
-    uint8_t* d_win_flags = nullptr; // systolic: windows with work
+    uint32_t* d_win_medium = nullptr;           // first medium node of every window
+    uint32_t* d_win_light = nullptr;            // first light node of every window
+    unsigned long long* d_word_cnt = nullptr;   // systolic lists: per bitmap word counts
+    uint64_t* d_word_off = nullptr;             // their exclusive prefix sum (+ totals)
+    unsigned long long* d_list_scratch = nullptr;
+    uint64_t list_scratch_len = 0;
+    uint32_t* d_light_list = nullptr;           // systolic: light nodes to check or copy
+    uint32_t* d_medium_list = nullptr;          // systolic: medium nodes to check or copy
     uint32_t* d_heavy = nullptr;
     uint64_t n_heavy = 0;
     hbk::TilePartial* d_partials = nullptr;  // one per tile, then one per heavy block
     uint64_t n_partials = 0;
     hbk::TilePartial* d_partial_scratch = nullptr;
     hbk::TilePartial* d_partial_out = nullptr;
+    unsigned long long* d_cursor = nullptr;  // chunk cursor of the union kernel
     int* d_any31 = nullptr;
     bool any31 = false;
     int grid_tile = 1, grid_heavy = 1, grid_mark = 1, grid_fin = 1;
@@ -112,6 +124,7 @@ struct hb_handle {
     int mod_cur = 0;     // d_bits[mod_cur] = curr_mod, d_bits[mod_cur ^ 1] = next_mod
     int mbc_cur = 2;     // d_bits[mbc_cur] = mbc, d_bits[mbc_cur ^ 1] = next_mbc
     uint64_t iteration = 0;
+    uint64_t launches = 0;          // kernels launched for this handle
     bool systolic = false, local = false, pre_local = false;
     uint64_t modified_counters = 0;
     double last = 0.0, relative_increment = 0.0;
@@ -173,6 +186,108 @@ void release(hb_handle* h) {
         if (e) cudaEventDestroy(e);
 }
 
+// Static work order of the union kernels (the graph does not change), and the
+// node renumbering that follows it. Nodes are cut into windows of `win_nodes`
+// consecutive ids; inside a window the heavy nodes (out-degree > medium_max),
+// the medium nodes (small_max < out-degree <= medium_max) and the light nodes
+// (out-degree <= small_max) take the window's ids in that order, each kind by
+// decreasing out-degree, ties by id: perm[new] = caller id, inv[caller] = new.
+// The light and medium runs are cut into chunks of one warp-step (`per_light`
+// or `per_medium` nodes); heavy nodes are listed by decreasing degree. Windows
+// are processed by all host threads.
+struct WorkPartition {
+    std::vector<uint32_t> tiles, perm, inv, heavy, win_medium, win_light;
+    std::vector<uint2> chunks;
+};
+
+void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium_max,
+                     uint32_t win_nodes, uint32_t per_light, uint32_t per_medium,
+                     WorkPartition& out) {
+    const uint64_t n = g->num_nodes;
+    const uint64_t* off = g->offsets;
+    const uint64_t nwin = (n + win_nodes - 1) / win_nodes;
+    struct WinCount {
+        uint64_t light, medium, heavy;
+    };
+    std::vector<WinCount> cnt(nwin);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t nthreads = std::min<uint64_t>(std::min<uint64_t>(hw, 64), std::max<uint64_t>(nwin, 1));
+    auto parallel = [&](auto&& body) {
+        std::vector<std::thread> th;
+        for (uint64_t t = 0; t < nthreads; t++)
+            th.emplace_back([&, t] {
+                for (uint64_t w = nwin * t / nthreads; w < nwin * (t + 1) / nthreads; w++) body(w);
+            });
+        for (auto& x : th) x.join();
+    };
+    parallel([&](uint64_t w) {
+        WinCount c{0, 0, 0};
+        const uint64_t w0 = w * win_nodes, w1 = std::min<uint64_t>(n, w0 + win_nodes);
+        for (uint64_t v = w0; v < w1; v++) {
+            const uint64_t d = off[v + 1] - off[v];
+            if (d > medium_max)
+                c.heavy++;
+            else if (d > small_max)
+                c.medium++;
+            else
+                c.light++;
+        }
+        cnt[w] = c;
+    });
+    // window offsets into chunks and heavy
+    std::vector<uint64_t> chunk_at(nwin + 1, 0), heavy_at(nwin + 1, 0);
+    for (uint64_t w = 0; w < nwin; w++) {
+        const WinCount& c = cnt[w];
+        chunk_at[w + 1] = chunk_at[w] + (c.medium + per_medium - 1) / per_medium +
+                          (c.light + per_light - 1) / per_light;
+        heavy_at[w + 1] = heavy_at[w] + c.heavy;
+    }
+    out.tiles.resize(n ? nwin + 1 : 0);
+    for (uint64_t w = 0; n && w <= nwin; w++) out.tiles[w] = (uint32_t)std::min<uint64_t>(n, w * win_nodes);
+    out.win_medium.resize(nwin);
+    out.win_light.resize(nwin);
+    for (uint64_t w = 0; w < nwin; w++) {
+        out.win_medium[w] = (uint32_t)(w * win_nodes + cnt[w].heavy);
+        out.win_light[w] = (uint32_t)(w * win_nodes + cnt[w].heavy + cnt[w].medium);
+    }
+    out.perm.resize(n);
+    out.inv.resize(n);
+    out.chunks.resize(chunk_at[nwin]);
+    out.heavy.resize(heavy_at[nwin]);
+    parallel([&](uint64_t w) {
+        const uint64_t w0 = w * win_nodes, w1 = std::min<uint64_t>(n, w0 + win_nodes);
+        // sort key: (inverted clamped degree, node): decreasing degree, ties by id
+        std::vector<uint64_t> kind[3];
+        for (uint64_t v = w0; v < w1; v++) {
+            const uint64_t d = off[v + 1] - off[v];
+            const uint64_t key = ((uint64_t)(0xffffffffu - (uint32_t)std::min<uint64_t>(d, 0xffffffffu)) << 32) | v;
+            kind[d > medium_max ? 0 : d > small_max ? 1 : 2].push_back(key);
+        }
+        uint64_t next = w0, cp = chunk_at[w], hp = heavy_at[w];
+        for (int k = 0; k < 3; k++) {
+            std::sort(kind[k].begin(), kind[k].end());
+            const uint64_t first = next;
+            for (uint64_t key : kind[k]) {
+                out.perm[next] = (uint32_t)key;
+                out.inv[(uint32_t)key] = (uint32_t)next;
+                if (k == 0) out.heavy[hp++] = (uint32_t)next;
+                next++;
+            }
+            if (k == 0) continue;
+            const uint32_t per = k == 1 ? per_medium : per_light;
+            const uint32_t flag = k == 1 ? 0x80000000u : 0u;
+            for (uint64_t i = 0; i < kind[k].size(); i += per) {
+                const uint32_t c = (uint32_t)std::min<uint64_t>(per, kind[k].size() - i);
+                out.chunks[cp++] = make_uint2((uint32_t)(first + i), c | flag);
+            }
+        }
+    });
+    std::stable_sort(out.heavy.begin(), out.heavy.end(), [&](uint32_t x, uint32_t y) {
+        const uint32_t ux = out.perm[x], uy = out.perm[y];
+        return off[ux + 1] - off[ux] > off[uy + 1] - off[uy];
+    });
+}
+
 bool check_view(const hb_graph_view* g, std::string& why) {
     if (!g) {
         why = "graph is NULL";
@@ -215,6 +330,38 @@ int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t*
     HB_CUDA(h, cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     if (bad) return set_err(h, HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
+    return HB_OK;
+}
+
+// Frees one buffer of the handle before its end of life.
+void dfree(hb_handle* h, void* p) {
+    for (auto it = h->bufs.begin(); it != h->bufs.end(); ++it)
+        if (it->p == p) {
+            cudaFree(p);
+            h->bufs.erase(it);
+            return;
+        }
+}
+
+// CSR (caller ids) -> CSR of the renumbered graph: node i is caller node
+// perm[i], successor u becomes inv[u].
+int relabel_csr(hb_handle* h, const uint64_t* off0, const uint32_t* succ0, uint64_t** d_off,
+                uint32_t** d_succ) {
+    const uint64_t n = h->n, m = h->m;
+    int r;
+    unsigned long long* deg = nullptr;
+    unsigned long long* scratch = nullptr;
+    const uint64_t sl = hbk::scan_scratch_len(n + 1);
+    if ((r = dalloc(h, d_off, n + 1))) return r;
+    if ((r = dalloc(h, d_succ, m))) return r;
+    if ((r = dalloc(h, &deg, n + 1))) return r;
+    if ((r = dalloc(h, &scratch, sl))) return r;
+    HB_LAUNCH(h, hbk::launch_perm_degree(off0, h->d_perm, n, deg, h->stream));
+    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(deg, *d_off, n + 1, scratch, sl, h->stream));
+    if (n) HB_LAUNCH(h, hbk::launch_relabel_succ(off0, succ0, h->d_perm, h->d_inv, *d_off, *d_succ, n, h->stream));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    dfree(h, deg);
+    dfree(h, scratch);
     return HB_OK;
 }
 
@@ -283,24 +430,36 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.ln_table = h->d_lnt;
     a.tiles = h->d_tiles;
     a.n_tiles = (uint32_t)h->n_tiles;
-    a.win_flags = h->d_win_flags;
-    a.perm = h->d_perm;
+    a.light_list = nullptr;
+    a.medium_list = nullptr;
+    a.list_counts = nullptr;
     a.chunks = h->d_chunks;
+    a.gather_all = 0;
     a.n_chunks = h->n_chunks;
     a.tile_max_degree = h->medium_max;
     a.acc_slot = (uint32_t)(h->n_partials - 1);
+    a.cursor = h->d_cursor;
     a.partials = h->d_partials;
     return a;
 }
 
+// Adds the kernels launched by this thread during its lifetime to h->launches.
+struct LaunchTally {
+    hb_handle* h;
+    uint64_t c0;
+    explicit LaunchTally(hb_handle* hh) : h(hh), c0(hbk::launch_count()) {}
+    ~LaunchTally() { h->launches += hbk::launch_count() - c0; }
+};
+
 int do_init(hb_handle* h) {
     const uint64_t n = h->n;
-    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[0], 0, n * h->counter_bytes, h->stream));
-    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[1], 0, n * h->counter_bytes, h->stream));
+    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[0], 0, n * h->stride, h->stream));
+    HB_CUDA(h, cudaMemsetAsync(h->d_cnt[1], 0, n * h->stride, h->stream));
     h->cur = 0;
     h->mod_cur = 0;
     h->mbc_cur = 2;
     hbk::InitArgs ia{};
+    ia.perm = h->d_perm;
     ia.curr = h->d_cnt[0];
     ia.est = h->d_est;
     ia.n = n;
@@ -352,6 +511,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     h->pre_local = h->systolic && m > 0 && prev_mod < (n * n) / (m * 10);
 
     const uint64_t words = (n + 31) / 32;
+    const uint64_t launches0 = hbk::launch_count();
     cudaStream_t s = h->stream;
     HB_CUDA(h, cudaEventRecord(h->ev[0], s));
     HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mod_cur ^ 1], 0, words * 4, s));
@@ -367,11 +527,20 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         }
     }
     HB_CUDA(h, cudaMemsetAsync(h->d_partials, 0, h->n_partials * sizeof(hbk::TilePartial), s));
+    HB_CUDA(h, cudaMemsetAsync(h->d_cursor, 0, sizeof(unsigned long long), s));
     hbk::UnionArgs a = union_args(h);
+    // nearly every counter changed in the previous iteration: merge all
+    // successors without waiting for their modified bits
+    a.gather_all = !h->systolic && prev_mod >= n - n / 8;
     if (h->systolic && h->n_tiles) {
-        // windows holding a node to check or to copy
-        HB_LAUNCH(h, hbk::launch_window_flags(h->d_tiles, (uint32_t)h->n_tiles, a.mbc, a.curr_mod,
-                                              h->d_win_flags, s));
+        // the chunks of the windows holding a node to check or to copy
+        HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_win_medium, h->d_win_light, n,
+                                            h->d_word_cnt, h->d_word_off, h->d_list_scratch,
+                                            h->list_scratch_len, h->d_light_list,
+                                            h->d_medium_list, s));
+        a.light_list = h->d_light_list;
+        a.medium_list = h->d_medium_list;
+        a.list_counts = h->d_word_off + words;
     }
     HB_CUDA(h, cudaEventRecord(h->ev[1], s));
     if (h->n_tiles) HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, h->grid_tile, s));
@@ -394,7 +563,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     struct {
         unsigned long long st[4];
         double nf;
-    } host{{tot.vis, tot.mod, tot.scanned, 0}, tot.nf};
+    } host{{tot.vis, tot.mod, tot.scanned, tot.sarcs}, tot.nf};
 
     // swap states (HB:909-914)
     h->cur ^= 1;
@@ -425,6 +594,8 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     cudaEventElapsedTime(&ms_all, h->ev[0], h->ev[3]);
     st.union_ms = ms_union;
     st.iteration_ms = ms_all;
+    st.scanned_arcs = host.st[3];
+    st.kernel_launches = hbk::launch_count() - launches0;
     h->stats.push_back(st);
     if (out) *out = st;
     return HB_OK;
@@ -442,6 +613,25 @@ int copy_d2h(const hb_handle* h, const void* src, void* dst, size_t bytes) {
     HB_CUDA(hh, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
     HB_CUDA(hh, cudaStreamSynchronize(h->stream));
     return HB_OK;
+}
+
+// A per-node device array (device node order) into caller order on the host.
+int copy_nodes_d2h(const hb_handle* h, const double* src, double* dst) {
+    hb_handle* hh = const_cast<hb_handle*>(h);
+    if (h->n == 0) return HB_OK;
+    HB_CUDA(hh, cudaSetDevice(h->device));
+    double* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, h->n * 8, h->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_err(hh, e, "cudaMallocAsync");
+    }
+    int r = hbk::launch_gather_f64(src, h->d_inv, tmp, h->n, h->stream);
+    if (r == 0) r = copy_d2h(h, tmp, dst, h->n * 8);
+    else r = cuda_err(hh, (cudaError_t)r, "launch_gather_f64");
+    cudaFreeAsync(tmp, h->stream);
+    cudaStreamSynchronize(h->stream);
+    return r;
 }
 
 int check_len(const hb_handle* h, size_t len) {
@@ -465,6 +655,8 @@ void hb_options_default(hb_options* o) {
 }
 
 const char* hb_version(void) { return "hyperball_gb300 0.1 sm_103a"; }
+
+uint64_t hb_kernel_launches(const hb_handle* h) { return h ? h->launches : 0; }
 const char* hb_global_last_error(void) { return g_global_err.c_str(); }
 const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_global_err.c_str(); }
 
@@ -510,6 +702,7 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
     h->m = graph->num_arcs;
     h->log2m = o.log2m;
     h->counter_bytes = ((uint64_t)1 << o.log2m) * 5 / 8;
+    h->stride = (uint64_t)1 << o.log2m;
     h->hash_kind = o.hash_kind;
     h->hash_seed = o.hash_seed;
     h->do_sod = o.flags & HB_SUM_OF_DISTANCES;
@@ -543,6 +736,7 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
     }
 
     hb_handle* hp = h.get();
+    LaunchTally tally(hp);
     int r;
     int ndev = 0;
     cudaError_t ce = cudaGetDeviceCount(&ndev);
@@ -562,16 +756,66 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         release(hp);
         return code;
     };
-    if ((r = upload_csr(hp, graph, &h->d_off, &h->d_succ))) return fail(r);
+    // Work partition and renumbering (host), then the CSR (and the transpose
+    // when given) uploaded, validated and renumbered on the device.
+    h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
+    h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
+    if (h->medium_max < h->small_max) h->medium_max = h->small_max;
+    {
+        uint32_t win_nodes = 0, win_arcs = 0, per_light = 0, per_medium = 0;
+        hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
+        hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
+        WorkPartition wp;
+        build_partition(graph, h->small_max, h->medium_max, win_nodes, per_light, per_medium, wp);
+        h->n_tiles = h->n ? wp.tiles.size() - 1 : 0;
+        h->n_chunks = wp.chunks.size();
+        h->n_heavy = wp.heavy.size();
+        auto upload = [&](auto** dst, const auto& src) {
+            int rr = dalloc(hp, dst, src.size());
+            if (rr) return rr;
+            if (src.empty()) return (int)HB_OK;
+            return cuda_err(hp,
+                            cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice),
+                            "cudaMemcpy");
+        };
+        if ((r = upload(&h->d_tiles, wp.tiles))) return fail(r);
+        if ((r = upload(&h->d_chunks, wp.chunks))) return fail(r);
+        if ((r = upload(&h->d_perm, wp.perm))) return fail(r);
+        if ((r = upload(&h->d_inv, wp.inv))) return fail(r);
+        if (h->n_heavy && (r = upload(&h->d_heavy, wp.heavy))) return fail(r);
+        if ((r = upload(&h->d_win_medium, wp.win_medium))) return fail(r);
+        if ((r = upload(&h->d_win_light, wp.win_light))) return fail(r);
+        const uint64_t words = (h->n + 31) / 32;
+        if ((r = dalloc(hp, &h->d_word_cnt, words + 1))) return fail(r);
+        if ((r = dalloc(hp, &h->d_word_off, words + 1))) return fail(r);
+        h->list_scratch_len = hbk::scan_scratch_len(words + 1);
+        if ((r = dalloc(hp, &h->d_list_scratch, h->list_scratch_len))) return fail(r);
+        if ((r = dalloc(hp, &h->d_light_list, h->n + 1))) return fail(r);
+        if ((r = dalloc(hp, &h->d_medium_list, h->n + 1))) return fail(r);
+        h->inv_host = std::move(wp.inv);
+    }
+    {
+        uint64_t* off0 = nullptr;
+        uint32_t* succ0 = nullptr;
+        if ((r = upload_csr(hp, graph, &off0, &succ0))) return fail(r);
+        if ((r = relabel_csr(hp, off0, succ0, &h->d_off, &h->d_succ))) return fail(r);
+        dfree(hp, off0);
+        dfree(hp, succ0);
+    }
     if (transpose) {
-        if ((r = upload_csr(hp, transpose, &h->d_toff, &h->d_tsucc))) return fail(r);
+        uint64_t* off0 = nullptr;
+        uint32_t* succ0 = nullptr;
+        if ((r = upload_csr(hp, transpose, &off0, &succ0))) return fail(r);
+        if ((r = relabel_csr(hp, off0, succ0, &h->d_toff, &h->d_tsucc))) return fail(r);
+        dfree(hp, off0);
+        dfree(hp, succ0);
         h->has_transpose = true;
     } else if (o.flags & HB_TRANSPOSE_ON_DEVICE) {
         if ((r = build_transpose_on_device(hp))) return fail(r);
     }
     const uint64_t n = h->n;
-    if ((r = dalloc(hp, &h->d_cnt[0], n * h->counter_bytes))) return fail(r);
-    if ((r = dalloc(hp, &h->d_cnt[1], n * h->counter_bytes))) return fail(r);
+    if ((r = dalloc(hp, &h->d_cnt[0], n * h->stride))) return fail(r);
+    if ((r = dalloc(hp, &h->d_cnt[1], n * h->stride))) return fail(r);
     const uint64_t words = (n + 31) / 32;
     for (int b = 0; b < 4; b++)
         if ((r = dalloc(hp, &h->d_bits[b], words))) return fail(r);
@@ -594,69 +838,6 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
                           "cudaMemcpy")))
             return fail(r);
     }
-    // Work partition (static: the graph does not change). Nodes are cut into
-    // windows of consecutive ids; inside a window, light (out-degree <=
-    // small_max) and medium (up to medium_max) nodes are listed by decreasing
-    // out-degree so that neighbouring lanes walk equally long lists. Nodes
-    // above medium_max run one CTA each, heaviest first.
-    h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
-    h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
-    if (h->medium_max < h->small_max) h->medium_max = h->small_max;
-    {
-        uint32_t win_nodes = 0, win_arcs = 0, per_light = 0, per_medium = 0;
-        hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
-        hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
-        std::vector<uint32_t> hvy, tiles, perm, light, medium;
-        std::vector<uint2> chunks;
-        auto deg = [&](uint32_t x) { return graph->offsets[x + 1] - graph->offsets[x]; };
-        auto by_degree = [&](uint32_t x, uint32_t y) { return deg(x) > deg(y); };
-        perm.reserve(n);
-        for (uint64_t w0 = 0; w0 < n; w0 += win_nodes) {
-            const uint64_t w1 = std::min<uint64_t>(n, w0 + win_nodes);
-            tiles.push_back((uint32_t)w0);
-            light.clear();
-            medium.clear();
-            for (uint64_t v = w0; v < w1; v++) {
-                const uint64_t d = deg((uint32_t)v);
-                if (d > h->medium_max)
-                    hvy.push_back((uint32_t)v);
-                else if (d > h->small_max)
-                    medium.push_back((uint32_t)v);
-                else
-                    light.push_back((uint32_t)v);
-            }
-            std::stable_sort(light.begin(), light.end(), by_degree);
-            std::stable_sort(medium.begin(), medium.end(), by_degree);
-            for (size_t i = 0; i < medium.size(); i += per_medium) {
-                const uint32_t c = (uint32_t)std::min<size_t>(per_medium, medium.size() - i);
-                chunks.push_back(make_uint2((uint32_t)(perm.size() + i), c | 0x80000000u));
-            }
-            perm.insert(perm.end(), medium.begin(), medium.end());
-            for (size_t i = 0; i < light.size(); i += per_light) {
-                const uint32_t c = (uint32_t)std::min<size_t>(per_light, light.size() - i);
-                chunks.push_back(make_uint2((uint32_t)(perm.size() + i), c));
-            }
-            perm.insert(perm.end(), light.begin(), light.end());
-        }
-        if (n) tiles.push_back((uint32_t)n);
-        h->n_tiles = n ? tiles.size() - 1 : 0;
-        h->n_chunks = chunks.size();
-        std::stable_sort(hvy.begin(), hvy.end(), by_degree);
-        h->n_heavy = hvy.size();
-        auto upload = [&](auto** dst, const auto& src) {
-            int rr = dalloc(hp, dst, src.size());
-            if (rr) return rr;
-            if (src.empty()) return (int)HB_OK;
-            return cuda_err(hp,
-                            cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice),
-                            "cudaMemcpy");
-        };
-        if ((r = upload(&h->d_tiles, tiles))) return fail(r);
-        if ((r = upload(&h->d_perm, perm))) return fail(r);
-        if ((r = upload(&h->d_chunks, chunks))) return fail(r);
-        if (h->n_heavy && (r = upload(&h->d_heavy, hvy))) return fail(r);
-        if ((r = dalloc(hp, &h->d_win_flags, h->n_tiles + 1))) return fail(r);
-    }
     h->grid_tile = hbk::tile_grid(h->log2m, h->device);
     {
         // one warp per chunk, 8 warps per block
@@ -678,6 +859,7 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
     if ((r = dalloc(hp, &h->d_partial_scratch, 256))) return fail(r);
     if ((r = dalloc(hp, &h->d_partial_out, 1))) return fail(r);
     if ((r = dalloc(hp, &h->d_any31, 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_cursor, 1))) return fail(r);
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     *out = h.release();
     return HB_OK;
@@ -706,12 +888,14 @@ void hb_destroy(hb_handle* h) {
 
 int hb_init(hb_handle* h) {
     if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    LaunchTally tally(h);
     HB_CUDA(h, cudaSetDevice(h->device));
     return do_init(h);
 }
 
 int hb_iterate(hb_handle* h, hb_iter_stats* out) {
     if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    LaunchTally tally(h);
     if (!h->initialised) return set_err(h, HB_ERR_NOT_RUN, "hb_init must precede hb_iterate");
     HB_CUDA(h, cudaSetDevice(h->device));
     return do_iterate(h, out);
@@ -719,6 +903,7 @@ int hb_iterate(hb_handle* h, hb_iter_stats* out) {
 
 int hb_run(hb_handle* h, uint64_t upper_bound, double threshold) {
     if (!h) return set_err(nullptr, HB_ERR_INVALID, "handle is NULL");
+    LaunchTally tally(h);
     HB_CUDA(h, cudaSetDevice(h->device));
     upper_bound = std::min<uint64_t>(upper_bound, h->n);  // HB:541
     int r = do_init(h);
@@ -758,7 +943,7 @@ int hb_get_sum_of_distances(const hb_handle* h, double* dst, size_t len) {
         return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
                        "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building HyperBall to compute them");
     if ((r = check_len(h, len))) return r;
-    return copy_d2h(h, h->d_sod, dst, len * 8);
+    return copy_nodes_d2h(h, h->d_sod, dst);
 }
 
 int hb_get_harmonic_centralities(const hb_handle* h, double* dst, size_t len) {
@@ -768,7 +953,7 @@ int hb_get_harmonic_centralities(const hb_handle* h, double* dst, size_t len) {
         return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
                        "Sum of inverse distances were not requested. Set HB_SUM_OF_INVERSE_DISTANCES while building HyperBall to compute them");
     if ((r = check_len(h, len))) return r;
-    return copy_d2h(h, h->d_harm, dst, len * 8);
+    return copy_nodes_d2h(h, h->d_harm, dst);
 }
 
 int hb_get_discounted_centrality(const hb_handle* h, size_t index, double* dst, size_t len) {
@@ -778,7 +963,7 @@ int hb_get_discounted_centrality(const hb_handle* h, size_t index, double* dst, 
         return set_err(const_cast<hb_handle*>(h), HB_ERR_NOT_REQUESTED,
                        "Discount centrality of index " + std::to_string(index) + " does not exist");
     if ((r = check_len(h, len))) return r;
-    return copy_d2h(h, h->d_disc[index], dst, len * 8);
+    return copy_nodes_d2h(h, h->d_disc[index], dst);
 }
 
 int hb_get_closeness_centrality(const hb_handle* h, double* dst, size_t len) {
@@ -797,14 +982,14 @@ int hb_get_reachable_nodes(const hb_handle* h, double* dst, size_t len) {
     int r = ensure_iteration(h);
     if (r) return r;
     if ((r = check_len(h, len))) return r;
-    return copy_d2h(h, h->d_est, dst, len * 8);
+    return copy_nodes_d2h(h, h->d_est, dst);
 }
 
 int hb_reachable_nodes_from(const hb_handle* h, uint64_t node, double* out) {
     int r = ensure_iteration(h);
     if (r) return r;
     if (node >= h->n || !out) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "node out of range");
-    return copy_d2h(h, h->d_est + node, out, 8);
+    return copy_d2h(h, h->d_est + h->inv_host[node], out, 8);
 }
 
 static int lin_or_nieminen(const hb_handle* h, double* dst, size_t len, bool lin) {
@@ -817,7 +1002,7 @@ static int lin_or_nieminen(const hb_handle* h, double* dst, size_t len, bool lin
         return r;
     }
     std::vector<double> cnt(len);
-    if ((r = copy_d2h(h, h->d_est, cnt.data(), len * 8))) return r;
+    if ((r = copy_nodes_d2h(h, h->d_est, cnt.data()))) return r;
     for (size_t i = 0; i < len; i++) {
         const double d = dst[i];
         if (lin) {
@@ -843,7 +1028,23 @@ int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes) {
     if (which != HB_CURRENT_STATE && which != HB_NEXT_STATE)
         return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "which must be HB_CURRENT_STATE or HB_NEXT_STATE");
     const int idx = which == HB_CURRENT_STATE ? h->cur : (h->cur ^ 1);
-    return copy_d2h(h, h->d_cnt[idx], dst, bytes);
+    if (bytes == 0) return HB_OK;
+    // the device keeps a byte per register; pack into the reference's layout
+    hb_handle* hh = const_cast<hb_handle*>(h);
+    HB_CUDA(hh, cudaSetDevice(h->device));
+    void* packed = nullptr;
+    cudaError_t e = cudaMallocAsync(&packed, bytes, h->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_err(hh, e, "cudaMallocAsync");
+    }
+    int r = hbk::launch_pack_counters(h->log2m, h->d_cnt[idx], h->d_inv, (uint8_t*)packed, h->n,
+                                      h->stream);
+    if (r == 0) r = copy_d2h(h, packed, dst, bytes);
+    else r = cuda_err(hh, (cudaError_t)r, "launch_pack_counters");
+    cudaFreeAsync(packed, h->stream);
+    cudaStreamSynchronize(h->stream);
+    return r;
 }
 
 int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* reg_size) {

@@ -40,13 +40,14 @@ struct TilePartial {
     unsigned long long vis;       // visited arcs
     unsigned long long mod;       // modified counters
     unsigned long long scanned;   // scanned nodes
+    unsigned long long sarcs;     // arcs of the scanned nodes
 };
 
 // Everything the union kernels read or write in one iteration.
 struct UnionArgs {
     const uint64_t* off;      // CSR offsets, n+1
     const uint32_t* succ;     // CSR successors, m
-    const uint8_t* curr;      // current counters, n * counter_bytes
+    const uint8_t* curr;      // current counters, n * 2^log2m bytes (byte per register)
     uint8_t* next;            // next counters
     const uint32_t* curr_mod; // modified in the previous iteration (bitmap)
     uint32_t* next_mod;       // modified in this iteration (bitmap, cleared)
@@ -71,16 +72,23 @@ struct UnionArgs {
     uint64_t list_len;
     const uint32_t* tiles;    // window k = nodes [tiles[k], tiles[k+1])
     uint32_t n_tiles;         // number of windows
-    const uint8_t* win_flags; // systolic: window holds a node to check or copy
-    const uint32_t* perm;     // per window: medium nodes then light nodes, largest degree first
-    const uint2* chunks;      // {first perm index, count | medium << 31}, in node order
+    // systolic iterations: the light and medium nodes to check or to copy, in
+    // node order, and their counts (device word: light | medium << 32);
+    // null in standard iterations, which walk the chunk table
+    const uint32_t* light_list;
+    const uint32_t* medium_list;
+    const uint64_t* list_counts;
+    const uint2* chunks;      // {first node, count | medium << 31}, in node order
+    int gather_all;           // merge every successor (nearly all changed before)
     uint64_t n_chunks;
+    unsigned long long* cursor; // next chunk to take (zero at launch)
     uint32_t tile_max_degree; // nodes above this out-degree are listed as heavy
     uint32_t acc_slot;        // partial slot accumulating the union kernels' integer totals
     TilePartial* partials;    // one per finalize block, then acc_slot
 };
 
 struct InitArgs {
+    const uint32_t* perm;     // device node -> caller node (the id that is hashed)
     uint8_t* curr;
     double* est;
     uint64_t n;
@@ -96,6 +104,20 @@ struct InitArgs {
 
 // Launchers (hb_kernels.cu). All return cudaError_t as int.
 int launch_init(int log2m, const InitArgs& a, void* stream);
+// device counters (one byte per register) -> the reference's packed layout,
+// in caller node order (inv: caller node -> device node)
+int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uint8_t* dst,
+                         uint64_t n, void* stream);
+// renumbering: deg[i] = out-degree of perm[i] (deg[n] = 0)
+int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
+                       unsigned long long* deg, void* stream);
+// succ[off[i] ..] = inv[succ0[off0[perm[i]] ..]]
+int launch_relabel_succ(const uint64_t* off0, const uint32_t* succ0, const uint32_t* perm,
+                        const uint32_t* inv, const uint64_t* off, uint32_t* succ, uint64_t n,
+                        void* stream);
+// dst[u] = src[inv[u]]: a per-node array back to caller order
+int launch_gather_f64(const double* src, const uint32_t* inv, double* dst, uint64_t n,
+                      void* stream);
 // persistent tile kernel over the worklist (or all tiles)
 int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream);
 int tile_grid(int log2m, int device);
@@ -108,8 +130,14 @@ int heavy_grid(int log2m, int device);
 // writes partials[0 .. grid)
 int launch_finalize(int log2m, const UnionArgs& a, int grid, void* stream);
 int finalize_grid(int log2m, int device);
-int launch_window_flags(const uint32_t* tiles, uint32_t n_tiles, const uint32_t* mbc,
-                        const uint32_t* curr_mod, uint8_t* flags, void* stream);
+// systolic work lists: every light / medium node set in mbc | curr_mod, in
+// node order (win_medium[w], win_light[w]: first medium / light node of
+// window w). cnt and off hold nwords + 1 words; off[nwords] gets the counts
+// (light | medium << 32).
+int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* win_medium,
+                      const uint32_t* win_light, uint64_t n, unsigned long long* cnt, uint64_t* off,
+                      unsigned long long* scratch, uint64_t scratch_len, uint32_t* light_list,
+                      uint32_t* medium_list, void* stream);
 // nodes per chunk of the union kernel: light nodes (lane-group each) and
 // medium nodes (team each)
 int chunk_nodes(int log2m, uint32_t* light, uint32_t* medium);
@@ -130,5 +158,7 @@ int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint6
                     void* stream);
 
 int num_sms(int device);
+// kernels launched so far by the calling host thread
+uint64_t launch_count();
 
 }  // namespace hbk

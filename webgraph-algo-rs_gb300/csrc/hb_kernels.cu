@@ -2,11 +2,10 @@
 //
 // One HyperBall iteration (reference: HyperBall::iterate / parallel_task,
 // src/algo/hyperball/hyperball_impl.rs:775-1152) runs as
-//   1. k_window_flags    — systolic iterations only: one byte per window of
-//                          consecutive nodes, set when the window holds a node
-//                          to check or to copy;
-//   2. k_union_window    — grid-stride sweep, one warp per chunk of nodes in
-//                          node order; every node of out-degree up to
+//   1. k_list_count,     — systolic iterations only: the light and medium
+//      k_list_fill         nodes to check or to copy, in node order;
+//   2. k_union_window    — one warp per chunk of nodes, chunks taken in node
+//                          order from a global cursor; every node of out-degree up to
 //                          tile_max_degree: merge of the modified successors'
 //                          counters, modified test, next-state store;
 //   3. k_union_heavy     — the remaining (heavy) nodes, one CTA per node;
@@ -37,6 +36,10 @@
 using namespace hbd;
 
 namespace hbk {
+
+// kernels launched by this host thread (diagnostics: launches per iteration)
+static thread_local uint64_t t_launches = 0;
+uint64_t launch_count() { return t_launches; }
 
 // ---------------------------------------------------------------------------
 // block-level publish of per-thread statistics into one partial slot
@@ -192,25 +195,38 @@ __device__ __forceinline__ void gather_successors(const UnionArgs& a, uint64_t v
 // ---------------------------------------------------------------------------
 // windows and chunks: every node up to tile_max_degree
 //
-// The graph never changes, so the work order is fixed once at build time:
-// nodes are cut into windows of WINDOW consecutive ids; inside a window the
-// medium nodes (out-degree above the light bound, up to tile_max_degree) and
-// then the light nodes are listed by decreasing out-degree in one host-built
-// permutation. The permutation is cut into chunks of one warp-step each
-// (32/G light nodes, one lane-group each, or 32/TB_MED medium nodes, one
-// team each), and the chunk table follows node order. Nodes above
-// tile_max_degree go to k_union_heavy.
+// The graph never changes, so the work order is fixed once at build time and
+// the nodes are renumbered to follow it: nodes are cut into windows of WINDOW
+// consecutive ids, and inside a window the heavy nodes, then the medium nodes
+// (out-degree above the light bound, up to tile_max_degree), then the light
+// nodes take the window's ids by decreasing out-degree. Renumbering moves a
+// node by less than WINDOW, so URL-order locality survives, and a run of
+// nodes of one kind is a run of consecutive ids: their offsets, counters and
+// per-node sums are read and written coalesced. The runs are cut into chunks
+// of one warp-step each (32/G light nodes, one lane-group each, or 32/TB_MED
+// medium nodes, one team each); the chunk table follows node order. Heavy
+// nodes run in k_union_heavy.
 //
-// k_union_window sweeps the chunk table with a grid stride, so the warps in
-// flight at any moment work on a narrow band of consecutive node ids; with
-// URL-order locality their successors cluster around that band and its
-// counters stay L2-resident while the band passes. Systolic iterations skip
-// the chunks of windows without work. Neighbouring lanes walk successor
-// lists of equal length; each lane keeps PIPE counter gathers in flight while
-// the ids and modified bits of the next PIPE successors load.
+// k_union_window hands out the chunk table in order through a global cursor,
+// so the warps in flight at any moment work on a narrow band of consecutive
+// node ids; with URL-order locality their successors cluster around that band
+// and its counters stay L2-resident while the band passes (a static
+// assignment lets warps drift apart and the band outgrows L2). Each warp
+// fetches its next chunk while it runs the current one. Systolic iterations
+// walk node lists instead (k_list_fill): runs of the light list, then of the
+// medium list; list order is node order, so locality and the degree order
+// inside each kind survive. Neighbouring lanes walk successor lists of equal
+// length; each lane keeps PIPE counter gathers in flight while the ids and
+// modified bits of the next PIPE successors load.
+//
+// In iterations where nearly every counter changed before (`gather_all`), a
+// successor's counter is merged without waiting for its modified bit: an
+// unmodified successor's counter is already contained in the node's own
+// (c_{t-1}(u) = c_{t-2}(u) <= c_{t-1}(v)), so merging it changes nothing, and
+// the bit is tested only to count visited arcs.
 // ---------------------------------------------------------------------------
 constexpr int WINDOW = 1024;
-constexpr int PIPE = 2;
+constexpr int PIPE = 4;
 
 template <int LOG2M>
 struct TileGeo {
@@ -219,62 +235,56 @@ struct TileGeo {
 };
 
 // Merges into acc (chunk c) the counters of the successors e0, e0+stride, ...
-// (< e1) of node v modified in the previous iteration; returns how many were
-// merged (self-loops excluded).
+// (< e1) of node v modified in the previous iteration (or of all of them when
+// `all`); returns how many modified non-loop successors there were.
 template <int LOG2M>
-__device__ __forceinline__ uint32_t gather_pipelined(const UnionArgs& a, uint64_t v, int c,
+__device__ __forceinline__ uint32_t gather_pipelined(const UnionArgs& a, uint32_t v, int c,
                                                      uint64_t e0, uint64_t e1, uint32_t stride,
-                                                     uint32_t (&acc)[Geo<LOG2M>::NW],
+                                                     bool all, uint32_t (&acc)[Geo<LOG2M>::NW],
                                                      uint32_t& grew) {
     using Gm = Geo<LOG2M>;
     constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
-    const uint32_t vv = (uint32_t)v;
     uint32_t cnt = 0;
     uint32_t s[PIPE];
-    bool m[PIPE];
+    bool ld[PIPE];
 #pragma unroll
     for (int k = 0; k < PIPE; k++) {
         const uint64_t e = e0 + (uint64_t)k * stride;
-        s[k] = e < e1 ? __ldg(a.succ + e) : vv;
+        s[k] = e < e1 ? __ldg(a.succ + e) : v;
     }
 #pragma unroll
-    for (int k = 0; k < PIPE; k++) m[k] = s[k] != vv && test_bit(a.curr_mod, s[k]);
+    for (int k = 0; k < PIPE; k++) {
+        const bool m = s[k] != v && test_bit(a.curr_mod, s[k]);
+        cnt += m;
+        ld[k] = all ? s[k] != v : m;
+    }
     for (uint64_t e = e0; e < e1; e += (uint64_t)PIPE * stride) {
         uint32_t y[PIPE][NW];
 #pragma unroll
         for (int k = 0; k < PIPE; k++)
-            if (m[k]) load_chunk<LOG2M>(a.curr, s[k], c, y[k]);
-        uint32_t ns[PIPE];
+            if (ld[k]) load_chunk<LOG2M>(a.curr, s[k], c, y[k]);
 #pragma unroll
         for (int k = 0; k < PIPE; k++) {
             const uint64_t en = e + (uint64_t)(PIPE + k) * stride;
-            ns[k] = en < e1 ? __ldg(a.succ + en) : vv;
-        }
-        bool nm[PIPE];
-#pragma unroll
-        for (int k = 0; k < PIPE; k++) nm[k] = ns[k] != vv && test_bit(a.curr_mod, ns[k]);
-#pragma unroll
-        for (int k = 0; k < PIPE; k++) {
-            if (m[k]) {
-                merge_chunk<REGS>(acc, y[k], grew);
-                cnt++;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < PIPE; k++) {
-            s[k] = ns[k];
-            m[k] = nm[k];
+            const uint32_t ns = en < e1 ? __ldg(a.succ + en) : v;
+            if (ld[k]) merge_chunk<REGS>(acc, y[k], grew);
+            const bool m = ns != v && test_bit(a.curr_mod, ns);
+            cnt += m;
+            ld[k] = all ? ns != v : m;
+            s[k] = ns;
         }
     }
     return cnt;
 }
 
-// One warp-step over up to 32/G nodes of a list: scan, copy or nothing.
-// Returns through the accumulators; sets the modified bits.
+// One warp-step over up to 32/TB nodes: the consecutive nodes [b, e), or
+// list[b .. e) when a list is given. Scan, copy or nothing; returns through the
+// accumulators; sets the modified bits.
 template <int LOG2M, int TB>
-__device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ perm,
-                                          uint32_t b, uint32_t e, unsigned long long& vis,
-                                          unsigned long long& modc, unsigned long long& scanned) {
+__device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
+                                          uint32_t b, uint32_t e,
+                                          unsigned long long& vis, unsigned long long& modc,
+                                          unsigned long long& scanned, unsigned long long& sarcs) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
     constexpr int PB = TB / G;   // arc lanes per node
@@ -285,10 +295,9 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
     const unsigned lmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * TB));
     for (uint32_t base = b; base < e; base += NPW) {
         const uint32_t idx = base + slot;
+        const uint32_t v = list ? (idx < e ? __ldg(list + idx) : 0u) : idx;
         bool scan = false, copy = false;
-        uint64_t v = 0;
         if (idx < e) {
-            v = __ldg(perm + idx);
             if (!a.systolic || test_bit(a.mbc, v))
                 scan = true;
             else if (test_bit(a.curr_mod, v))
@@ -305,7 +314,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                 for (int k = 0; k < NW; k++) acc[k] = 0u;
             }
             uint32_t grew = 0;
-            uint32_t w = gather_pipelined<LOG2M>(a, v, c, s0 + p, s1, PB, acc, grew);
+            uint32_t w = gather_pipelined<LOG2M>(a, v, c, s0 + p, s1, PB, a.gather_all != 0, acc, grew);
             if constexpr (PB > 1) {
                 __syncwarp(tmask);
 #pragma unroll
@@ -333,6 +342,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                 store_chunk<LOG2M>(a.next, v, c, acc);
                 if (c == 0) {
                     scanned++;
+                    sarcs += s1 - s0;
                     vis += w;
                 }
             }
@@ -345,7 +355,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
         const bool flag = changed && p == 0 && c == 0;
         const unsigned want = __ballot_sync(0xffffffffu, flag);
         if (want) {
-            const uint32_t word = flag ? (uint32_t)(v >> 5) : 0xffffffffu;
+            const uint32_t word = flag ? (v >> 5) : 0xffffffffu;
             const unsigned peers = __match_any_sync(0xffffffffu, word);
             // each group of lanes on one word reduces with its own mask
             const uint32_t bits = __reduce_or_sync(peers, flag ? (1u << (v & 31)) : 0u);
@@ -355,31 +365,80 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
     }
 }
 
+// Work item k: a chunk of the table, or (systolic) a run of the light list
+// followed by runs of the medium list; {first, count | medium << 31}.
+struct WorkItems {
+    uint64_t n_work, light_items;
+    uint32_t n_light, n_medium;
+};
+
+template <int NPW_L, int NPW_M>
+__device__ __forceinline__ WorkItems work_items(const UnionArgs& a) {
+    WorkItems w{};
+    if (a.light_list) {
+        const uint64_t c = *a.list_counts;
+        w.n_light = (uint32_t)c;
+        w.n_medium = (uint32_t)(c >> 32);
+        w.light_items = (w.n_light + NPW_L - 1) / NPW_L;
+        w.n_work = w.light_items + (w.n_medium + NPW_M - 1) / NPW_M;
+    } else {
+        w.n_work = a.n_chunks;
+    }
+    return w;
+}
+
+template <int NPW_L, int NPW_M>
+__device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
+                                         unsigned long long k) {
+    if (k >= w.n_work) return make_uint2(0u, 0u);
+    if (!a.light_list) return __ldg(a.chunks + k);
+    if (k < w.light_items) {
+        const uint32_t f = (uint32_t)(k * NPW_L);
+        return make_uint2(f, min((uint32_t)NPW_L, w.n_light - f));
+    }
+    const uint32_t f = (uint32_t)((k - w.light_items) * NPW_M);
+    return make_uint2(f, min((uint32_t)NPW_M, w.n_medium - f) | 0x80000000u);
+}
+
 template <int LOG2M>
-__global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
+__global__ void __launch_bounds__(256, 2) k_union_window(UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
     constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
     const int lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long vis = 0, modc = 0, scanned = 0;
-    // Warp w takes chunks w, w+W, ...: all warps sweep the node range
-    // together, so the counters of nearby successors stay in L2.
-    for (uint64_t k = gw; k < a.n_chunks; k += nw) {
-        const uint2 d = __ldg(a.chunks + k);
-        const uint32_t cnt = d.y & 0x7fffffffu;
-        if (a.systolic && !__ldg(a.win_flags + __ldg(a.perm + d.x) / WINDOW)) continue;
-        if (d.y >> 31)
-            run_nodes<LOG2M, TB_MED>(a, a.perm, d.x, d.x + cnt, vis, modc, scanned);
+    constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
+    unsigned long long vis = 0, modc = 0, scanned = 0, sarcs = 0;
+    const WorkItems wi = work_items<NPW_L, NPW_M>(a);
+    const uint64_t n_work = wi.n_work;
+    // two-deep pipeline of work items: the descriptor of the next chunk and
+    // the cursor value of the one after load while the current chunk runs
+    unsigned long long k0 = 0, k1 = 0;
+    if (lane == 0) {
+        k0 = atomicAdd(a.cursor, 1ull);
+        k1 = atomicAdd(a.cursor, 1ull);
+    }
+    k0 = __shfl_sync(0xffffffffu, k0, 0);
+    k1 = __shfl_sync(0xffffffffu, k1, 0);
+    uint2 d0 = item_at<NPW_L, NPW_M>(a, wi, k0);
+    while (k0 < n_work) {
+        const uint2 d1 = item_at<NPW_L, NPW_M>(a, wi, k1);
+        unsigned long long k2 = 0;
+        if (lane == 0 && k1 < n_work) k2 = atomicAdd(a.cursor, 1ull);
+        const uint32_t cnt = d0.y & 0x7fffffffu;
+        if (d0.y >> 31)
+            run_nodes<LOG2M, TB_MED>(a, a.medium_list, d0.x, d0.x + cnt, vis, modc, scanned, sarcs);
         else
-            run_nodes<LOG2M, G>(a, a.perm, d.x, d.x + cnt, vis, modc, scanned);
+            run_nodes<LOG2M, G>(a, a.light_list, d0.x, d0.x + cnt, vis, modc, scanned, sarcs);
+        k0 = k1;
+        d0 = d1;
+        k1 = k1 < n_work ? __shfl_sync(0xffffffffu, k2, 0) : k1;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         vis += __shfl_xor_sync(0xffffffffu, vis, off);
         modc += __shfl_xor_sync(0xffffffffu, modc, off);
         scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+        sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
     }
     if (lane == 0) {
         // integer totals are order independent
@@ -387,6 +446,7 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
         if (vis) atomicAdd(&t->vis, vis);
         if (modc) atomicAdd(&t->mod, modc);
         if (scanned) atomicAdd(&t->scanned, scanned);
+        if (sarcs) atomicAdd(&t->sarcs, sarcs);
     }
 }
 
@@ -405,7 +465,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     const int tid = threadIdx.x;
     const int p = tid / G, c = tid % G;
     const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
-    unsigned long long vis = 0, modc = 0, scanned = 0;
+    unsigned long long vis = 0, modc = 0, scanned = 0, sarcs = 0;
     for (uint64_t idx = blockIdx.x; idx < a.list_len; idx += gridDim.x) {
         const uint64_t v = __ldg(a.list + idx);
         const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
@@ -446,6 +506,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                 const bool changed = commit_node<LOG2M>(a, v, c, leader_mask, prev, acc);
                 if (c == 0) {
                     scanned++;
+                    sarcs += s1 - s0;
                     if (changed) {
                         atomicOr(a.next_mod + (v >> 5), 1u << (v & 31));
                         modc++;
@@ -466,6 +527,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
         vis += __shfl_xor_sync(0xffffffffu, vis, off);
         modc += __shfl_xor_sync(0xffffffffu, modc, off);
         scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+        sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
     }
     if (lane == 0) {
         // integer totals are order independent
@@ -473,31 +535,19 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
         if (vis) atomicAdd(&t->vis, vis);
         if (modc) atomicAdd(&t->mod, modc);
         if (scanned) atomicAdd(&t->scanned, scanned);
+        if (sarcs) atomicAdd(&t->sarcs, sarcs);
     }
 }
 
 // ---------------------------------------------------------------------------
 // init (HB:1155-1213): every counter gets add(node) (or its weighted values)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t get_reg(const uint8_t* c, uint32_t j) {
-    const uint32_t bit = 5u * j, byte = bit >> 3, sh = bit & 7u;
-    const uint32_t w = (uint32_t)c[byte] | ((sh + 5u > 8u) ? ((uint32_t)c[byte + 1] << 8) : 0u);
-    return (w >> sh) & 31u;
-}
-__device__ __forceinline__ void set_reg(uint8_t* c, uint32_t j, uint32_t val) {
-    const uint32_t bit = 5u * j, byte = bit >> 3, sh = bit & 7u;
-    const uint32_t mask = 31u << sh;
-    c[byte] = (uint8_t)((c[byte] & ~mask) | ((val << sh) & 0xffu));
-    if (sh + 5u > 8u)
-        c[byte + 1] = (uint8_t)((c[byte + 1] & ~(mask >> 8)) | (val >> (8u - sh)));
-}
-
 template <int LOG2M>
 __device__ __forceinline__ uint32_t add_hash(uint8_t* counter, uint64_t x) {
     const uint32_t j = (uint32_t)(x & ((1ull << LOG2M) - 1ull));
     const uint64_t y = (x >> LOG2M) | (1ull << 30);
     const uint32_t cand = (uint32_t)__ffsll((long long)y);  // trailing zeros + 1
-    if (get_reg(counter, j) < cand) set_reg(counter, j, cand);
+    if (counter[j] < cand) counter[j] = (uint8_t)cand;
     return cand;
 }
 
@@ -509,7 +559,8 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
          v += (uint64_t)gridDim.x * blockDim.x) {
         uint8_t* counter = a.curr + v * (uint64_t)Gm::COUNTER_BYTES;
         if (a.weights == nullptr) {
-            const uint64_t x = a.hash_kind == 1 ? hash_jenkins(v, a.seed) : hash_sip13(v);
+            const uint64_t u = __ldg(a.perm + v);  // the caller's id is hashed
+            const uint64_t x = a.hash_kind == 1 ? hash_jenkins(u, a.seed) : hash_sip13(u);
             const uint32_t val = add_hash<LOG2M>(counter, x);
             saw31 |= val == 31u;
             // one register holds val, the other m-1 are zero
@@ -520,8 +571,9 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
         } else {
             // HB:1167-1174 adds random values; here value k of node v is
             // SplitMix64 step k from weight_seed ^ v * golden, hashed as usual.
-            uint64_t s = a.weight_seed ^ (v * 0x9e3779b97f4a7c15ull);
-            const uint64_t w = a.weights[v];
+            const uint64_t u = __ldg(a.perm + v);
+            uint64_t s = a.weight_seed ^ (u * 0x9e3779b97f4a7c15ull);
+            const uint64_t w = a.weights[u];
             for (uint64_t k = 0; k < w; k++) {
                 s += 0x9e3779b97f4a7c15ull;
                 uint64_t z = s;
@@ -534,7 +586,7 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
             uint64_t hs = 0;
             uint32_t z = 0, c31 = 0;
             for (uint32_t j = 0; j < (uint32_t)Gm::M; j++) {
-                const uint32_t r = get_reg(counter, j);
+                const uint32_t r = counter[j];
                 hs += (uint64_t)(0x80000000u >> r);
                 z += r == 0u;
                 c31 += r == 31u;
@@ -546,6 +598,71 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
     // Registers only ever take values some initial register had; remember
     // whether 31 occurs so counts can skip looking for it.
     if (__syncthreads_or(saw31) && threadIdx.x == 0) atomicOr(a.any31, 1);
+}
+
+// ---------------------------------------------------------------------------
+// byte registers -> the reference's packed layout (5-bit registers LSB-first,
+// HLL:72-115): one thread per group of 8 registers (8 bytes in, 5 bytes out)
+// ---------------------------------------------------------------------------
+template <int LOG2M>
+__global__ void __launch_bounds__(256) k_pack_counters(const uint8_t* __restrict__ src,
+                                                       const uint32_t* __restrict__ inv,
+                                                       uint8_t* __restrict__ dst, uint64_t n) {
+    using Gm = Geo<LOG2M>;
+    constexpr uint64_t GROUPS = Gm::M / 8;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * GROUPS;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = i / GROUPS, g = i % GROUPS;
+        const uint64_t dv = __ldg(inv + v);
+        const uint2 r = __ldg(reinterpret_cast<const uint2*>(src + dv * Gm::COUNTER_BYTES) + g);
+        uint64_t bits = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            bits |= (uint64_t)((r.x >> (8 * k)) & 31u) << (5 * k);
+            bits |= (uint64_t)((r.y >> (8 * k)) & 31u) << (5 * (k + 4));
+        }
+        uint8_t* o = dst + v * (uint64_t)Gm::PACKED_BYTES + g * 5;
+#pragma unroll
+        for (int k = 0; k < 5; k++) o[k] = (uint8_t)(bits >> (8 * k));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// renumbering (see "windows and chunks") and results back in caller order
+// ---------------------------------------------------------------------------
+__global__ void k_perm_degree(const uint64_t* __restrict__ off0, const uint32_t* __restrict__ perm,
+                              uint64_t n, unsigned long long* __restrict__ deg) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i == n) {
+            deg[n] = 0;
+        } else {
+            const uint32_t u = __ldg(perm + i);
+            deg[i] = __ldg(off0 + u + 1) - __ldg(off0 + u);
+        }
+    }
+}
+
+// one warp per renumbered node: its successor list, renumbered
+__global__ void k_relabel_succ(const uint64_t* __restrict__ off0, const uint32_t* __restrict__ succ0,
+                               const uint32_t* __restrict__ perm, const uint32_t* __restrict__ inv,
+                               const uint64_t* __restrict__ off, uint32_t* __restrict__ succ,
+                               uint64_t n) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = gw; i < n; i += nw) {
+        const uint32_t u = __ldg(perm + i);
+        const uint64_t s0 = __ldg(off0 + u), d = __ldg(off0 + u + 1) - s0, t0 = __ldg(off + i);
+        for (uint64_t j = lane; j < d; j += 32) succ[t0 + j] = __ldg(inv + __ldg(succ0 + s0 + j));
+    }
+}
+
+__global__ void k_gather_f64(const double* __restrict__ src, const uint32_t* __restrict__ inv,
+                             double* __restrict__ dst, uint64_t n) {
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
+         u += (uint64_t)gridDim.x * blockDim.x)
+        dst[u] = src[__ldg(inv + u)];
 }
 
 // ---------------------------------------------------------------------------
@@ -582,21 +699,23 @@ constexpr int REDUCE_BLOCKS = 256;
 __global__ void k_reduce_partials(const TilePartial* __restrict__ in, uint64_t count,
                                   TilePartial* __restrict__ out) {
     __shared__ double s_nf[256];
-    __shared__ unsigned long long s_v[256], s_m[256], s_s[256];
+    __shared__ unsigned long long s_v[256], s_m[256], s_s[256], s_a[256];
     const uint64_t per = (count + gridDim.x - 1) / gridDim.x;
     const uint64_t b = (uint64_t)blockIdx.x * per, e = min(count, b + per);
     double nf = 0.0;
-    unsigned long long v = 0, mo = 0, sc = 0;
+    unsigned long long v = 0, mo = 0, sc = 0, sa = 0;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
         nf = __dadd_rn(nf, in[i].nf);
         v += in[i].vis;
         mo += in[i].mod;
         sc += in[i].scanned;
+        sa += in[i].sarcs;
     }
     s_nf[threadIdx.x] = nf;
     s_v[threadIdx.x] = v;
     s_m[threadIdx.x] = mo;
     s_s[threadIdx.x] = sc;
+    s_a[threadIdx.x] = sa;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
         if ((int)threadIdx.x < w) {
@@ -604,29 +723,64 @@ __global__ void k_reduce_partials(const TilePartial* __restrict__ in, uint64_t c
             s_v[threadIdx.x] += s_v[threadIdx.x + w];
             s_m[threadIdx.x] += s_m[threadIdx.x + w];
             s_s[threadIdx.x] += s_s[threadIdx.x + w];
+            s_a[threadIdx.x] += s_a[threadIdx.x + w];
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = TilePartial{s_nf[0], s_v[0], s_m[0], s_s[0]};
+    if (threadIdx.x == 0) out[blockIdx.x] = TilePartial{s_nf[0], s_v[0], s_m[0], s_s[0], s_a[0]};
 }
 
 // Systolic iterations: flags the windows holding a node that must be checked
 // or copied; the union kernel skips the chunks of the other windows.
-__global__ void k_window_flags(const uint32_t* __restrict__ tiles, uint32_t n_tiles,
-                               const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
-                               uint8_t* flags) {
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_tiles; k += gridDim.x * blockDim.x) {
-        const uint64_t r0 = __ldg(tiles + k), r1 = __ldg(tiles + k + 1);
-        bool any = false;
-        for (uint64_t w = r0 >> 5; w <= ((r1 - 1) >> 5) && !any; w++) {
-            uint32_t bits = __ldg(mbc + w) | __ldg(curr_mod + w);
-            // keep only the bits of this window's nodes
-            const uint64_t lo = w << 5;
-            if (r0 > lo) bits &= ~0u << (uint32_t)(r0 - lo);
-            if (r1 < lo + 32) bits &= (1u << (uint32_t)(r1 - lo)) - 1u;
-            any = bits != 0u;
+// bits of word i (nodes 32i .. 32i+31, all in one window) split into light
+// and medium nodes
+__device__ __forceinline__ void split_word(uint64_t i, uint32_t bits, const uint32_t* win_medium,
+                                           const uint32_t* win_light, uint32_t& lb, uint32_t& mb) {
+    const uint64_t lo = i << 5, w = lo / WINDOW;
+    const uint64_t ms = __ldg(win_medium + w), ls = __ldg(win_light + w);
+    auto from = [&](uint64_t x) -> uint32_t {  // bits of nodes >= x
+        return x <= lo ? 0xffffffffu : x >= lo + 32 ? 0u : 0xffffffffu << (uint32_t)(x - lo);
+    };
+    lb = bits & from(ls);
+    mb = bits & from(ms) & ~from(ls);
+}
+
+__global__ void k_list_count(const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
+                             const uint32_t* __restrict__ win_medium,
+                             const uint32_t* __restrict__ win_light, uint64_t nwords,
+                             unsigned long long* __restrict__ cnt) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nwords;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i == nwords) {
+            cnt[i] = 0;
+            continue;
         }
-        flags[k] = any ? 1 : 0;
+        uint32_t lb, mb;
+        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), win_medium, win_light, lb, mb);
+        cnt[i] = (unsigned long long)__popc(lb) | ((unsigned long long)__popc(mb) << 32);
+    }
+}
+
+__global__ void k_list_fill(const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
+                            const uint32_t* __restrict__ win_medium,
+                            const uint32_t* __restrict__ win_light, uint64_t nwords,
+                            const uint64_t* __restrict__ off, uint32_t* __restrict__ light_list,
+                            uint32_t* __restrict__ medium_list) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lb, mb;
+        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), win_medium, win_light, lb, mb);
+        const uint64_t o = off[i];
+        uint32_t ol = (uint32_t)o, om = (uint32_t)(o >> 32);
+        const uint32_t lo = (uint32_t)(i << 5);
+        while (lb) {
+            light_list[ol++] = lo + (uint32_t)(__ffs(lb) - 1);
+            lb &= lb - 1u;
+        }
+        while (mb) {
+            medium_list[om++] = lo + (uint32_t)(__ffs(mb) - 1);
+            mb &= mb - 1u;
+        }
     }
 }
 
@@ -746,24 +900,38 @@ int num_sms(int device) {
 template <int LOG2M>
 static int init_impl(const InitArgs& a, cudaStream_t s) {
     const int grid = (int)std::min<uint64_t>((a.n + 255) / 256 + 1, 65535);
+    ++t_launches;
     k_init<LOG2M><<<grid, 256, 0, s>>>(a);
     return (int)cudaGetLastError();
 }
 
 template <int LOG2M>
+static int pack_impl(const uint8_t* src, const uint32_t* inv, uint8_t* dst, uint64_t n,
+                     cudaStream_t s) {
+    const uint64_t items = n * (uint64_t)(Geo<LOG2M>::M / 8);
+    const int grid = (int)std::min<uint64_t>((items + 255) / 256 + 1, 65535);
+    ++t_launches;
+    k_pack_counters<LOG2M><<<grid, 256, 0, s>>>(src, inv, dst, n);
+    return (int)cudaGetLastError();
+}
+
+template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    ++t_launches;
     k_union_window<LOG2M><<<grid, 256, 0, s>>>(a);
     return (int)cudaGetLastError();
 }
 
 template <int LOG2M>
 static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    ++t_launches;
     k_union_heavy<LOG2M><<<grid, 256, 0, s>>>(a);
     return (int)cudaGetLastError();
 }
 
 template <int LOG2M>
 static int finalize_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    ++t_launches;
     k_finalize<LOG2M><<<grid, 256, 0, s>>>(a);
     return (int)cudaGetLastError();
 }
@@ -814,6 +982,38 @@ int launch_init(int log2m, const InitArgs& a, void* stream) {
 #undef CALL
 }
 
+int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uint8_t* dst,
+                         uint64_t n, void* stream) {
+#define CALL(L) pack_impl<L>(src, inv, dst, n, (cudaStream_t)stream)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
+                       unsigned long long* deg, void* stream) {
+    const int grid = (int)std::min<uint64_t>((n + 256) / 256 + 1, 8192);
+    ++t_launches;
+    k_perm_degree<<<grid, 256, 0, (cudaStream_t)stream>>>(off0, perm, n, deg);
+    return (int)cudaGetLastError();
+}
+
+int launch_relabel_succ(const uint64_t* off0, const uint32_t* succ0, const uint32_t* perm,
+                        const uint32_t* inv, const uint64_t* off, uint32_t* succ, uint64_t n,
+                        void* stream) {
+    const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256 + 1, 16384);
+    ++t_launches;
+    k_relabel_succ<<<grid, 256, 0, (cudaStream_t)stream>>>(off0, succ0, perm, inv, off, succ, n);
+    return (int)cudaGetLastError();
+}
+
+int launch_gather_f64(const double* src, const uint32_t* inv, double* dst, uint64_t n,
+                      void* stream) {
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256 + 1, 8192);
+    ++t_launches;
+    k_gather_f64<<<grid, 256, 0, (cudaStream_t)stream>>>(src, inv, dst, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream) {
 #define CALL(L) tile_impl<L>(a, grid, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
@@ -859,24 +1059,39 @@ int chunk_nodes(int log2m, uint32_t* light, uint32_t* medium) {
 #undef CALL
 }
 
-int launch_window_flags(const uint32_t* tiles, uint32_t n_tiles, const uint32_t* mbc,
-                        const uint32_t* curr_mod, uint8_t* flags, void* stream) {
-    if (n_tiles == 0) return 0;
-    const int grid = (int)std::min<uint64_t>((n_tiles + 255) / 256, 4096);
-    k_window_flags<<<grid, 256, 0, (cudaStream_t)stream>>>(tiles, n_tiles, mbc, curr_mod, flags);
+int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* win_medium,
+                      const uint32_t* win_light, uint64_t n, unsigned long long* cnt, uint64_t* off,
+                      unsigned long long* scratch, uint64_t scratch_len, uint32_t* light_list,
+                      uint32_t* medium_list, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t nwords = (n + 31) / 32;
+    const int grid = (int)std::min<uint64_t>((nwords + 256) / 256 + 1, 8192);
+    ++t_launches;
+    k_list_count<<<grid, 256, 0, s>>>(mbc, curr_mod, win_medium, win_light, nwords, cnt);
+    int e = (int)cudaGetLastError();
+    if (e) return e;
+    e = launch_exclusive_scan_u64(cnt, off, nwords + 1, scratch, scratch_len, stream);
+    if (e) return e;
+    ++t_launches;
+    k_list_fill<<<grid, 256, 0, s>>>(mbc, curr_mod, win_medium, win_light, nwords, off, light_list,
+                                     medium_list);
     return (int)cudaGetLastError();
 }
+
 
 int launch_reduce_partials(const TilePartial* in, uint64_t count, TilePartial* scratch,
                            TilePartial* out, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
+    ++t_launches;
     k_reduce_partials<<<REDUCE_BLOCKS, 256, 0, s>>>(in, count, scratch);
+    ++t_launches;
     k_reduce_partials<<<1, 256, 0, s>>>(scratch, REDUCE_BLOCKS, out);
     return (int)cudaGetLastError();
 }
 
 int launch_mark_preds(const uint32_t* next_mod, const uint64_t* toff, const uint32_t* tsucc,
                       uint32_t* next_mbc, uint64_t n, int grid, void* stream) {
+    ++t_launches;
     k_mark_preds<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, toff, tsucc, next_mbc, n);
     return (int)cudaGetLastError();
 }
@@ -884,6 +1099,7 @@ int launch_mark_preds(const uint32_t* next_mod, const uint64_t* toff, const uint
 int launch_fill_u32(uint32_t* p, uint32_t v, uint64_t count, void* stream) {
     if (count == 0) return 0;
     const int grid = (int)std::min<uint64_t>((count + 255) / 256, 4096);
+    ++t_launches;
     k_fill_u32<<<grid, 256, 0, (cudaStream_t)stream>>>(p, v, count);
     return (int)cudaGetLastError();
 }
@@ -892,6 +1108,7 @@ int launch_transpose_count(const uint32_t* succ, uint64_t m, unsigned long long*
                            void* stream) {
     if (m == 0) return 0;
     const int grid = (int)std::min<uint64_t>((m + 255) / 256, 8192);
+    ++t_launches;
     k_count_indeg<<<grid, 256, 0, (cudaStream_t)stream>>>(succ, m, indeg);
     return (int)cudaGetLastError();
 }
@@ -915,6 +1132,7 @@ int launch_exclusive_scan_u64(const unsigned long long* in, uint64_t* out_, uint
     if (2 * tiles > scratch_len) return (int)cudaErrorInvalidValue;
     unsigned long long* sums = scratch;
     unsigned long long* sums_scan = scratch + tiles;
+    ++t_launches;
     k_scan_tile<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, count, sums);
     int e = (int)cudaGetLastError();
     if (e) return e;
@@ -922,6 +1140,7 @@ int launch_exclusive_scan_u64(const unsigned long long* in, uint64_t* out_, uint
         e = launch_exclusive_scan_u64(sums, (uint64_t*)sums_scan, tiles, scratch + 2 * tiles,
                                       scratch_len - 2 * tiles, stream);
         if (e) return e;
+        ++t_launches;
         k_scan_add<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(out, count, sums_scan);
         e = (int)cudaGetLastError();
     }
@@ -932,6 +1151,7 @@ int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t
                              unsigned long long* cursor, uint32_t* tsucc, void* stream) {
     if (n == 0) return 0;
     const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256, 8192);
+    ++t_launches;
     k_transpose_scatter<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, cursor, tsucc);
     return (int)cudaGetLastError();
 }
@@ -939,6 +1159,7 @@ int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t
 int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m, int* bad,
                     void* stream) {
     const int grid = (int)std::min<uint64_t>((std::max(n, m) + 255) / 256 + 1, 8192);
+    ++t_launches;
     k_validate<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, m, bad);
     return (int)cudaGetLastError();
 }

@@ -1,22 +1,29 @@
 // Device-side HyperLogLog arithmetic for sm_103a.
 //
-// Counter layout is the reference's (src/utils/slice_counter_array.rs:166-169
-// with hyper_log_log_logic.rs:72-115): counter i occupies bytes
-// [i*B, (i+1)*B), B = 2^log2m * 5 / 8, 5-bit registers packed LSB-first into
-// little-endian words. Register width is always 5: register_size(n) =
-// max(5, ceil(ln(log2(n)/ln 2))) exceeds 5 only for log2(n) > 102.
+// The reference keeps counter i in bytes [i*B, (i+1)*B), B = 2^log2m * 5 / 8,
+// with 5-bit registers packed LSB-first into little-endian words
+// (src/utils/slice_counter_array.rs:166-169, hyper_log_log_logic.rs:72-115).
+// Register width is always 5: register_size(n) = max(5, ceil(ln(log2(n)/ln 2)))
+// exceeds 5 only for log2(n) > 102. That packed form is the interchange
+// format (hb_get_registers packs on the device, k_pack_counters).
 //
-// GPU restructuring: a counter is split into register-aligned chunks of at
-// most 64 registers (320 bits = 40 bytes). The reference's broadword max
-// (hyper_log_log_logic.rs:469-576) never carries, borrows or shifts across a
-// register boundary, and 320 is a multiple of both 5 and 32, so each chunk is
-// merged independently by one lane, on ten 32-bit words, with the very same
-// formula:
-//     z    = ((((y | H) - (x & ~H)) | (y ^ x)) ^ (y | ~x)) & H
-//     mask = ((((z >> 4) | H) - L) | H) ^ z
-//     x    = x ^ ((x ^ y) & mask)
-// (H / L: highest / lowest bit of every register), the multi-word
-// subtractions running as one PTX borrow chain.
+// In HBM a counter holds one register per byte: counter i occupies bytes
+// [i*m, (i+1)*m), register j is byte j. A register never exceeds 31
+// (trailing zeros of a value with bit 30 set, plus one), so bits 5-7 of every
+// byte are zero, and the register-wise max of the reference's broadword merge
+// (hyper_log_log_logic.rs:469-576) becomes, per 32-bit word of four registers,
+//     t    = (x | 0x80808080) - y      bit 7 of a byte set iff x >= y there;
+//                                      no borrow leaves a byte (x+128-y > 0)
+//     keep = prmt(t, sign-replicate)   0xff where x >= y, else 0x00
+//     x    = y ^ ((x ^ y) & keep)
+// five integer instructions per four registers, against about fourteen per
+// word of the packed broadword form. Counters of 2^log2m bytes are also
+// 16-byte aligned (128-bit loads and stores) and, at log2m >= 6, never cross a
+// 64-byte boundary, so a counter gather moves exactly its own sectors.
+//
+// A counter is processed in chunks of at most 32 registers (32 bytes, eight
+// words, two 128-bit accesses), one lane per chunk, so a lane holds a chunk
+// and four in-flight successor chunks in registers at full occupancy.
 //
 // count() (hyper_log_log_logic.rs:169-186) is computed exactly: the harmonic
 // sum of 2^-v over <= 2^12 registers is a multiple of 2^-31 below 2^13, so it
@@ -34,221 +41,66 @@ namespace hbd {
 template <int LOG2M>
 struct Geo {
     static constexpr int M = 1 << LOG2M;
-    static constexpr int CHUNK_REGS = M < 64 ? M : 64;
-    static constexpr int CHUNKS = M / CHUNK_REGS;               // chunks per counter
-    static constexpr int NW = (CHUNK_REGS * 5 + 31) / 32;       // 32-bit words per chunk
-    static constexpr int COUNTER_BYTES = M * 5 / 8;
-    static constexpr int CHUNK_BYTES = CHUNK_REGS * 5 / 8;      // 10, 20 or 40
+    static constexpr int CHUNK_REGS = M < 32 ? M : 32;
+    static constexpr int CHUNKS = M / CHUNK_REGS;            // chunks per counter
+    static constexpr int NW = CHUNK_REGS / 4;                // 32-bit words per chunk
+    static constexpr int COUNTER_BYTES = M;                  // device stride, one byte per register
+    static constexpr int CHUNK_BYTES = CHUNK_REGS;           // 16 or 32
+    static constexpr int PACKED_BYTES = M * 5 / 8;           // the reference's counter size
 };
 
-// Word i of the mask with bit `bit` of each of `regs` 5-bit registers set.
-__host__ __device__ constexpr uint32_t mask_word(int regs, int i, int bit) {
-    uint32_t w = 0;
-    for (int k = 0; k < regs; k++) {
-        int p = 5 * k + bit;
-        if (p >= 32 * i && p < 32 * i + 32) w |= 1u << (p - 32 * i);
-    }
-    return w;
+// Replicates bit 7 of every byte of t over its byte (PTX prmt, sign mode).
+__device__ __forceinline__ uint32_t byte_signs(uint32_t t) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(t), "r"(0u), "r"(0xBA98u));
+    return r;
 }
 
-// ---------------------------------------------------------------------------
-// multi-word subtraction r = a - b (little-endian words) as one borrow chain
-// ---------------------------------------------------------------------------
-template <int NW>
-struct SubChain;
-
-template <>
-struct SubChain<3> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[3], const uint32_t (&a)[3],
-                                               const uint32_t (&b)[3]) {
-        asm("sub.cc.u32 %0, %3, %6;\n\t"
-            "subc.cc.u32 %1, %4, %7;\n\t"
-            "subc.u32 %2, %5, %8;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
-    }
-};
-
-template <>
-struct SubChain<5> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[5], const uint32_t (&a)[5],
-                                               const uint32_t (&b)[5]) {
-        asm("sub.cc.u32 %0, %5, %10;\n\t"
-            "subc.cc.u32 %1, %6, %11;\n\t"
-            "subc.cc.u32 %2, %7, %12;\n\t"
-            "subc.cc.u32 %3, %8, %13;\n\t"
-            "subc.u32 %4, %9, %14;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(b[0]), "r"(b[1]),
-              "r"(b[2]), "r"(b[3]), "r"(b[4]));
-    }
-};
-
-template <>
-struct SubChain<10> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[10], const uint32_t (&a)[10],
-                                               const uint32_t (&b)[10]) {
-        asm("sub.cc.u32 %0, %10, %20;\n\t"
-            "subc.cc.u32 %1, %11, %21;\n\t"
-            "subc.cc.u32 %2, %12, %22;\n\t"
-            "subc.cc.u32 %3, %13, %23;\n\t"
-            "subc.cc.u32 %4, %14, %24;\n\t"
-            "subc.cc.u32 %5, %15, %25;\n\t"
-            "subc.cc.u32 %6, %16, %26;\n\t"
-            "subc.cc.u32 %7, %17, %27;\n\t"
-            "subc.cc.u32 %8, %18, %28;\n\t"
-            "subc.u32 %9, %19, %29;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-              "=r"(r[7]), "=r"(r[8]), "=r"(r[9])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]),
-              "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]),
-              "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]));
-    }
-};
-
-// x = register-wise max(x, y) over one chunk of REGS registers; ORs into
-// `grew` the bits of x that took y's value and changed.
+// x = register-wise max(x, y) over one chunk of REGS byte registers; ORs into
+// `grew` the bits of x that changed.
 template <int REGS>
-__device__ __forceinline__ void merge_chunk(uint32_t (&x)[(REGS * 5 + 31) / 32],
-                                            const uint32_t (&y)[(REGS * 5 + 31) / 32],
+__device__ __forceinline__ void merge_chunk(uint32_t (&x)[REGS / 4], const uint32_t (&y)[REGS / 4],
                                             uint32_t& grew) {
-    constexpr int NW = (REGS * 5 + 31) / 32;
-    uint32_t a[NW], b[NW], z[NW];
 #pragma unroll
-    for (int i = 0; i < NW; i++) {
-        const uint32_t H = mask_word(REGS, i, 4);
-        a[i] = y[i] | H;
-        b[i] = x[i] & ~H;
-    }
-    SubChain<NW>::run(z, a, b);
-#pragma unroll
-    for (int i = 0; i < NW; i++) {
-        const uint32_t H = mask_word(REGS, i, 4);
-        z[i] = ((z[i] | (y[i] ^ x[i])) ^ (y[i] | ~x[i])) & H;
-    }
-    uint32_t t[NW], l[NW], mk[NW];
-#pragma unroll
-    for (int i = 0; i < NW; i++) {
-        const uint32_t H = mask_word(REGS, i, 4);
-        const uint32_t sh = (i + 1 < NW) ? __funnelshift_r(z[i], z[i + 1 < NW ? i + 1 : i], 4)
-                                         : (z[i] >> 4);
-        t[i] = sh | H;
-        l[i] = mask_word(REGS, i, 0);
-    }
-    SubChain<NW>::run(mk, t, l);
-#pragma unroll
-    for (int i = 0; i < NW; i++) {
-        const uint32_t H = mask_word(REGS, i, 4);
-        const uint32_t m = (mk[i] | H) ^ z[i];
-        const uint32_t d = (x[i] ^ y[i]) & m;
-        grew |= d;
-        x[i] = x[i] ^ d;
+    for (int i = 0; i < REGS / 4; i++) {
+        const uint32_t keep = byte_signs((x[i] | 0x80808080u) - y[i]);
+        const uint32_t r = y[i] ^ ((x[i] ^ y[i]) & keep);
+        grew |= r ^ x[i];
+        x[i] = r;
     }
 }
 
 template <int REGS>
-__device__ __forceinline__ void merge_chunk(uint32_t (&x)[(REGS * 5 + 31) / 32],
-                                            const uint32_t (&y)[(REGS * 5 + 31) / 32]) {
+__device__ __forceinline__ void merge_chunk(uint32_t (&x)[REGS / 4], const uint32_t (&y)[REGS / 4]) {
     uint32_t unused = 0;
     merge_chunk<REGS>(x, y, unused);
 }
 
-template <int NW>
-struct AddChain;
-template <>
-struct AddChain<3> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[3], const uint32_t (&a)[3],
-                                               const uint32_t (&b)[3]) {
-        asm("add.cc.u32 %0, %3, %6;\n\t"
-            "addc.cc.u32 %1, %4, %7;\n\t"
-            "addc.u32 %2, %5, %8;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(b[0]), "r"(b[1]), "r"(b[2]));
-    }
-};
-template <>
-struct AddChain<5> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[5], const uint32_t (&a)[5],
-                                               const uint32_t (&b)[5]) {
-        asm("add.cc.u32 %0, %5, %10;\n\t"
-            "addc.cc.u32 %1, %6, %11;\n\t"
-            "addc.cc.u32 %2, %7, %12;\n\t"
-            "addc.cc.u32 %3, %8, %13;\n\t"
-            "addc.u32 %4, %9, %14;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(b[0]), "r"(b[1]),
-              "r"(b[2]), "r"(b[3]), "r"(b[4]));
-    }
-};
-template <>
-struct AddChain<10> {
-    static __device__ __forceinline__ void run(uint32_t (&r)[10], const uint32_t (&a)[10],
-                                               const uint32_t (&b)[10]) {
-        asm("add.cc.u32 %0, %10, %20;\n\t"
-            "addc.cc.u32 %1, %11, %21;\n\t"
-            "addc.cc.u32 %2, %12, %22;\n\t"
-            "addc.cc.u32 %3, %13, %23;\n\t"
-            "addc.cc.u32 %4, %14, %24;\n\t"
-            "addc.cc.u32 %5, %15, %25;\n\t"
-            "addc.cc.u32 %6, %16, %26;\n\t"
-            "addc.cc.u32 %7, %17, %27;\n\t"
-            "addc.cc.u32 %8, %18, %28;\n\t"
-            "addc.u32 %9, %19, %29;"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-              "=r"(r[7]), "=r"(r[8]), "=r"(r[9])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]),
-              "r"(a[7]), "r"(a[8]), "r"(a[9]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]),
-              "r"(b[4]), "r"(b[5]), "r"(b[6]), "r"(b[7]), "r"(b[8]), "r"(b[9]));
-    }
-};
+// Number of zero bytes of w (all bytes below 0x80): ((b | 0x80) - 1) keeps
+// bit 7 iff b != 0, and never borrows across bytes.
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t w) {
+    return 4u - __popc(((w | 0x80808080u) - 0x01010101u) & 0x80808080u);
+}
 
 // Partial count of one chunk: hsum += sum over registers of 2^(31-v),
 // zeroes += #(v == 0), and, only when `with31`, c31 += #(v == 31).
-//  * 2^(31-v): funnel-shifting 0x80000000 right by the raw extracted field
-//    uses the shift amount mod 32, so the unmasked field gives the term in
-//    one instruction.
-//  * zero registers, broadword: ((x & ~H) + low4) | x has bit 4 of a
-//    register set iff the register is non-zero (low4 = bits 0-3 of every
-//    register; the add never carries out of a register).
+// 2^(31-v): funnel-shifting 0x80000000 right uses the shift amount mod 32, so
+// the word shifted right by 8k gives register k's term without masking.
 template <int REGS>
-__device__ __forceinline__ void count_chunk(const uint32_t (&w)[(REGS * 5 + 31) / 32],
-                                            uint64_t& hsum, uint32_t& zeroes, uint32_t& c31,
-                                            bool with31) {
-    constexpr int NW = (REGS * 5 + 31) / 32;
+__device__ __forceinline__ void count_chunk(const uint32_t (&w)[REGS / 4], uint64_t& hsum,
+                                            uint32_t& zeroes, uint32_t& c31, bool with31) {
     uint32_t lo = 0, hi = 0;
 #pragma unroll
-    for (int k = 0; k < REGS; k++) {
-        const int p = 5 * k;
-        const int i = p / 32, s = p % 32;
-        const uint32_t raw =
-            (s + 5 <= 32) ? (w[i] >> s) : __funnelshift_r(w[i], w[(i + 1) < NW ? i + 1 : i], s);
-        const uint32_t term = __funnelshift_r(0x80000000u, 0u, raw);
-        asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, 0;" : "+r"(lo), "+r"(hi) : "r"(term));
+    for (int i = 0; i < REGS / 4; i++) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t term = __funnelshift_r(0x80000000u, 0u, w[i] >> (8 * k));
+            asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, 0;" : "+r"(lo), "+r"(hi) : "r"(term));
+        }
+        zeroes += zero_bytes(w[i]);
+        if (with31) c31 += zero_bytes(w[i] ^ 0x1f1f1f1fu);
     }
     hsum += ((uint64_t)hi << 32) | lo;
-    uint32_t t[NW], low4[NW], sum[NW];
-#pragma unroll
-    for (int i = 0; i < NW; i++) {
-        const uint32_t H = mask_word(REGS, i, 4);
-        low4[i] = mask_word(REGS, i, 0) | mask_word(REGS, i, 1) | mask_word(REGS, i, 2) |
-                  mask_word(REGS, i, 3);
-        t[i] = w[i] & ~H;
-    }
-    AddChain<NW>::run(sum, t, low4);
-    uint32_t nz = 0;
-#pragma unroll
-    for (int i = 0; i < NW; i++) nz += __popc((sum[i] | w[i]) & mask_word(REGS, i, 4));
-    zeroes += (uint32_t)REGS - nz;
-    if (with31) {
-#pragma unroll
-        for (int k = 0; k < REGS; k++) {
-            const int p = 5 * k;
-            const int i = p / 32, s = p % 32;
-            const uint32_t raw = (s + 5 <= 32) ? (w[i] >> s)
-                                               : __funnelshift_r(w[i], w[(i + 1) < NW ? i + 1 : i], s);
-            c31 += ((raw & 31u) == 31u);
-        }
-    }
 }
 
 // HLL:181-185 from the exact integer harmonic sum (reference arithmetic, f64
@@ -307,26 +159,15 @@ template <int LOG2M>
 __device__ __forceinline__ void load_chunk(const uint8_t* __restrict__ base, uint64_t node, int c,
                                            uint32_t (&w)[Geo<LOG2M>::NW]) {
     using G = Geo<LOG2M>;
-    const uint8_t* p = base + node * (uint64_t)G::COUNTER_BYTES + (uint64_t)c * G::CHUNK_BYTES;
-    if constexpr (G::CHUNK_BYTES == 40) {
-        const uint2* q = reinterpret_cast<const uint2*>(p);
+    const uint4* q = reinterpret_cast<const uint4*>(base + node * (uint64_t)G::COUNTER_BYTES +
+                                                    (uint64_t)c * G::CHUNK_BYTES);
 #pragma unroll
-        for (int i = 0; i < 5; i++) {
-            const uint2 t = __ldg(q + i);
-            w[2 * i] = t.x;
-            w[2 * i + 1] = t.y;
-        }
-    } else if constexpr (G::CHUNK_BYTES == 20) {
-        const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
-#pragma unroll
-        for (int i = 0; i < 5; i++) w[i] = __ldg(q + i);
-    } else {
-        const uint16_t* q = reinterpret_cast<const uint16_t*>(p);
-        const uint32_t h0 = __ldg(q), h1 = __ldg(q + 1), h2 = __ldg(q + 2), h3 = __ldg(q + 3),
-                       h4 = __ldg(q + 4);
-        w[0] = h0 | (h1 << 16);
-        w[1] = h2 | (h3 << 16);
-        w[2] = h4;
+    for (int i = 0; i < G::NW / 4; i++) {
+        const uint4 t = __ldg(q + i);
+        w[4 * i] = t.x;
+        w[4 * i + 1] = t.y;
+        w[4 * i + 2] = t.z;
+        w[4 * i + 3] = t.w;
     }
 }
 
@@ -334,23 +175,11 @@ template <int LOG2M>
 __device__ __forceinline__ void store_chunk(uint8_t* __restrict__ base, uint64_t node, int c,
                                             const uint32_t (&w)[Geo<LOG2M>::NW]) {
     using G = Geo<LOG2M>;
-    uint8_t* p = base + node * (uint64_t)G::COUNTER_BYTES + (uint64_t)c * G::CHUNK_BYTES;
-    if constexpr (G::CHUNK_BYTES == 40) {
-        uint2* q = reinterpret_cast<uint2*>(p);
+    uint4* q = reinterpret_cast<uint4*>(base + node * (uint64_t)G::COUNTER_BYTES +
+                                        (uint64_t)c * G::CHUNK_BYTES);
 #pragma unroll
-        for (int i = 0; i < 5; i++) q[i] = make_uint2(w[2 * i], w[2 * i + 1]);
-    } else if constexpr (G::CHUNK_BYTES == 20) {
-        uint32_t* q = reinterpret_cast<uint32_t*>(p);
-#pragma unroll
-        for (int i = 0; i < 5; i++) q[i] = w[i];
-    } else {
-        uint16_t* q = reinterpret_cast<uint16_t*>(p);
-        q[0] = (uint16_t)w[0];
-        q[1] = (uint16_t)(w[0] >> 16);
-        q[2] = (uint16_t)w[1];
-        q[3] = (uint16_t)(w[1] >> 16);
-        q[4] = (uint16_t)w[2];
-    }
+    for (int i = 0; i < G::NW / 4; i++)
+        q[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
 }
 
 // ---------------------------------------------------------------------------

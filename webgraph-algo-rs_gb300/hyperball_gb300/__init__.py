@@ -127,6 +127,8 @@ class IterStats(ctypes.Structure):
         ("reserved", ctypes.c_int32),
         ("union_ms", ctypes.c_double),
         ("iteration_ms", ctypes.c_double),
+        ("scanned_arcs", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -177,6 +179,7 @@ EXPORTS = [
     ("hb_graph_get_view", GraphView, [_H]),
     ("hb_graph_free", None, [_H]),
     ("hb_version", ctypes.c_char_p, []),
+    ("hb_kernel_launches", ctypes.c_uint64, [_H]),
 ]
 
 _lib = None
@@ -298,6 +301,24 @@ class Graph:
 
     def transpose(self):
         return Graph._make(load_library().hb_graph_transpose, self._h)
+
+
+class CsrView:
+    """A CSR graph in caller-owned host memory (for instance pinned buffers),
+    passed to hb_create without a copy into a library-owned Graph. The caller
+    keeps the buffers alive while a builder or HyperBall uses the view."""
+
+    def __init__(self, num_nodes, num_arcs, offsets_ptr, successors_ptr, owner=None):
+        self.num_nodes = int(num_nodes)
+        self.num_arcs = int(num_arcs)
+        self._off_ptr = int(offsets_ptr)
+        self._suc_ptr = int(successors_ptr)
+        self._owner = owner
+
+    def view(self):
+        return GraphView(self.num_nodes, self.num_arcs,
+                         ctypes.cast(self._off_ptr, _P(ctypes.c_uint64)),
+                         ctypes.cast(self._suc_ptr, _P(ctypes.c_uint32)))
 
 
 # ---------------------------------------------------------------------------
@@ -606,6 +627,10 @@ class HyperBall:
         v = ctypes.c_double()
         _check(self._lib.hb_reachable_nodes_from(self._h, node, ctypes.byref(v)), self._h)
         return v.value
+
+    def kernel_launches(self):
+        """CUDA kernels the library launched for this instance so far."""
+        return int(self._lib.hb_kernel_launches(self._h))
 
     def registers(self, which=HB_CURRENT_STATE):
         """Raw counter bytes (num_nodes x counter_bytes), reference layout."""
