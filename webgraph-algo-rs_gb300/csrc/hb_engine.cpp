@@ -95,6 +95,9 @@ struct hb_handle {
     uint32_t* d_tiles = nullptr;  // window boundaries
     uint64_t n_tiles = 0;         // number of windows
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
+    uint32_t* d_indeg = nullptr;    // in-degree without self-loops
+    uint64_t self_loops = 0;
+    uint64_t pending_visited = 0;   // arcs the next iteration visits
     uint32_t* d_perm = nullptr;     // device node -> caller node
     uint32_t* d_inv = nullptr;      // caller node -> device node
     std::vector<uint32_t> inv_host;
@@ -111,12 +114,12 @@ struct hb_handle {
     uint64_t n_heavy = 0;
     hbk::TilePartial* d_partials = nullptr;  // one per tile, then one per heavy block
     uint64_t n_partials = 0;
-    hbk::TilePartial* d_partial_scratch = nullptr;
-    hbk::TilePartial* d_partial_out = nullptr;
+    double* d_nf_items = nullptr;     // neighbourhood-function part per work item / heavy node
+    double* d_nf_scratch = nullptr;
     unsigned long long* d_cursor = nullptr;  // chunk cursor of the union kernel
     int* d_any31 = nullptr;
     bool any31 = false;
-    int grid_tile = 1, grid_heavy = 1, grid_mark = 1, grid_fin = 1;
+    int grid_tile = 1, grid_heavy = 1, grid_mark = 1;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // reference state (IterationContext + HyperBall fields)
@@ -435,6 +438,9 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.list_counts = nullptr;
     a.chunks = h->d_chunks;
     a.gather_all = 0;
+    a.indeg = h->d_indeg;
+    a.nf_items = h->d_nf_items;
+    a.heavy_item_base = h->n_chunks;
     a.n_chunks = h->n_chunks;
     a.tile_max_degree = h->medium_max;
     a.acc_slot = (uint32_t)(h->n_partials - 1);
@@ -458,6 +464,8 @@ int do_init(hb_handle* h) {
     h->cur = 0;
     h->mod_cur = 0;
     h->mbc_cur = 2;
+    // every counter is modified at init, so iteration 1 visits every non-loop arc
+    h->pending_visited = h->m - h->self_loops;
     hbk::InitArgs ia{};
     ia.perm = h->d_perm;
     ia.curr = h->d_cnt[0];
@@ -527,6 +535,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         }
     }
     HB_CUDA(h, cudaMemsetAsync(h->d_partials, 0, h->n_partials * sizeof(hbk::TilePartial), s));
+    HB_CUDA(h, cudaMemsetAsync(h->d_nf_items, 0, (h->n_chunks + h->n_heavy) * sizeof(double), s));
     HB_CUDA(h, cudaMemsetAsync(h->d_cursor, 0, sizeof(unsigned long long), s));
     hbk::UnionArgs a = union_args(h);
     // nearly every counter changed in the previous iteration: merge all
@@ -550,14 +559,14 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, a, h->grid_heavy, s));
     }
     HB_CUDA(h, cudaEventRecord(h->ev[2], s));
-    if (n) HB_LAUNCH(h, hbk::launch_finalize(h->log2m, a, h->grid_fin, s));
     if (h->systolic)
         HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
                                             h->d_bits[h->mbc_cur ^ 1], n, h->grid_mark, s));
-    HB_LAUNCH(h, hbk::launch_reduce_partials(h->d_partials, h->n_partials, h->d_partial_scratch,
-                                             h->d_partial_out, s));
+    // the neighbourhood-function parts, in a fixed order, into partials[0].nf
+    HB_LAUNCH(h, hbk::launch_sum_f64(h->d_nf_items, h->n_chunks + h->n_heavy, h->d_nf_scratch,
+                                     &h->d_partials[0].nf, s));
     hbk::TilePartial tot{};
-    HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partial_out, sizeof(tot), cudaMemcpyDeviceToHost, s));
+    HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partials, sizeof(tot), cudaMemcpyDeviceToHost, s));
     HB_CUDA(h, cudaEventRecord(h->ev[3], s));
     HB_CUDA(h, cudaStreamSynchronize(s));
     struct {
@@ -571,6 +580,9 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     if (h->systolic) h->mbc_cur ^= 1;
 
     h->modified_counters = host.st[1];
+    // arcs visited in this iteration were fixed by the previous one
+    const uint64_t visited = h->pending_visited;
+    h->pending_visited = host.st[0];
     current_nf += host.nf;
     h->last = current_nf;
     const double last_output = h->nf.back();
@@ -582,7 +594,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     hb_iter_stats st{};
     st.iteration = h->iteration;
     st.modified_counters = host.st[1];
-    st.visited_arcs = host.st[0];
+    st.visited_arcs = visited;
     st.scanned_nodes = host.st[2];
     st.neighborhood_function = current_nf;
     st.relative_increment = h->relative_increment;
@@ -802,6 +814,24 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         dfree(hp, off0);
         dfree(hp, succ0);
     }
+    {
+        unsigned long long* loops = nullptr;
+        if ((r = dalloc(hp, &h->d_indeg, h->n))) return fail(r);
+        if ((r = dalloc(hp, &loops, 1))) return fail(r);
+        if ((r = cuda_err(hp, cudaMemsetAsync(h->d_indeg, 0, h->n * 4, h->stream), "cudaMemsetAsync")))
+            return fail(r);
+        if ((r = cuda_err(hp, cudaMemsetAsync(loops, 0, 8, h->stream), "cudaMemsetAsync"))) return fail(r);
+        if (h->n && (r = cuda_err(hp, (cudaError_t)hbk::launch_indeg_noloop(h->d_off, h->d_succ, h->n,
+                                                                         h->d_indeg, loops, h->stream),
+                                  "launch_indeg_noloop")))
+            return fail(r);
+        unsigned long long nl = 0;
+        if ((r = cuda_err(hp, cudaMemcpyAsync(&nl, loops, 8, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy")))
+            return fail(r);
+        if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
+        h->self_loops = nl;
+        dfree(hp, loops);
+    }
     if (transpose) {
         uint64_t* off0 = nullptr;
         uint32_t* succ0 = nullptr;
@@ -847,17 +877,12 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
     h->grid_heavy = hbk::heavy_grid(h->log2m, h->device);
     if ((uint64_t)h->grid_heavy > h->n_heavy + 1) h->grid_heavy = (int)(h->n_heavy + 1);
     h->grid_mark = 8 * hbk::num_sms(h->device);
-    h->grid_fin = hbk::finalize_grid(h->log2m, h->device);
-    {
-        const uint64_t need = (n + 255) / 256 + 1;
-        if ((uint64_t)h->grid_fin > need) h->grid_fin = (int)need;
-    }
-    // partial slots: one per finalize block (neighbourhood function), then one
-    // accumulating the union kernels' integer totals
-    h->n_partials = (uint64_t)h->grid_fin + 1;
+    // integer totals of the union kernels (atomics) and the summed
+    // neighbourhood function
+    h->n_partials = 1;
     if ((r = dalloc(hp, &h->d_partials, h->n_partials))) return fail(r);
-    if ((r = dalloc(hp, &h->d_partial_scratch, 256))) return fail(r);
-    if ((r = dalloc(hp, &h->d_partial_out, 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_nf_items, h->n_chunks + h->n_heavy + 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_nf_scratch, 256))) return fail(r);
     if ((r = dalloc(hp, &h->d_any31, 1))) return fail(r);
     if ((r = dalloc(hp, &h->d_cursor, 1))) return fail(r);
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);

@@ -37,7 +37,7 @@ constexpr int MAX_DISCOUNT = 8;
 // iteration; summed in a fixed order after the union kernels.
 struct TilePartial {
     double nf;                    // neighbourhood-function contribution
-    unsigned long long vis;       // visited arcs
+    unsigned long long vis;       // arcs the next iteration visits (k_finalize)
     unsigned long long mod;       // modified counters
     unsigned long long scanned;   // scanned nodes
     unsigned long long sarcs;     // arcs of the scanned nodes
@@ -80,6 +80,9 @@ struct UnionArgs {
     const uint64_t* list_counts;
     const uint2* chunks;      // {first node, count | medium << 31}, in node order
     int gather_all;           // merge every successor (nearly all changed before)
+    const uint32_t* indeg;    // in-degree without self-loops
+    double* nf_items;         // neighbourhood-function part of each work item, then of each heavy node
+    uint64_t heavy_item_base; // index of the first heavy node's part
     uint64_t n_chunks;
     unsigned long long* cursor; // next chunk to take (zero at launch)
     uint32_t tile_max_degree; // nodes above this out-degree are listed as heavy
@@ -108,6 +111,9 @@ int launch_init(int log2m, const InitArgs& a, void* stream);
 // in caller node order (inv: caller node -> device node)
 int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uint8_t* dst,
                          uint64_t n, void* stream);
+// in-degree without self-loops (indeg zeroed by the caller); *loops += self-loops
+int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
+                        unsigned long long* loops, void* stream);
 // renumbering: deg[i] = out-degree of perm[i] (deg[n] = 0)
 int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
                        unsigned long long* deg, void* stream);
@@ -126,10 +132,8 @@ int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);
 // heavy nodes, one CTA each
 int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream);
 int heavy_grid(int log2m, int device);
-// counts, neighbourhood function and per-node sums of the changed nodes;
-// writes partials[0 .. grid)
-int launch_finalize(int log2m, const UnionArgs& a, int grid, void* stream);
-int finalize_grid(int log2m, int device);
+// fixed-order sum of count doubles into *out (scratch: 256 doubles)
+int launch_sum_f64(const double* in, uint64_t count, double* scratch, double* out, void* stream);
 // systolic work lists: every light / medium node set in mbc | curr_mod, in
 // node order (win_medium[w], win_light[w]: first medium / light node of
 // window w). cnt and off hold nwords + 1 words; off[nwords] gets the counts

@@ -5,21 +5,21 @@
 //   1. k_list_count,     — systolic iterations only: the light and medium
 //      k_list_fill         nodes to check or to copy, in node order;
 //   2. k_union_window    — one warp per chunk of nodes, chunks taken in node
-//                          order from a global cursor; every node of out-degree up to
-//                          tile_max_degree: merge of the modified successors'
-//                          counters, modified test, next-state store;
-//   3. k_union_heavy     — the remaining (heavy) nodes, one CTA per node;
-//   4. k_finalize        — warp per word of the new modified bitmap: exact
-//                          count of every changed counter, neighbourhood-
-//                          function contribution, per-node f64 sums;
+//                          order from a global cursor; every node of
+//                          out-degree up to tile_max_degree: merge of the
+//                          successors' counters, modified test, next-state
+//                          store, and for changed counters the exact count,
+//                          neighbourhood-function part and per-node f64 sums
+//                          (finish_node) while the counter is in registers;
+//   3. k_union_heavy     — the same for the heavy nodes, one CTA per node;
+//   4. k_sum_f64         — the neighbourhood-function parts summed in a fixed
+//                          order (reproducible);
 //   5. k_mark_preds      — systolic iterations: predecessors of modified nodes
-//                          (through the transpose) into next-must-be-checked;
-//   6. k_reduce_partials — per-block partials (neighbourhood function, visited
-//                          arcs, modified and scanned nodes) summed in a fixed
-//                          order.
+//                          (through the transpose) into next-must-be-checked.
 // Only successors flagged in the previous iteration's modified bitmap are
-// merged (HB:1038). The count of an unchanged counter is the cached estimate
-// of the previous iteration, so k_finalize touches changed nodes only.
+// merged (HB:1038), or all of them where that gives the same counters. The
+// count of an unchanged counter is the cached estimate of the previous
+// iteration, so only changed counters are counted.
 //
 // GB300's f64 pipe issues 2 lane-operations per cycle per SM (1/64 of fp32),
 // so the epilogue keeps f64 instructions to the reference's own operations:
@@ -81,7 +81,7 @@ __device__ __forceinline__ void publish(double nf, unsigned long long vis, unsig
 // ---------------------------------------------------------------------------
 // end of a node's union, run by the G lanes (one per chunk) of a team: store
 // the merged counter into the next state; true when it differs from the
-// previous one (HB:1052). Counting is left to k_finalize.
+// previous one (HB:1052).
 // ---------------------------------------------------------------------------
 template <int LOG2M>
 __device__ __forceinline__ bool commit_node(const UnionArgs& a, uint64_t v, int c,
@@ -100,40 +100,37 @@ __device__ __forceinline__ bool commit_node(const UnionArgs& a, uint64_t v, int 
 }
 
 // ---------------------------------------------------------------------------
-// k_finalize: the per-node arithmetic of HB:1052-1093 for every node whose
-// counter changed (and, in standard iterations, the count of every node for
-// the neighbourhood function). One warp per 32 consecutive nodes, so loads
-// are coalesced and all lanes run the f64 instructions together:
-//   post = count(next counter)  (exact integer harmonic sum, one division)
+// End of a node's union, for the nodes whose counter changed: the per-node
+// arithmetic of HB:1052-1093, run by the G lanes that hold the new counter
+// (lane c == 0 does the f64 part), while it is still in registers:
+//   post = count(new counter)   (exact integer harmonic sum, one division)
 //   pre  = cached count of the previous counter
-//   NF  += post (standard) or post - pre (systolic)
+//   NF  += post (standard) or post - pre (systolic); unchanged nodes add
+//          their cached count in standard iterations
 //   delta = post - pre; if delta > 0: sod += delta*(t+1), harm += delta/(t+1),
 //   discounted sums += delta*f(t+1)
-// Partial NF sums per block (fixed grid and assignment: reproducible).
+// and the in-degree of a changed node is added to the arcs the next
+// iteration visits.
 // ---------------------------------------------------------------------------
 template <int LOG2M>
-__global__ void __launch_bounds__(256) k_finalize(UnionArgs a) {
+__device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int c, unsigned gmask,
+                                            const uint32_t (&acc)[Geo<LOG2M>::NW], bool changed,
+                                            double& nf, unsigned long long& vis) {
     using Gm = Geo<LOG2M>;
-    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
-    const int lane = threadIdx.x & 31;
-    const uint64_t nwords = (a.n + 31) >> 5;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    double nf = 0.0;
-    for (uint64_t w = gw; w < nwords; w += nw) {
-        const uint32_t bits = __ldg(a.next_mod + w);
-        if (a.systolic && bits == 0u) continue;
-        const uint64_t v = (w << 5) + lane;
-        if (v >= a.n) continue;
-        if ((bits >> lane) & 1u) {
-            uint64_t hs = 0;
-            uint32_t z = 0, c31 = 0;
-#pragma unroll 1
-            for (int c = 0; c < G; c++) {
-                uint32_t x[NW];
-                load_chunk<LOG2M>(a.next, v, c, x);
-                count_chunk<REGS>(x, hs, z, c31, a.any31 != 0);
+    constexpr int G = Gm::CHUNKS, REGS = Gm::CHUNK_REGS;
+    if (changed) {
+        uint64_t hs = 0;
+        uint32_t z = 0, c31 = 0;
+        count_chunk<REGS>(acc, hs, z, c31, a.any31 != 0);
+        if constexpr (G > 1) {
+#pragma unroll
+            for (int off = 1; off < G; off <<= 1) {
+                hs += __shfl_xor_sync(gmask, hs, off);
+                z += __shfl_xor_sync(gmask, z, off);
+                c31 += __shfl_xor_sync(gmask, c31, off);
             }
+        }
+        if (c == 0) {
             const double pre = a.est[v];
             const double post = estimate_fast(signed_hsum(hs, c31, a.quirk), z, a.alpha_m_m,
                                               a.a_scaled, a.small_bits, (double)Gm::M, a.ln_table);
@@ -153,43 +150,18 @@ __global__ void __launch_bounds__(256) k_finalize(UnionArgs a) {
                 for (int k = 0; k < a.ndisc; k++)
                     a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, a.disc_factor[k]));
             }
-        } else if (!a.systolic) {
-            nf = __dadd_rn(nf, a.est[v]);
+            vis += __ldg(a.indeg + v);
         }
+    } else if (!a.systolic && c == 0) {
+        nf = __dadd_rn(nf, a.est[v]);
     }
-    publish(nf, 0, 0, 0, a.partials + blockIdx.x);
 }
 
-// Merges into acc (chunk c) the counters of the successors in [e, e1) of node v
-// that were modified in the previous iteration; `stride` arcs apart. Two
-// successors per step keep two counter gathers in flight per lane.
-template <int LOG2M>
-__device__ __forceinline__ void gather_successors(const UnionArgs& a, uint64_t v, int c,
-                                                  uint64_t e, uint64_t e1, uint64_t stride,
-                                                  uint32_t (&acc)[Geo<LOG2M>::NW],
-                                                  unsigned long long& vis) {
-    using Gm = Geo<LOG2M>;
-    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
-    for (; e + stride < e1; e += 2 * stride) {
-        const uint32_t sa = __ldg(a.succ + e), sb = __ldg(a.succ + e + stride);
-        const bool ma = sa != v && test_bit(a.curr_mod, sa);
-        const bool mb = sb != v && test_bit(a.curr_mod, sb);
-        uint32_t ya[NW], yb[NW];
-        if (ma) load_chunk<LOG2M>(a.curr, sa, c, ya);
-        if (mb) load_chunk<LOG2M>(a.curr, sb, c, yb);
-        if (ma) merge_chunk<REGS>(acc, ya);
-        if (mb) merge_chunk<REGS>(acc, yb);
-        vis += (unsigned long long)ma + (unsigned long long)mb;
-    }
-    if (e < e1) {
-        const uint32_t s = __ldg(a.succ + e);
-        if (s != v && test_bit(a.curr_mod, s)) {
-            uint32_t y[NW];
-            load_chunk<LOG2M>(a.curr, s, c, y);
-            merge_chunk<REGS>(acc, y);
-            vis++;
-        }
-    }
+// fixed-order warp sum (lane 0 gets it)
+__device__ __forceinline__ double warp_sum_f64(double x) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x = __dadd_rn(x, __shfl_xor_sync(0xffffffffu, x, off));
+    return x;
 }
 
 // ---------------------------------------------------------------------------
@@ -211,8 +183,7 @@ __device__ __forceinline__ void gather_successors(const UnionArgs& a, uint64_t v
 // so the warps in flight at any moment work on a narrow band of consecutive
 // node ids; with URL-order locality their successors cluster around that band
 // and its counters stay L2-resident while the band passes (a static
-// assignment lets warps drift apart and the band outgrows L2). Each warp
-// fetches its next chunk while it runs the current one. Systolic iterations
+// assignment lets warps drift apart and the band outgrows L2). Systolic iterations
 // walk node lists instead (k_list_fill): runs of the light list, then of the
 // medium list; list order is node order, so locality and the degree order
 // inside each kind survive. Neighbouring lanes walk successor lists of equal
@@ -220,13 +191,21 @@ __device__ __forceinline__ void gather_successors(const UnionArgs& a, uint64_t v
 // modified bits of the next PIPE successors load.
 //
 // In iterations where nearly every counter changed before (`gather_all`), a
-// successor's counter is merged without waiting for its modified bit: an
-// unmodified successor's counter is already contained in the node's own
-// (c_{t-1}(u) = c_{t-2}(u) <= c_{t-1}(v)), so merging it changes nothing, and
-// the bit is tested only to count visited arcs.
+// successor's counter is merged without its modified bit: an unmodified
+// successor's counter is already contained in the node's own
+// (c_{t-1}(u) = c_{t-2}(u) <= c_{t-1}(v)), and so is the node's own counter,
+// so merging them changes nothing and no dependent bitmap load stands before
+// the gather. Visited arcs are not counted per arc at all: every predecessor
+// of a node modified in t-1 is scanned in t, in every mode, so
+// visited_t = sum over u modified in t-1 of (in-degree of u without
+// self-loops), which finish_node accumulates for the next iteration.
 // ---------------------------------------------------------------------------
 constexpr int WINDOW = 1024;
-constexpr int PIPE = 4;
+// counter loads in flight per lane: 64 bytes, within the register budget of
+// three 256-thread blocks per SM (measured: more resident warps beat deeper
+// per-lane pipelines)
+template <int NW>
+__host__ __device__ constexpr int pipe_depth() { return NW >= 16 ? 1 : NW >= 8 ? 2 : 4; }
 
 template <int LOG2M>
 struct TileGeo {
@@ -235,56 +214,161 @@ struct TileGeo {
 };
 
 // Merges into acc (chunk c) the counters of the successors e0, e0+stride, ...
-// (< e1) of node v modified in the previous iteration (or of all of them when
-// `all`); returns how many modified non-loop successors there were.
+// (< e1) of node v: all of them, or (filter) only the non-loop ones modified
+// in the previous iteration. A rolling pipeline keeps PIPE counter loads in
+// flight per lane: slot k merges its counter, then reloads with the id that
+// was fetched one round earlier and fetches the id after it.
 template <int LOG2M>
-__device__ __forceinline__ uint32_t gather_pipelined(const UnionArgs& a, uint32_t v, int c,
-                                                     uint64_t e0, uint64_t e1, uint32_t stride,
-                                                     bool all, uint32_t (&acc)[Geo<LOG2M>::NW],
-                                                     uint32_t& grew) {
+__device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
+                                               uint64_t e1, uint32_t stride, bool filter,
+                                               uint32_t (&acc)[Geo<LOG2M>::NW]) {
     using Gm = Geo<LOG2M>;
-    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
-    uint32_t cnt = 0;
-    uint32_t s[PIPE];
-    bool ld[PIPE];
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIPE = pipe_depth<NW>();
+    uint32_t y[PIPE][NW];
+    bool have[PIPE];
+    uint32_t nid[PIPE];
 #pragma unroll
     for (int k = 0; k < PIPE; k++) {
         const uint64_t e = e0 + (uint64_t)k * stride;
-        s[k] = e < e1 ? __ldg(a.succ + e) : v;
+        const uint32_t sid = e < e1 ? __ldg(a.succ + e) : v;
+        const uint64_t en = e + (uint64_t)PIPE * stride;
+        nid[k] = en < e1 ? __ldg(a.succ + en) : v;
+        have[k] = e < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+        if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
     }
-#pragma unroll
-    for (int k = 0; k < PIPE; k++) {
-        const bool m = s[k] != v && test_bit(a.curr_mod, s[k]);
-        cnt += m;
-        ld[k] = all ? s[k] != v : m;
-    }
-    for (uint64_t e = e0; e < e1; e += (uint64_t)PIPE * stride) {
-        uint32_t y[PIPE][NW];
-#pragma unroll
-        for (int k = 0; k < PIPE; k++)
-            if (ld[k]) load_chunk<LOG2M>(a.curr, s[k], c, y[k]);
+    for (uint64_t e = e0 + (uint64_t)PIPE * stride; e < e1 + (uint64_t)PIPE * stride;
+         e += (uint64_t)PIPE * stride) {
 #pragma unroll
         for (int k = 0; k < PIPE; k++) {
-            const uint64_t en = e + (uint64_t)(PIPE + k) * stride;
-            const uint32_t ns = en < e1 ? __ldg(a.succ + en) : v;
-            if (ld[k]) merge_chunk<REGS>(acc, y[k], grew);
-            const bool m = ns != v && test_bit(a.curr_mod, ns);
-            cnt += m;
-            ld[k] = all ? ns != v : m;
-            s[k] = ns;
+            if (have[k]) merge_chunk<REGS>(acc, y[k]);
+            const uint64_t ek = e + (uint64_t)k * stride;
+            const uint32_t sid = nid[k];
+            const uint64_t en = ek + (uint64_t)PIPE * stride;
+            nid[k] = en < e1 ? __ldg(a.succ + en) : v;
+            have[k] = ek < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+            if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
         }
     }
-    return cnt;
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory ring for successor counters: every lane keeps RING counter
+// copies in flight with cp.async (16-byte pieces, cached in L1 as well), so
+// the gather depth per lane costs shared memory instead of registers and more
+// warps stay resident. Lane `lane`'s piece q of slot j sits at
+// ((j * PIECES + q) * 32 + lane) * 16 bytes of its warp's ring: the 32 lanes'
+// 16-byte accesses are contiguous, without bank conflicts.
+// ---------------------------------------------------------------------------
+constexpr int RING = 0;
+
+template <int LOG2M>
+struct RingGeo {
+    static constexpr int PIECES = Geo<LOG2M>::CHUNK_BYTES / 16;
+    static constexpr int WARP_BYTES = RING * PIECES * 32 * 16;
+};
+
+__device__ __forceinline__ void cp_async_16(uint32_t smem, const void* g) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// gather_rolling with the successor counters staged in the lane's ring slots
+template <int LOG2M>
+__device__ __forceinline__ void gather_ring(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
+                                            uint64_t e1, uint32_t stride, bool filter,
+                                            uint32_t (&acc)[Geo<LOG2M>::NW], uint32_t ring) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIECES = RingGeo<LOG2M>::PIECES;
+    const uint32_t lane16 = (threadIdx.x & 31) * 16;
+    auto issue = [&](int j, uint32_t s) {
+        const uint8_t* src =
+            a.curr + (uint64_t)s * Gm::COUNTER_BYTES + (uint64_t)c * Gm::CHUNK_BYTES;
+#pragma unroll
+        for (int q = 0; q < PIECES; q++)
+            cp_async_16(ring + (uint32_t)((j * PIECES + q) * 512) + lane16, src + 16 * q);
+    };
+    uint32_t have = 0;
+    uint32_t ids[RING];
+#pragma unroll
+    for (int j = 0; j < RING; j++) {
+        const uint64_t e = e0 + (uint64_t)j * stride;
+        ids[j] = e < e1 ? __ldg(a.succ + e) : v;
+    }
+#pragma unroll
+    for (int j = 0; j < RING; j++) {
+        const uint64_t e = e0 + (uint64_t)j * stride;
+        const bool ok = e < e1 && (!filter || (ids[j] != v && test_bit(a.curr_mod, ids[j])));
+        if (ok) issue(j, ids[j]);
+        have |= (uint32_t)ok << j;
+        cp_async_commit();
+    }
+    uint64_t pos = e0 + (uint64_t)RING * stride;
+    uint32_t nid = pos < e1 ? __ldg(a.succ + pos) : v;
+    for (uint64_t base = e0; base < e1; base += (uint64_t)RING * stride) {
+#pragma unroll
+        for (int j = 0; j < RING; j++) {
+            cp_async_wait<RING - 1>();
+            if ((have >> j) & 1u) {
+                uint32_t y[NW];
+#pragma unroll
+                for (int q = 0; q < PIECES; q++) {
+                    uint32_t t0, t1, t2, t3;
+                    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                                 : "=r"(t0), "=r"(t1), "=r"(t2), "=r"(t3)
+                                 : "r"(ring + (uint32_t)((j * PIECES + q) * 512) + lane16));
+                    y[4 * q] = t0;
+                    y[4 * q + 1] = t1;
+                    y[4 * q + 2] = t2;
+                    y[4 * q + 3] = t3;
+                }
+                merge_chunk<REGS>(acc, y);
+            }
+            const bool ok = pos < e1 && (!filter || (nid != v && test_bit(a.curr_mod, nid)));
+            if (ok) issue(j, nid);
+            have = (have & ~(1u << j)) | ((uint32_t)ok << j);
+            cp_async_commit();
+            pos += stride;
+            nid = pos < e1 ? __ldg(a.succ + pos) : v;
+        }
+    }
+}
+
+// true when chunk c of counter v in `base` differs from w (read 32 bytes at a
+// time, so few registers are live)
+template <int LOG2M>
+__device__ __forceinline__ bool differs_from(const uint8_t* __restrict__ base, uint64_t v, int c,
+                                             const uint32_t (&w)[Geo<LOG2M>::NW]) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW;
+    const uint8_t* p = base + v * (uint64_t)Gm::COUNTER_BYTES + (uint64_t)c * Gm::CHUNK_BYTES;
+    uint32_t diff = 0;
+    if constexpr (NW >= 8) {
+#pragma unroll
+        for (int i = 0; i < NW / 8; i++) {
+            uint32_t x[8];
+            ld_nc_256(p + 32 * i, x);
+#pragma unroll
+            for (int k = 0; k < 8; k++) diff |= x[k] ^ w[8 * i + k];
+        }
+    } else {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
+        diff = (t.x ^ w[0]) | (t.y ^ w[1]) | (t.z ^ w[2]) | (t.w ^ w[3]);
+    }
+    return diff != 0u;
 }
 
 // One warp-step over up to 32/TB nodes: the consecutive nodes [b, e), or
-// list[b .. e) when a list is given. Scan, copy or nothing; returns through the
-// accumulators; sets the modified bits.
+// list[b .. e) when a list is given. Scan, copy or nothing; sets the modified
+// bits and counts scanned nodes, their arcs and the changed counters.
 template <int LOG2M, int TB>
 __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
-                                          uint32_t b, uint32_t e,
-                                          unsigned long long& vis, unsigned long long& modc,
-                                          unsigned long long& scanned, unsigned long long& sarcs) {
+                                          uint32_t b, uint32_t e, unsigned long long& modc,
+                                          unsigned long long& scanned, unsigned long long& sarcs,
+                                          unsigned long long& vis, double& nf, uint32_t ring) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
     constexpr int PB = TB / G;   // arc lanes per node
@@ -293,6 +377,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
     const int slot = lane / TB, tl = lane % TB, p = tl / G, c = tl % G;
     const unsigned tmask = TB == 32 ? 0xffffffffu : (((1u << TB) - 1u) << (slot * TB));
     const unsigned lmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * TB));
+    const bool filter = !a.gather_all;
     for (uint32_t base = b; base < e; base += NPW) {
         const uint32_t idx = base + slot;
         const uint32_t v = list ? (idx < e ? __ldg(list + idx) : 0u) : idx;
@@ -313,8 +398,10 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
 #pragma unroll
                 for (int k = 0; k < NW; k++) acc[k] = 0u;
             }
-            uint32_t grew = 0;
-            uint32_t w = gather_pipelined<LOG2M>(a, v, c, s0 + p, s1, PB, a.gather_all != 0, acc, grew);
+            if constexpr (RING > 0)
+                gather_ring<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc, ring);
+            else
+                gather_rolling<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc);
             if constexpr (PB > 1) {
                 __syncwarp(tmask);
 #pragma unroll
@@ -324,27 +411,17 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                     for (int k = 0; k < NW; k++) y[k] = __shfl_xor_sync(tmask, acc[k], off);
                     merge_chunk<REGS>(acc, y);
                 }
-                if (c != 0) w = 0;
-#pragma unroll
-                for (int off = G; off < TB; off <<= 1) w += __shfl_xor_sync(tmask, w, off);
-                if (p == 0) {
-                    // partial counters started empty: compare with the previous counter
-                    uint32_t prev[NW];
-                    load_chunk<LOG2M>(a.curr, v, c, prev);
-                    grew = 0;
-#pragma unroll
-                    for (int k = 0; k < NW; k++) grew |= prev[k] ^ acc[k];
-                }
             }
             if (p == 0) {
-                changed = grew != 0u;
+                // the previous counter, read again (L1/L2) rather than kept in registers
+                changed = differs_from<LOG2M>(a.curr, v, c, acc);
                 if constexpr (G > 1) changed = __any_sync(lmask, changed);
                 store_chunk<LOG2M>(a.next, v, c, acc);
                 if (c == 0) {
                     scanned++;
                     sarcs += s1 - s0;
-                    vis += w;
                 }
+                finish_node<LOG2M>(a, v, c, lmask, acc, changed, nf, vis);
             }
         } else if (copy && p == 0) {
             uint32_t w[NW];
@@ -401,52 +478,58 @@ __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
 }
 
 template <int LOG2M>
-__global__ void __launch_bounds__(256, 2) k_union_window(UnionArgs a) {
+__global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
     constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
     const int lane = threadIdx.x & 31;
+    extern __shared__ __align__(16) uint8_t ring_smem[];
+    const uint32_t ring = (uint32_t)__cvta_generic_to_shared(ring_smem) +
+                          (threadIdx.x >> 5) * (uint32_t)RingGeo<LOG2M>::WARP_BYTES;
     constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
-    unsigned long long vis = 0, modc = 0, scanned = 0, sarcs = 0;
+    unsigned long long modc = 0, scanned = 0, sarcs = 0, vis = 0;
     const WorkItems wi = work_items<NPW_L, NPW_M>(a);
     const uint64_t n_work = wi.n_work;
-    // two-deep pipeline of work items: the descriptor of the next chunk and
-    // the cursor value of the one after load while the current chunk runs
-    unsigned long long k0 = 0, k1 = 0;
-    if (lane == 0) {
-        k0 = atomicAdd(a.cursor, 1ull);
-        k1 = atomicAdd(a.cursor, 1ull);
-    }
-    k0 = __shfl_sync(0xffffffffu, k0, 0);
-    k1 = __shfl_sync(0xffffffffu, k1, 0);
-    uint2 d0 = item_at<NPW_L, NPW_M>(a, wi, k0);
-    while (k0 < n_work) {
-        const uint2 d1 = item_at<NPW_L, NPW_M>(a, wi, k1);
-        unsigned long long k2 = 0;
-        if (lane == 0 && k1 < n_work) k2 = atomicAdd(a.cursor, 1ull);
-        const uint32_t cnt = d0.y & 0x7fffffffu;
-        if (d0.y >> 31)
-            run_nodes<LOG2M, TB_MED>(a, a.medium_list, d0.x, d0.x + cnt, vis, modc, scanned, sarcs);
+    // Work items come GRAB at a time from the cursor (one atomic per GRAB
+    // chunks; measured fastest at 1). Handing out consecutive items keeps the
+    // band of nodes in flight narrow.
+    constexpr unsigned GRAB = 1;
+    unsigned long long k = 0, kend = 0;
+    for (;;) {
+        if (k == kend) {
+            unsigned long long first = 0;
+            if (lane == 0) first = atomicAdd(a.cursor, (unsigned long long)GRAB);
+            k = __shfl_sync(0xffffffffu, first, 0);
+            kend = k + GRAB;
+        }
+        if (k >= n_work) break;
+        const uint2 d = item_at<NPW_L, NPW_M>(a, wi, k);
+        k++;
+        const uint32_t cnt = d.y & 0x7fffffffu;
+        double nf = 0.0;
+        if (d.y >> 31)
+            run_nodes<LOG2M, TB_MED>(a, a.medium_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf,
+                                     ring);
         else
-            run_nodes<LOG2M, G>(a, a.light_list, d0.x, d0.x + cnt, vis, modc, scanned, sarcs);
-        k0 = k1;
-        d0 = d1;
-        k1 = k1 < n_work ? __shfl_sync(0xffffffffu, k2, 0) : k1;
+            run_nodes<LOG2M, G>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, ring);
+        // the item's neighbourhood-function part: fixed lanes, fixed order
+        nf = warp_sum_f64(nf);
+        if (lane == 0) a.nf_items[k - 1] = nf;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        vis += __shfl_xor_sync(0xffffffffu, vis, off);
         modc += __shfl_xor_sync(0xffffffffu, modc, off);
         scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
         sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
     }
     if (lane == 0) {
         // integer totals are order independent
         TilePartial* t = a.partials + a.acc_slot;
-        if (vis) atomicAdd(&t->vis, vis);
         if (modc) atomicAdd(&t->mod, modc);
         if (scanned) atomicAdd(&t->scanned, scanned);
         if (sarcs) atomicAdd(&t->sarcs, sarcs);
+        if (vis) atomicAdd(&t->vis, vis);
     }
 }
 
@@ -465,8 +548,9 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     const int tid = threadIdx.x;
     const int p = tid / G, c = tid % G;
     const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
-    unsigned long long vis = 0, modc = 0, scanned = 0, sarcs = 0;
+    unsigned long long modc = 0, scanned = 0, sarcs = 0, vis = 0;
     for (uint64_t idx = blockIdx.x; idx < a.list_len; idx += gridDim.x) {
+        double nf = 0.0;
         const uint64_t v = __ldg(a.list + idx);
         const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
         const bool scan = !a.systolic || test_bit(a.mbc, v);
@@ -480,9 +564,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
 #pragma unroll
                 for (int i = 0; i < NW; i++) acc[i] = prev[i] = 0u;
             }
-            unsigned long long my_vis = 0;
-            gather_successors<LOG2M>(a, v, c, s0 + p, s1, P, acc, my_vis);
-            if (c == 0) vis += my_vis;
+            gather_rolling<LOG2M>(a, (uint32_t)v, c, s0 + p, s1, P, !a.gather_all, acc);
             __syncwarp();
 #pragma unroll
             for (int off = G; off < 32; off <<= 1) {
@@ -512,6 +594,8 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                         modc++;
                     }
                 }
+                finish_node<LOG2M>(a, (uint32_t)v, c, leader_mask, acc, changed, nf, vis);
+                if (c == 0) a.nf_items[a.heavy_item_base + idx] = nf;
             }
         } else if (test_bit(a.curr_mod, v)) {
             if (tid < G) {
@@ -524,18 +608,18 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        vis += __shfl_xor_sync(0xffffffffu, vis, off);
         modc += __shfl_xor_sync(0xffffffffu, modc, off);
         scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
         sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
     }
     if (lane == 0) {
         // integer totals are order independent
         TilePartial* t = a.partials + a.acc_slot;
-        if (vis) atomicAdd(&t->vis, vis);
         if (modc) atomicAdd(&t->mod, modc);
         if (scanned) atomicAdd(&t->scanned, scanned);
         if (sarcs) atomicAdd(&t->sarcs, sarcs);
+        if (vis) atomicAdd(&t->vis, vis);
     }
 }
 
@@ -625,6 +709,48 @@ __global__ void __launch_bounds__(256) k_pack_counters(const uint8_t* __restrict
 #pragma unroll
         for (int k = 0; k < 5; k++) o[k] = (uint8_t)(bits >> (8 * k));
     }
+}
+
+// ---------------------------------------------------------------------------
+// in-degree without self-loops (visited-arc accounting), and the number of
+// self-loops; one warp per node
+// ---------------------------------------------------------------------------
+__global__ void k_indeg_noloop(const uint64_t* __restrict__ off, const uint32_t* __restrict__ succ,
+                               uint64_t n, uint32_t* __restrict__ indeg,
+                               unsigned long long* __restrict__ loops) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long nl = 0;
+    for (uint64_t v = gw; v < n; v += nw) {
+        const uint64_t s0 = __ldg(off + v), s1 = __ldg(off + v + 1);
+        for (uint64_t e = s0 + lane; e < s1; e += 32) {
+            const uint32_t s = __ldg(succ + e);
+            if (s == (uint32_t)v)
+                nl++;
+            else
+                atomicAdd(indeg + s, 1u);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) nl += __shfl_xor_sync(0xffffffffu, nl, o);
+    if (lane == 0 && nl) atomicAdd(loops, nl);
+}
+
+// fixed-order sum of doubles: block b sums its contiguous range (strided by
+// thread, then a tree); a second launch sums the block results the same way
+__global__ void k_sum_f64(const double* __restrict__ in, uint64_t count, double* __restrict__ out) {
+    __shared__ double s[256];
+    const uint64_t per = (count + gridDim.x - 1) / gridDim.x;
+    const uint64_t b = (uint64_t)blockIdx.x * per, e = min(count, b + per);
+    double x = 0.0;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) x = __dadd_rn(x, in[i]);
+    s[threadIdx.x] = x;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] = __dadd_rn(s[threadIdx.x], s[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = s[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -916,9 +1042,15 @@ static int pack_impl(const uint8_t* src, const uint32_t* inv, uint8_t* dst, uint
 }
 
 template <int LOG2M>
+static int ring_bytes() { return RING > 0 ? 8 * RingGeo<LOG2M>::WARP_BYTES : 0; }
+
+template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    static const cudaError_t attr = cudaFuncSetAttribute(
+        k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize, ring_bytes<LOG2M>());
+    if (attr != cudaSuccess) return (int)attr;
     ++t_launches;
-    k_union_window<LOG2M><<<grid, 256, 0, s>>>(a);
+    k_union_window<LOG2M><<<grid, 256, ring_bytes<LOG2M>(), s>>>(a);
     return (int)cudaGetLastError();
 }
 
@@ -929,36 +1061,16 @@ static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     return (int)cudaGetLastError();
 }
 
-template <int LOG2M>
-static int finalize_impl(const UnionArgs& a, int grid, cudaStream_t s) {
-    ++t_launches;
-    k_finalize<LOG2M><<<grid, 256, 0, s>>>(a);
-    return (int)cudaGetLastError();
-}
 
-template <int LOG2M>
-static int finalize_grid_impl(int device) {
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_finalize<LOG2M>, 256, 0);
-    return std::max(1, per_sm) * num_sms(device);
-}
 
-int launch_finalize(int log2m, const UnionArgs& a, int grid, void* stream) {
-#define CALL(L) finalize_impl<L>(a, grid, (cudaStream_t)stream)
-    HB_DISPATCH_LOG2M(log2m, CALL)
-#undef CALL
-}
-
-int finalize_grid(int log2m, int device) {
-#define CALL(L) finalize_grid_impl<L>(device)
-    HB_DISPATCH_LOG2M(log2m, CALL)
-#undef CALL
-}
 
 template <int LOG2M>
 static int tile_grid_impl(int device) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M>, 256, 0);
+    cudaFuncSetAttribute(k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         ring_bytes<LOG2M>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M>, 256,
+                                                  ring_bytes<LOG2M>());
     return std::max(1, per_sm) * num_sms(device);
 }
 
@@ -987,6 +1099,23 @@ int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uin
 #define CALL(L) pack_impl<L>(src, inv, dst, n, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
+}
+
+int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
+                        unsigned long long* loops, void* stream) {
+    const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256 + 1, 16384);
+    ++t_launches;
+    k_indeg_noloop<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, indeg, loops);
+    return (int)cudaGetLastError();
+}
+
+int launch_sum_f64(const double* in, uint64_t count, double* scratch, double* out, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    ++t_launches;
+    k_sum_f64<<<REDUCE_BLOCKS, 256, 0, s>>>(in, count, scratch);
+    ++t_launches;
+    k_sum_f64<<<1, 256, 0, s>>>(scratch, REDUCE_BLOCKS, out);
+    return (int)cudaGetLastError();
 }
 
 int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,

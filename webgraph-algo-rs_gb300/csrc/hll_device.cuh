@@ -21,9 +21,10 @@
 // 16-byte aligned (128-bit loads and stores) and, at log2m >= 6, never cross a
 // 64-byte boundary, so a counter gather moves exactly its own sectors.
 //
-// A counter is processed in chunks of at most 32 registers (32 bytes, eight
-// words, two 128-bit accesses), one lane per chunk, so a lane holds a chunk
-// and four in-flight successor chunks in registers at full occupancy.
+// A counter is processed in chunks of at most 64 registers (64 bytes, 16
+// words, four 128-bit accesses), one lane per chunk: at log2m <= 6 a whole
+// counter is one lane's, so per-arc work (successor id, address, loop) is not
+// repeated across lanes.
 //
 // count() (hyper_log_log_logic.rs:169-186) is computed exactly: the harmonic
 // sum of 2^-v over <= 2^12 registers is a multiple of 2^-31 below 2^13, so it
@@ -41,11 +42,11 @@ namespace hbd {
 template <int LOG2M>
 struct Geo {
     static constexpr int M = 1 << LOG2M;
-    static constexpr int CHUNK_REGS = M < 32 ? M : 32;
+    static constexpr int CHUNK_REGS = M < 64 ? M : 64;
     static constexpr int CHUNKS = M / CHUNK_REGS;            // chunks per counter
     static constexpr int NW = CHUNK_REGS / 4;                // 32-bit words per chunk
     static constexpr int COUNTER_BYTES = M;                  // device stride, one byte per register
-    static constexpr int CHUNK_BYTES = CHUNK_REGS;           // 16 or 32
+    static constexpr int CHUNK_BYTES = CHUNK_REGS;           // 16, 32 or 64
     static constexpr int PACKED_BYTES = M * 5 / 8;           // the reference's counter size
 };
 
@@ -155,19 +156,38 @@ __device__ __forceinline__ int64_t signed_hsum(uint64_t hsum, uint32_t c31, int 
 // ---------------------------------------------------------------------------
 // chunk load / store
 // ---------------------------------------------------------------------------
+// 32-byte pieces move as one 256-bit access (sm_100 and later): half the
+// load instructions and L1 wavefronts of 128-bit accesses for a divergent
+// gather. Chunks of 32 or 64 bytes are 32-byte aligned.
+__device__ __forceinline__ void ld_nc_256(const void* p, uint32_t* w) {
+    asm("ld.global.nc.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]),
+          "=r"(w[7])
+        : "l"(p));
+}
+
+__device__ __forceinline__ void st_256(void* p, const uint32_t* w) {
+    asm volatile("st.global.v8.u32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :
+                 : "l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]),
+                   "r"(w[6]), "r"(w[7])
+                 : "memory");
+}
+
 template <int LOG2M>
 __device__ __forceinline__ void load_chunk(const uint8_t* __restrict__ base, uint64_t node, int c,
                                            uint32_t (&w)[Geo<LOG2M>::NW]) {
     using G = Geo<LOG2M>;
-    const uint4* q = reinterpret_cast<const uint4*>(base + node * (uint64_t)G::COUNTER_BYTES +
-                                                    (uint64_t)c * G::CHUNK_BYTES);
+    const uint8_t* p = base + node * (uint64_t)G::COUNTER_BYTES + (uint64_t)c * G::CHUNK_BYTES;
+    if constexpr (G::NW >= 8) {
 #pragma unroll
-    for (int i = 0; i < G::NW / 4; i++) {
-        const uint4 t = __ldg(q + i);
-        w[4 * i] = t.x;
-        w[4 * i + 1] = t.y;
-        w[4 * i + 2] = t.z;
-        w[4 * i + 3] = t.w;
+        for (int i = 0; i < G::NW / 8; i++) ld_nc_256(p + 32 * i, w + 8 * i);
+    } else {
+        const uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
+        w[0] = t.x;
+        w[1] = t.y;
+        w[2] = t.z;
+        w[3] = t.w;
     }
 }
 
@@ -175,11 +195,13 @@ template <int LOG2M>
 __device__ __forceinline__ void store_chunk(uint8_t* __restrict__ base, uint64_t node, int c,
                                             const uint32_t (&w)[Geo<LOG2M>::NW]) {
     using G = Geo<LOG2M>;
-    uint4* q = reinterpret_cast<uint4*>(base + node * (uint64_t)G::COUNTER_BYTES +
-                                        (uint64_t)c * G::CHUNK_BYTES);
+    uint8_t* p = base + node * (uint64_t)G::COUNTER_BYTES + (uint64_t)c * G::CHUNK_BYTES;
+    if constexpr (G::NW >= 8) {
 #pragma unroll
-    for (int i = 0; i < G::NW / 4; i++)
-        q[i] = make_uint4(w[4 * i], w[4 * i + 1], w[4 * i + 2], w[4 * i + 3]);
+        for (int i = 0; i < G::NW / 8; i++) st_256(p + 32 * i, w + 8 * i);
+    } else {
+        *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
 }
 
 // ---------------------------------------------------------------------------
