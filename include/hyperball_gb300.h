@@ -209,6 +209,23 @@ int hb_graph_from_csr(const hb_graph_view* view, hb_graph** out);
 hb_graph_view hb_graph_get_view(const hb_graph* g);
 void hb_graph_free(hb_graph* g);
 
+/* ---- device CSR utilities ----------------------------------------------------- */
+
+/* Transpose of a device-resident CSR graph: d_offsets[num_nodes + 1] and
+ * d_successors[num_arcs] (device pointers) into caller-allocated device arrays
+ * d_t_offsets[num_nodes + 1] and d_t_successors[num_arcs], on `stream` (NULL =
+ * legacy default stream); returns when the result is complete. Rows of the
+ * transpose are in no particular order. Checks the input first (offsets[0] ==
+ * 0, offsets[num_nodes] == num_arcs, non-decreasing offsets, successors <
+ * num_nodes) and returns HB_ERR_INVALID otherwise. Allocates and frees about
+ * 8 * (num_nodes + 1) bytes of temporary device memory on the stream.
+ * The reference takes the transpose as an input of
+ * HyperBallBuilder::with_transpose (HB:204-210), built on the host; this is
+ * the same transpose built where the graph already is. */
+int hb_device_transpose(const uint64_t* d_offsets, const uint32_t* d_successors, uint64_t num_nodes,
+                        uint64_t num_arcs, uint64_t* d_t_offsets, uint32_t* d_t_successors,
+                        void* stream);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* Library build string, e.g. "hyperball_gb300 sm_103a". */
 const char* hb_version(void);

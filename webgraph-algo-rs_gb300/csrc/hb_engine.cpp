@@ -368,6 +368,23 @@ int relabel_csr(hb_handle* h, const uint64_t* off0, const uint32_t* succ0, uint6
     return HB_OK;
 }
 
+// Transpose of a device CSR (n nodes, m arcs) into toff[n + 1] / tsucc[m]:
+// in-degrees into `cursor` (n + 1 words, zeroed here), exclusive scan into
+// toff (`scan`: scan_scratch_len(n + 1) words), scatter with `cursor` as the
+// per-row write position. Rows of the result are in no particular order.
+cudaError_t transpose_core(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
+                           uint64_t* toff, uint32_t* tsucc, unsigned long long* cursor,
+                           unsigned long long* scan, uint64_t scan_len, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(cursor, 0, (n + 1) * 8, s);
+    if (e != cudaSuccess) return e;
+    int r = m ? hbk::launch_transpose_count(succ, m, cursor, s) : 0;
+    if (!r) r = hbk::launch_exclusive_scan_u64(cursor, toff, n + 1, scan, scan_len, s);
+    if (r || n == 0 || m == 0) return (cudaError_t)r;
+    e = cudaMemcpyAsync(cursor, toff, n * 8, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    return (cudaError_t)hbk::launch_transpose_scatter(off, succ, n, cursor, tsucc, s);
+}
+
 int build_transpose_on_device(hb_handle* h) {
     const uint64_t n = h->n, m = h->m;
     int r;
@@ -378,12 +395,8 @@ int build_transpose_on_device(hb_handle* h) {
     const uint64_t sl = hbk::scan_scratch_len(n + 1);
     unsigned long long* scratch = nullptr;
     if ((r = dalloc(h, &scratch, sl))) return r;
-    HB_CUDA(h, cudaMemsetAsync(indeg, 0, (n + 1) * 8, h->stream));
-    HB_LAUNCH(h, hbk::launch_transpose_count(h->d_succ, m, indeg, h->stream));
-    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(indeg, h->d_toff, n + 1, scratch, sl, h->stream));
-    // reuse indeg as the scatter cursor
-    HB_CUDA(h, cudaMemcpyAsync(indeg, h->d_toff, n * 8, cudaMemcpyDeviceToDevice, h->stream));
-    HB_LAUNCH(h, hbk::launch_transpose_scatter(h->d_off, h->d_succ, n, indeg, h->d_tsucc, h->stream));
+    HB_CUDA(h, transpose_core(h->d_off, h->d_succ, n, m, h->d_toff, h->d_tsucc, indeg, scratch, sl,
+                              h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     // temporaries are released right away
     for (auto it = h->bufs.begin(); it != h->bufs.end();) {
@@ -664,6 +677,72 @@ void hb_options_default(hb_options* o) {
     o->hash_kind = HB_HASH_SIP13;
     o->small_max_degree = HB_AUTO;
     o->medium_max_degree = HB_AUTO;
+}
+
+// ---- device CSR utilities ----------------------------------------------------
+namespace {
+// Checks a device CSR before any kernel indexes with it: offsets[0] == 0,
+// offsets[n] == m (read back), offsets non-decreasing and successors < n
+// (k_validate into the device int `flag`).
+int check_device_csr(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m, int* flag,
+                     cudaStream_t s) {
+    uint64_t ends[2] = {1, 0};
+    cudaError_t e = cudaMemcpyAsync(&ends[0], off, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ends[1], off + n, 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    int r = e == cudaSuccess ? hbk::launch_validate(off, succ, n, m, flag, s) : (int)e;
+    int bad = 0;
+    if (!r) r = (int)cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (!r) r = (int)cudaStreamSynchronize(s);
+    if (r) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_CUDA, std::string("device CSR check: ") + cudaGetErrorString((cudaError_t)r));
+    }
+    if (ends[0] != 0 || ends[1] != m)
+        return set_err(nullptr, HB_ERR_INVALID, "offsets[0] must be 0 and offsets[num_nodes] must equal num_arcs");
+    if (bad) return set_err(nullptr, HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
+    return HB_OK;
+}
+
+int device_transpose_args(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
+                          const uint64_t* toff, const uint32_t* tsucc) {
+    if (!off || !toff) return set_err(nullptr, HB_ERR_INVALID, "offsets and t_offsets must not be NULL");
+    if (m && (!succ || !tsucc))
+        return set_err(nullptr, HB_ERR_INVALID, "successors and t_successors must not be NULL");
+    if (n > 0xffffffffull) return set_err(nullptr, HB_ERR_INVALID, "more than 2^32 nodes do not fit u32 successors");
+    return HB_OK;
+}
+}  // namespace
+
+int hb_device_transpose(const uint64_t* d_offsets, const uint32_t* d_successors, uint64_t num_nodes,
+                        uint64_t num_arcs, uint64_t* d_t_offsets, uint32_t* d_t_successors,
+                        void* stream) {
+    int r = device_transpose_args(d_offsets, d_successors, num_nodes, num_arcs, d_t_offsets, d_t_successors);
+    if (r) return r;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t n = num_nodes, sl = hbk::scan_scratch_len(n + 1);
+    // temporaries: n + 1 cursors, the scan scratch, one flag word
+    const size_t bytes = (n + 1 + sl + 1) * 8;
+    unsigned long long* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, e == cudaErrorMemoryAllocation ? HB_ERR_OOM : HB_ERR_CUDA,
+                       std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+    }
+    r = check_device_csr(d_offsets, d_successors, n, num_arcs, (int*)(tmp + n + 1 + sl), s);
+    if (!r) {
+        e = transpose_core(d_offsets, d_successors, n, num_arcs, d_t_offsets, d_t_successors, tmp,
+                           tmp + n + 1, sl, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            r = set_err(nullptr, HB_ERR_CUDA, std::string("hb_device_transpose: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaFreeAsync(tmp, s);
+    cudaStreamSynchronize(s);
+    return r;
 }
 
 const char* hb_version(void) { return "hyperball_gb300 0.1 sm_103a"; }

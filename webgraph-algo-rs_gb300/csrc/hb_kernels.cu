@@ -112,10 +112,27 @@ __device__ __forceinline__ bool commit_node(const UnionArgs& a, uint64_t v, int 
 // and the in-degree of a changed node is added to the arcs the next
 // iteration visits.
 // ---------------------------------------------------------------------------
+// The per-node values finish_node reads (measured: loading them before the
+// gather instead gains nothing and costs registers).
+struct NodeSums {
+    double pre, sod, harm;
+    uint32_t indeg;
+};
+
+__device__ __forceinline__ NodeSums load_sums(const UnionArgs& a, uint32_t v) {
+    NodeSums s;
+    s.pre = a.est[v];
+    s.sod = a.sod ? a.sod[v] : 0.0;
+    s.harm = a.harm ? a.harm[v] : 0.0;
+    s.indeg = __ldg(a.indeg + v);
+    return s;
+}
+
 template <int LOG2M>
 __device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int c, unsigned gmask,
                                             const uint32_t (&acc)[Geo<LOG2M>::NW], bool changed,
-                                            double& nf, unsigned long long& vis) {
+                                            const NodeSums& ns, double& nf,
+                                            unsigned long long& vis) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, REGS = Gm::CHUNK_REGS;
     if (changed) {
@@ -131,7 +148,7 @@ __device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int 
             }
         }
         if (c == 0) {
-            const double pre = a.est[v];
+            const double pre = ns.pre;
             const double post = estimate_fast(signed_hsum(hs, c31, a.quirk), z, a.alpha_m_m,
                                               a.a_scaled, a.small_bits, (double)Gm::M, a.ln_table);
             a.est[v] = post;
@@ -145,15 +162,15 @@ __device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int 
             // delta > 0.0 as an integer test: positive, not NaN
             const long long db = __double_as_longlong(delta);
             if (db > 0 && db <= 0x7ff0000000000000ll) {
-                if (a.sod) a.sod[v] = __dadd_rn(a.sod[v], __dmul_rn(delta, a.d1));
-                if (a.harm) a.harm[v] = __dadd_rn(a.harm[v], div_by_small_int(delta, a.d1, a.rd1));
+                if (a.sod) a.sod[v] = __dadd_rn(ns.sod, __dmul_rn(delta, a.d1));
+                if (a.harm) a.harm[v] = __dadd_rn(ns.harm, div_by_small_int(delta, a.d1, a.rd1));
                 for (int k = 0; k < a.ndisc; k++)
                     a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, a.disc_factor[k]));
             }
-            vis += __ldg(a.indeg + v);
+            vis += ns.indeg;
         }
     } else if (!a.systolic && c == 0) {
-        nf = __dadd_rn(nf, a.est[v]);
+        nf = __dadd_rn(nf, ns.pre);
     }
 }
 
@@ -421,7 +438,9 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                     scanned++;
                     sarcs += s1 - s0;
                 }
-                finish_node<LOG2M>(a, v, c, lmask, acc, changed, nf, vis);
+                NodeSums ns{};
+                if (c == 0) ns = load_sums(a, v);
+                finish_node<LOG2M>(a, v, c, lmask, acc, changed, ns, nf, vis);
             }
         } else if (copy && p == 0) {
             uint32_t w[NW];
@@ -555,6 +574,8 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
         const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
         const bool scan = !a.systolic || test_bit(a.mbc, v);
         if (scan) {
+            NodeSums ns{};
+            if (tid == 0) ns = load_sums(a, (uint32_t)v);
             uint32_t prev[NW], acc[NW];
             if (p == 0) {
                 load_chunk<LOG2M>(a.curr, v, c, prev);
@@ -594,7 +615,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                         modc++;
                     }
                 }
-                finish_node<LOG2M>(a, (uint32_t)v, c, leader_mask, acc, changed, nf, vis);
+                finish_node<LOG2M>(a, (uint32_t)v, c, leader_mask, acc, changed, ns, nf, vis);
                 if (c == 0) a.nf_items[a.heavy_item_base + idx] = nf;
             }
         } else if (test_bit(a.curr_mod, v)) {

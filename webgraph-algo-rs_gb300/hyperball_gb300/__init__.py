@@ -180,6 +180,9 @@ EXPORTS = [
     ("hb_graph_free", None, [_H]),
     ("hb_version", ctypes.c_char_p, []),
     ("hb_kernel_launches", ctypes.c_uint64, [_H]),
+    ("hb_device_transpose", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p]),
 ]
 
 _lib = None
