@@ -226,6 +226,22 @@ int hb_device_transpose(const uint64_t* d_offsets, const uint32_t* d_successors,
                         uint64_t num_arcs, uint64_t* d_t_offsets, uint32_t* d_t_successors,
                         void* stream);
 
+/* hb_device_transpose without any device allocation, for callers that cannot
+ * allocate: code that must not call the CUDA allocator while it runs (inside a
+ * stream-capture region, or a serving loop whose device memory is fixed up
+ * front) or a process whose memory pool is exhausted. No reference
+ * counterpart. Its scratch is one fixed array in the library's device memory
+ * (a little over 8 MiB per device), so num_nodes is at most 1,048,576;
+ * larger graphs get HB_ERR_INVALID. That array is shared by every call on a
+ * device: calls that overlap in time (other streams or threads) race on it and
+ * must be serialized by the caller. The first call on each device looks up the
+ * array's address (cudaGetSymbolAddress) once; make that first call before
+ * any stream capture. No claim is made about capturing the call in a CUDA
+ * graph. Same arguments, checks and results as hb_device_transpose. */
+int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_successors,
+                                uint64_t num_nodes, uint64_t num_arcs, uint64_t* d_t_offsets,
+                                uint32_t* d_t_successors, void* stream);
+
 /* ---- introspection ---------------------------------------------------------- */
 /* Library build string, e.g. "hyperball_gb300 sm_103a". */
 const char* hb_version(void);

@@ -745,6 +745,43 @@ int hb_device_transpose(const uint64_t* d_offsets, const uint32_t* d_successors,
     return r;
 }
 
+int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_successors,
+                                uint64_t num_nodes, uint64_t num_arcs, uint64_t* d_t_offsets,
+                                uint32_t* d_t_successors, void* stream) {
+    int r = device_transpose_args(d_offsets, d_successors, num_nodes, num_arcs, d_t_offsets, d_t_successors);
+    if (r) return r;
+    if (num_nodes > hbk::NOALLOC_MAX_NODES)
+        return set_err(nullptr, HB_ERR_INVALID,
+                       "hb_device_transpose_noalloc: num_nodes " + std::to_string(num_nodes) +
+                           " exceeds its fixed scratch (at most " +
+                           std::to_string(hbk::NOALLOC_MAX_NODES) +
+                           " nodes); use hb_device_transpose");
+    unsigned long long* scratch = nullptr;
+    uint64_t words = 0;
+    r = hbk::noalloc_scratch(&scratch, &words);
+    if (r) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_CUDA,
+                       std::string("hb_device_transpose_noalloc: cudaGetSymbolAddress: ") +
+                           cudaGetErrorString((cudaError_t)r));
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t n = num_nodes, sl = hbk::scan_scratch_len(n + 1);
+    if (n + 1 + sl + 1 > words)
+        return set_err(nullptr, HB_ERR_INVALID, "hb_device_transpose_noalloc: scratch too small");
+    // cursors [0, n], scan scratch, then the flag word (all cleared before use)
+    r = check_device_csr(d_offsets, d_successors, n, num_arcs, (int*)(scratch + n + 1 + sl), s);
+    if (r) return r;
+    cudaError_t e = transpose_core(d_offsets, d_successors, n, num_arcs, d_t_offsets, d_t_successors,
+                                   scratch, scratch + n + 1, sl, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_CUDA, std::string("hb_device_transpose_noalloc: ") + cudaGetErrorString(e));
+    }
+    return HB_OK;
+}
+
 const char* hb_version(void) { return "hyperball_gb300 0.1 sm_103a"; }
 
 uint64_t hb_kernel_launches(const hb_handle* h) { return h ? h->launches : 0; }

@@ -156,6 +156,10 @@ int launch_transpose_count(const uint32_t* succ, uint64_t m, unsigned long long*
 int launch_exclusive_scan_u64(const unsigned long long* in, uint64_t* out, uint64_t count,
                               unsigned long long* scratch, uint64_t scratch_len, void* stream);
 uint64_t scan_scratch_len(uint64_t count);
+// The fixed device scratch of hb_device_transpose_noalloc on the current
+// device (looked up on first use per device) and its size in words.
+constexpr uint64_t NOALLOC_MAX_NODES = 1ull << 20;
+int noalloc_scratch(unsigned long long** out, uint64_t* words);
 int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t n,
                              unsigned long long* cursor, uint32_t* tsucc, void* stream);
 int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m, int* bad,

@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "hb_internal.h"
 #include "hll_device.cuh"
@@ -1261,6 +1262,44 @@ int launch_transpose_count(const uint32_t* succ, uint64_t m, unsigned long long*
     ++t_launches;
     k_count_indeg<<<grid, 256, 0, (cudaStream_t)stream>>>(succ, m, indeg);
     return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Fixed device scratch of hb_device_transpose_noalloc: cursors for up to
+// NOALLOC_MAX_NODES + 1 rows, the scan scratch for that many, one flag word.
+// A file-scope device array, so using it allocates nothing; its address is
+// looked up once per device.
+// ---------------------------------------------------------------------------
+constexpr uint64_t noalloc_scan_len(uint64_t count) {
+    uint64_t total = 0;
+    while (count > 1) {
+        count = (count + SCAN_TILE - 1) / SCAN_TILE;
+        total += 2 * count;
+    }
+    return total + 2;
+}
+constexpr uint64_t NOALLOC_WORDS =
+    (NOALLOC_MAX_NODES + 1) + noalloc_scan_len(NOALLOC_MAX_NODES + 1) + 1;
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[NOALLOC_WORDS];
+
+int noalloc_scratch(unsigned long long** out, uint64_t* words) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static unsigned long long* ptrs[MAX_DEVICES] = {};
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= MAX_DEVICES) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return (int)e;
+        ptrs[dev] = (unsigned long long*)p;
+    }
+    *out = ptrs[dev];
+    *words = NOALLOC_WORDS;
+    return 0;
 }
 
 uint64_t scan_scratch_len(uint64_t count) {

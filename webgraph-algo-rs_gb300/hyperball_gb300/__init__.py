@@ -183,6 +183,9 @@ EXPORTS = [
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
+    ("hb_device_transpose_noalloc", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
+      ctypes.c_void_p, ctypes.c_void_p]),
 ]
 
 _lib = None
