@@ -132,8 +132,7 @@ __device__ __forceinline__ NodeSums load_sums(const UnionArgs& a, uint32_t v) {
 template <int LOG2M>
 __device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int c, unsigned gmask,
                                             const uint32_t (&acc)[Geo<LOG2M>::NW], bool changed,
-                                            const NodeSums& ns, double& nf,
-                                            unsigned long long& vis) {
+                                            const NodeSums& ns, double& nf, uint32_t& vis) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, REGS = Gm::CHUNK_REGS;
     if (changed) {
@@ -242,29 +241,49 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
                                                uint32_t (&acc)[Geo<LOG2M>::NW]) {
     using Gm = Geo<LOG2M>;
     constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIPE = pipe_depth<NW>();
-    uint32_t y[PIPE][NW];
-    bool have[PIPE];
-    uint32_t nid[PIPE];
-#pragma unroll
-    for (int k = 0; k < PIPE; k++) {
-        const uint64_t e = e0 + (uint64_t)k * stride;
-        const uint32_t sid = e < e1 ? __ldg(a.succ + e) : v;
-        const uint64_t en = e + (uint64_t)PIPE * stride;
-        nid[k] = en < e1 ? __ldg(a.succ + en) : v;
-        have[k] = e < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
-        if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
-    }
-    for (uint64_t e = e0 + (uint64_t)PIPE * stride; e < e1 + (uint64_t)PIPE * stride;
-         e += (uint64_t)PIPE * stride) {
+    if constexpr (PIPE == 1) {
+        // one counter in flight: the next successor id loads while the current
+        // counter is merged
+        if (e0 >= e1) return;
+        const uint32_t* sp = a.succ + e0;
+        const uint32_t cnt = (uint32_t)((e1 - e0 + stride - 1) / stride);
+        uint32_t s = __ldg(sp);
+        bool have = !filter || (s != v && test_bit(a.curr_mod, s));
+        uint32_t y[NW];
+        if (have) load_chunk<LOG2M>(a.curr, s, c, y);
+        for (uint32_t i = 1; i < cnt; i++) {
+            const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
+            const bool nh = !filter || (ns != v && test_bit(a.curr_mod, ns));
+            if (have) merge_chunk<REGS>(acc, y);
+            if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
+            have = nh;
+        }
+        if (have) merge_chunk<REGS>(acc, y);
+    } else {
+        uint32_t y[PIPE][NW];
+        bool have[PIPE];
+        uint32_t nid[PIPE];
 #pragma unroll
         for (int k = 0; k < PIPE; k++) {
-            if (have[k]) merge_chunk<REGS>(acc, y[k]);
-            const uint64_t ek = e + (uint64_t)k * stride;
-            const uint32_t sid = nid[k];
-            const uint64_t en = ek + (uint64_t)PIPE * stride;
+            const uint64_t e = e0 + (uint64_t)k * stride;
+            const uint32_t sid = e < e1 ? __ldg(a.succ + e) : v;
+            const uint64_t en = e + (uint64_t)PIPE * stride;
             nid[k] = en < e1 ? __ldg(a.succ + en) : v;
-            have[k] = ek < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+            have[k] = e < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
             if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
+        }
+        for (uint64_t e = e0 + (uint64_t)PIPE * stride; e < e1 + (uint64_t)PIPE * stride;
+             e += (uint64_t)PIPE * stride) {
+#pragma unroll
+            for (int k = 0; k < PIPE; k++) {
+                if (have[k]) merge_chunk<REGS>(acc, y[k]);
+                const uint64_t ek = e + (uint64_t)k * stride;
+                const uint32_t sid = nid[k];
+                const uint64_t en = ek + (uint64_t)PIPE * stride;
+                nid[k] = en < e1 ? __ldg(a.succ + en) : v;
+                have[k] = ek < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+                if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
+            }
         }
     }
 }
@@ -384,11 +403,10 @@ __device__ __forceinline__ bool differs_from(const uint8_t* __restrict__ base, u
 // bits and counts scanned nodes, their arcs and the changed counters.
 template <int LOG2M, int TB>
 __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
-                                          uint32_t b, uint32_t e, unsigned long long& modc,
-                                          unsigned long long& scanned, unsigned long long& sarcs,
-                                          unsigned long long& vis, double& nf, uint32_t ring) {
+                                          uint32_t b, uint32_t e, uint32_t& modc, uint32_t& scanned,
+                                          uint32_t& sarcs, uint32_t& vis, double& nf, uint32_t ring) {
     using Gm = Geo<LOG2M>;
-    constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW;
     constexpr int PB = TB / G;   // arc lanes per node
     constexpr int NPW = 32 / TB; // nodes per warp-step
     const int lane = threadIdx.x & 31;
@@ -424,10 +442,19 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                 __syncwarp(tmask);
 #pragma unroll
                 for (int off = G; off < TB; off <<= 1) {
-                    uint32_t y[NW];
+                    // four words at a time keeps few registers live
 #pragma unroll
-                    for (int k = 0; k < NW; k++) y[k] = __shfl_xor_sync(tmask, acc[k], off);
-                    merge_chunk<REGS>(acc, y);
+                    for (int k = 0; k < NW; k += 4) {
+                        uint32_t x4[4], y4[4];
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            x4[j] = acc[k + j];
+                            y4[j] = __shfl_xor_sync(tmask, acc[k + j], off);
+                        }
+                        merge_chunk<16>(x4, y4);
+#pragma unroll
+                        for (int j = 0; j < 4; j++) acc[k + j] = x4[j];
+                    }
                 }
             }
             if (p == 0) {
@@ -437,7 +464,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                 store_chunk<LOG2M>(a.next, v, c, acc);
                 if (c == 0) {
                     scanned++;
-                    sarcs += s1 - s0;
+                    sarcs += (uint32_t)(s1 - s0);
                 }
                 NodeSums ns{};
                 if (c == 0) ns = load_sums(a, v);
@@ -462,10 +489,18 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
     }
 }
 
+// The medium path (measured: inlining it beats a separate call frame).
+template <int LOG2M, int TB>
+__device__ __forceinline__ void run_medium(const UnionArgs& a, uint32_t b, uint32_t e,
+                                        uint32_t& modc, uint32_t& scanned, uint32_t& sarcs,
+                                        uint32_t& vis, double& nf) {
+    run_nodes<LOG2M, TB>(a, a.medium_list, b, e, modc, scanned, sarcs, vis, nf, 0u);
+}
+
 // Work item k: a chunk of the table, or (systolic) a run of the light list
 // followed by runs of the medium list; {first, count | medium << 31}.
 struct WorkItems {
-    uint64_t n_work, light_items;
+    uint32_t n_work, light_items;
     uint32_t n_light, n_medium;
 };
 
@@ -479,14 +514,14 @@ __device__ __forceinline__ WorkItems work_items(const UnionArgs& a) {
         w.light_items = (w.n_light + NPW_L - 1) / NPW_L;
         w.n_work = w.light_items + (w.n_medium + NPW_M - 1) / NPW_M;
     } else {
-        w.n_work = a.n_chunks;
+        w.n_work = (uint32_t)a.n_chunks;
     }
     return w;
 }
 
 template <int NPW_L, int NPW_M>
 __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
-                                         unsigned long long k) {
+                                         uint32_t k) {
     if (k >= w.n_work) return make_uint2(0u, 0u);
     if (!a.light_list) return __ldg(a.chunks + k);
     if (k < w.light_items) {
@@ -507,18 +542,20 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
     const uint32_t ring = (uint32_t)__cvta_generic_to_shared(ring_smem) +
                           (threadIdx.x >> 5) * (uint32_t)RingGeo<LOG2M>::WARP_BYTES;
     constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
-    unsigned long long modc = 0, scanned = 0, sarcs = 0, vis = 0;
+    // per-warp totals: at most one warp's share of the nodes and arcs of one
+    // iteration, far below 2^32
+    uint32_t modc = 0, scanned = 0, sarcs = 0, vis = 0;
     const WorkItems wi = work_items<NPW_L, NPW_M>(a);
-    const uint64_t n_work = wi.n_work;
+    const uint32_t n_work = wi.n_work;
     // Work items come GRAB at a time from the cursor (one atomic per GRAB
     // chunks; measured fastest at 1). Handing out consecutive items keeps the
     // band of nodes in flight narrow.
     constexpr unsigned GRAB = 1;
-    unsigned long long k = 0, kend = 0;
+    uint32_t k = 0, kend = 0;
     for (;;) {
         if (k == kend) {
-            unsigned long long first = 0;
-            if (lane == 0) first = atomicAdd(a.cursor, (unsigned long long)GRAB);
+            uint32_t first = 0;
+            if (lane == 0) first = (uint32_t)atomicAdd(a.cursor, (unsigned long long)GRAB);
             k = __shfl_sync(0xffffffffu, first, 0);
             kend = k + GRAB;
         }
@@ -528,8 +565,7 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
         const uint32_t cnt = d.y & 0x7fffffffu;
         double nf = 0.0;
         if (d.y >> 31)
-            run_nodes<LOG2M, TB_MED>(a, a.medium_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf,
-                                     ring);
+            run_medium<LOG2M, TB_MED>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf);
         else
             run_nodes<LOG2M, G>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, ring);
         // the item's neighbourhood-function part: fixed lanes, fixed order
@@ -546,10 +582,10 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
     if (lane == 0) {
         // integer totals are order independent
         TilePartial* t = a.partials + a.acc_slot;
-        if (modc) atomicAdd(&t->mod, modc);
-        if (scanned) atomicAdd(&t->scanned, scanned);
-        if (sarcs) atomicAdd(&t->sarcs, sarcs);
-        if (vis) atomicAdd(&t->vis, vis);
+        if (modc) atomicAdd(&t->mod, (unsigned long long)modc);
+        if (scanned) atomicAdd(&t->scanned, (unsigned long long)scanned);
+        if (sarcs) atomicAdd(&t->sarcs, (unsigned long long)sarcs);
+        if (vis) atomicAdd(&t->vis, (unsigned long long)vis);
     }
 }
 
@@ -568,7 +604,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     const int tid = threadIdx.x;
     const int p = tid / G, c = tid % G;
     const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
-    unsigned long long modc = 0, scanned = 0, sarcs = 0, vis = 0;
+    uint32_t modc = 0, scanned = 0, sarcs = 0, vis = 0;
     for (uint64_t idx = blockIdx.x; idx < a.list_len; idx += gridDim.x) {
         double nf = 0.0;
         const uint64_t v = __ldg(a.list + idx);
@@ -610,7 +646,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                 const bool changed = commit_node<LOG2M>(a, v, c, leader_mask, prev, acc);
                 if (c == 0) {
                     scanned++;
-                    sarcs += s1 - s0;
+                    sarcs += (uint32_t)(s1 - s0);
                     if (changed) {
                         atomicOr(a.next_mod + (v >> 5), 1u << (v & 31));
                         modc++;
@@ -638,10 +674,10 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     if (lane == 0) {
         // integer totals are order independent
         TilePartial* t = a.partials + a.acc_slot;
-        if (modc) atomicAdd(&t->mod, modc);
-        if (scanned) atomicAdd(&t->scanned, scanned);
-        if (sarcs) atomicAdd(&t->sarcs, sarcs);
-        if (vis) atomicAdd(&t->vis, vis);
+        if (modc) atomicAdd(&t->mod, (unsigned long long)modc);
+        if (scanned) atomicAdd(&t->scanned, (unsigned long long)scanned);
+        if (sarcs) atomicAdd(&t->sarcs, (unsigned long long)sarcs);
+        if (vis) atomicAdd(&t->vis, (unsigned long long)vis);
     }
 }
 

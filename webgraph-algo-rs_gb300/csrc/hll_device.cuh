@@ -12,11 +12,11 @@
 // (trailing zeros of a value with bit 30 set, plus one), so bits 5-7 of every
 // byte are zero, and the register-wise max of the reference's broadword merge
 // (hyper_log_log_logic.rs:469-576) becomes, per 32-bit word of four registers,
-//     t    = (x | 0x80808080) - y      bit 7 of a byte set iff x >= y there;
+//     t    = x + 0x80808080 - y        bit 7 of a byte set iff x >= y there;
 //                                      no borrow leaves a byte (x+128-y > 0)
 //     keep = prmt(t, sign-replicate)   0xff where x >= y, else 0x00
 //     x    = y ^ ((x ^ y) & keep)
-// five integer instructions per four registers, against about fourteen per
+// three integer instructions per four registers, against about fourteen per
 // word of the packed broadword form. Counters of 2^log2m bytes are also
 // 16-byte aligned (128-bit loads and stores) and, at log2m >= 6, never cross a
 // 64-byte boundary, so a counter gather moves exactly its own sectors.
@@ -64,17 +64,23 @@ __device__ __forceinline__ void merge_chunk(uint32_t (&x)[REGS / 4], const uint3
                                             uint32_t& grew) {
 #pragma unroll
     for (int i = 0; i < REGS / 4; i++) {
-        const uint32_t keep = byte_signs((x[i] | 0x80808080u) - y[i]);
+        // x + 0x80808080 - y == (x | 0x80808080) - y: bit 7 of every byte of x is 0
+        const uint32_t keep = byte_signs(x[i] + 0x80808080u - y[i]);
         const uint32_t r = y[i] ^ ((x[i] ^ y[i]) & keep);
         grew |= r ^ x[i];
         x[i] = r;
     }
 }
 
+// the same without the change mask: three instructions per word (one
+// three-input add, one byte permute, one three-input logic op)
 template <int REGS>
 __device__ __forceinline__ void merge_chunk(uint32_t (&x)[REGS / 4], const uint32_t (&y)[REGS / 4]) {
-    uint32_t unused = 0;
-    merge_chunk<REGS>(x, y, unused);
+#pragma unroll
+    for (int i = 0; i < REGS / 4; i++) {
+        const uint32_t keep = byte_signs(x[i] + 0x80808080u - y[i]);
+        x[i] = y[i] ^ ((x[i] ^ y[i]) & keep);
+    }
 }
 
 // Number of zero bytes of w (all bytes below 0x80): ((b | 0x80) - 1) keeps
@@ -128,7 +134,9 @@ __device__ __forceinline__ double exact_u64_to_double(uint64_t u) {
 //   scaling), so a_scaled = alpha*m^2*2^31 is precomputed; H > 0 converts
 //   exactly; `e < 2.5m` between positive finite doubles is an integer compare
 //   of their bit patterns. H <= 0 (only reachable through the i32 quirk)
-//   takes the reference arithmetic.
+//   takes the reference arithmetic. (An all-integer correctly rounded
+//   division measured no faster inside the union kernel, whose f64 pipe is
+//   about 17% busy.)
 __device__ __forceinline__ double estimate_fast(int64_t hsum, uint32_t zeroes, double alpha_m_m,
                                                 double a_scaled, long long small_bits, double m,
                                                 const double* __restrict__ ln_table) {
