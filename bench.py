@@ -171,19 +171,25 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # roofline model of the union kernels (k_union_window + k_union_heavy)
 # ---------------------------------------------------------------------------
+N_SUMS = 2  # sum of distances and harmonic centrality are requested
+
+
 def union_model_bytes(stats, n):
     """Compulsory HBM bytes of the union kernels of each iteration:
     8 B offsets per scanned node, 4 B per successor id read, one counter read
     per distinct modified successor (bounded by min(previously modified,
-    visited arcs)), prev read + next write of every scanned node, and the
-    modified / must-be-checked bitmaps."""
+    visited arcs)), prev read + next write of every scanned node, the
+    modified / must-be-checked bitmaps, and for every changed counter the
+    estimate cache and each requested per-node sum read and written once.
+    Counters count at the reference's size (2^log2m * 5 / 8 bytes)."""
     out = []
     prev_mod = n  # init marks every counter modified
     for s in stats:
-        S, A, V = s["scanned_nodes"], s["scanned_arcs"], s["visited_arcs"]
+        S, A, V, M = s["scanned_nodes"], s["scanned_arcs"], s["visited_arcs"], s["modified_counters"]
         U = min(prev_mod, V)
-        out.append(8 * S + 4 * A + COUNTER_BYTES * U + 2 * COUNTER_BYTES * S + n // 4)
-        prev_mod = s["modified_counters"]
+        out.append(8 * S + 4 * A + COUNTER_BYTES * U + 2 * COUNTER_BYTES * S + n // 4
+                   + (16 + 16 * N_SUMS) * M)
+        prev_mod = M
     return out
 
 

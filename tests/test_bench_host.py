@@ -54,10 +54,10 @@ def test_union_model_bytes():
         {"scanned_nodes": 1000, "scanned_arcs": 8000, "visited_arcs": 7900, "modified_counters": 900},
         {"scanned_nodes": 300, "scanned_arcs": 2000, "visited_arcs": 500, "modified_counters": 0},
     ]
-    w = bench.COUNTER_BYTES
+    w, f = bench.COUNTER_BYTES, 16 + 16 * bench.N_SUMS
     got = bench.union_model_bytes(stats, n)
-    assert got[0] == 8 * 1000 + 4 * 8000 + w * min(n, 7900) + 2 * w * 1000 + n // 4
-    assert got[1] == 8 * 300 + 4 * 2000 + w * min(900, 500) + 2 * w * 300 + n // 4
+    assert got[0] == 8 * 1000 + 4 * 8000 + w * min(n, 7900) + 2 * w * 1000 + n // 4 + f * 900
+    assert got[1] == 8 * 300 + 4 * 2000 + w * min(900, 500) + 2 * w * 300 + n // 4 + f * 0
 
 
 def test_clock_summary():
