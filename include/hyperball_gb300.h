@@ -209,6 +209,40 @@ int hb_graph_from_csr(const hb_graph_view* view, hb_graph** out);
 hb_graph_view hb_graph_get_view(const hb_graph* g);
 void hb_graph_free(hb_graph* g);
 
+/* ---- batches: many independent instances in one pass -------------------------- */
+
+typedef struct hb_batch hb_batch;
+
+/* Builds `count` independent HyperBall instances, graphs[i] (host CSR, copied)
+ * with log2m[i] registers per counter; every other option (hash, flags,
+ * device, stream, degree buckets) is shared; weights are not supported.
+ * Instances with the same log2m run together as one disjoint union, so each
+ * iteration is one pass of the union kernels over all of them. For every graph
+ * the batch returns what HyperBallBuilder::build (HB:321-403) followed by
+ * run_until_done (HB:614-621) returns for it alone: the same registers,
+ * iteration count, neighbourhood function and per-node sums. The reference has
+ * no batch API. */
+int hb_batch_create(const hb_graph_view* graphs, uint32_t count, const int32_t* log2m,
+                    const hb_options* opts, hb_batch** out);
+/* Runs every instance until no counter of it changes. */
+int hb_batch_run_until_done(hb_batch* b);
+uint32_t hb_batch_num_graphs(const hb_batch* b);
+/* Iterations graph `graph` ran (its own, as if alone). */
+uint64_t hb_batch_num_iterations(const hb_batch* b, uint32_t graph);
+/* Per-graph results, as the single-instance getters (HB:633-657). */
+int hb_batch_get_neighborhood_function(const hb_batch* b, uint32_t graph, double* dst,
+                                       size_t capacity, size_t* len);
+int hb_batch_get_sum_of_distances(const hb_batch* b, uint32_t graph, double* dst, size_t len);
+int hb_batch_get_harmonic_centralities(const hb_batch* b, uint32_t graph, double* dst, size_t len);
+/* Counters of graph `graph` in the reference layout (see hb_get_registers). */
+int hb_batch_get_registers(const hb_batch* b, uint32_t graph, void* dst, size_t bytes);
+/* Totals over the batch: iterations of the longest group, visited arcs and
+ * arc-register updates (visited arcs * 2^log2m) summed over every instance and
+ * iteration, device time of the iterations (summed over groups). */
+int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_arcs,
+                   uint64_t* register_updates, double* device_ms);
+void hb_batch_destroy(hb_batch* b);
+
 /* ---- device CSR utilities ----------------------------------------------------- */
 
 /* Transpose of a device-resident CSR graph: d_offsets[num_nodes + 1] and

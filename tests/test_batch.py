@@ -1,0 +1,87 @@
+"""Batched HyperBall: every instance of a batch must give what the same graph
+gives alone (registers bit-exact, iteration count, neighbourhood function and
+per-node sums to 1e-12)."""
+import numpy as np
+import pytest
+
+import hyperball_gb300 as hb
+
+RTOL = 1e-12
+
+
+def _graphs():
+    gs = [
+        hb.Graph.erdos_renyi(1000, 4, 1),
+        hb.Graph.rmat(10, 16, seed=3),
+        hb.Graph.erdos_renyi(3000, 9, 5),
+        hb.Graph.weblike(5000, seed=7),
+        hb.Graph.rmat(9, 16, seed=9),
+        hb.Graph.erdos_renyi(700, 6, 11),
+        # self-loops, isolated nodes and a node with no arcs at all
+        hb.Graph.from_csr(np.array([0, 2, 3, 3, 5], dtype=np.uint64),
+                          np.array([0, 1, 2, 0, 3], dtype=np.uint32)),
+        hb.Graph.from_csr(np.array([0], dtype=np.uint64), np.array([], dtype=np.uint32)),
+        hb.Graph.from_csr(np.array([0, 0], dtype=np.uint64), np.array([], dtype=np.uint32)),
+        hb.Graph.erdos_renyi(2048, 16, 13),
+    ]
+    log2ms = [4, 6, 8, 6, 4, 8, 6, 6, 4, 8]
+    return gs, log2ms
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("hasher", [hb.DefaultHasher(), hb.JenkinsHasher(42)], ids=["sip13", "jenkins"])
+def test_batch_equals_instances_alone(hasher):
+    gs, log2ms = _graphs()
+    b = hb.HyperBallBatch(gs, log2ms, hasher=hasher, sum_of_distances=True,
+                          sum_of_inverse_distances=True)
+    b.run_until_done()
+    for i, (g, l2m) in enumerate(zip(gs, log2ms)):
+        logic = hb.HyperLogLogBuilder(max(g.num_nodes, 1)).log_2_num_reg(l2m).build_hasher(hasher).build()
+        h = (hb.HyperBallBuilder.new(g, logic).transpose_on_device(True)
+             .sum_of_distances(True).sum_of_inverse_distances(True).build())
+        h.run_until_done()
+        assert b.iterations(i) == h.iteration, i
+        np.testing.assert_array_equal(b.registers(i), h.registers(), err_msg=f"graph {i}")
+        if h.iteration == 0:
+            # no nodes, no iteration: neither has computed fields (HB:624-630)
+            for get in ("neighborhood_function", "sum_of_distances", "harmonic_centralities"):
+                with pytest.raises(hb.NotRunError):
+                    getattr(h, get)()
+                with pytest.raises(hb.NotRunError):
+                    getattr(b, get)(i)
+        else:
+            np.testing.assert_allclose(b.neighborhood_function(i), h.neighborhood_function(), rtol=RTOL)
+            np.testing.assert_allclose(b.sum_of_distances(i), h.sum_of_distances(), rtol=RTOL)
+            np.testing.assert_allclose(b.harmonic_centralities(i), h.harmonic_centralities(), rtol=RTOL)
+        h.close()
+    st = b.stats()
+    assert st["iterations"] == max(b.iterations(i) for i in range(len(b)))
+    b.close()
+
+
+@pytest.mark.gpu
+def test_batch_errors():
+    gs, log2ms = _graphs()
+    with pytest.raises(hb.InvalidArgumentError):
+        hb.HyperBallBatch(gs[:2], [4, 3])
+    with pytest.raises(hb.InvalidArgumentError):
+        hb.HyperBallBatch(gs[:2], [4])
+    b = hb.HyperBallBatch(gs[:2], [4, 6])
+    with pytest.raises(hb.NotRunError):
+        b.neighborhood_function(0)
+    b.run_until_done()
+    with pytest.raises(hb.NotRequestedError):
+        b.sum_of_distances(0)
+    with pytest.raises(hb.InvalidArgumentError):
+        b.neighborhood_function(5)
+    b.close()
+
+
+def test_batch_needs_a_device(product_lib):
+    """Without a GPU the batch API fails loudly instead of computing on the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    g = hb.Graph.erdos_renyi(100, 3, 1)
+    with pytest.raises(hb.NoDeviceError):
+        hb.HyperBallBatch([g], [6])

@@ -21,6 +21,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -96,14 +97,24 @@ struct hb_handle {
     uint64_t n_tiles = 0;         // number of windows
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
     uint32_t* d_indeg = nullptr;    // in-degree without self-loops
+    std::vector<uint64_t> inst_start; // batch: instance starts (caller ids), then num_nodes
+    uint32_t* d_hash_id = nullptr;    // batch: device node -> its instance's own id
+    uint64_t* d_inst_start = nullptr;
+    unsigned long long* d_inst_mod = nullptr;
+    double* d_inst_nf = nullptr;
+    std::vector<unsigned long long> inst_mod;    // last iteration, per instance
+    std::vector<double> inst_sum;                // last iteration, per instance
+    std::vector<uint64_t> inst_iters;            // iterations run so far
+    std::vector<uint8_t> inst_done;              // stopped (HB:559-570)
+    std::vector<std::vector<double>> inst_nf;    // neighbourhood function per instance
     uint64_t self_loops = 0;
     uint64_t pending_visited = 0;   // arcs the next iteration visits
     uint32_t* d_perm = nullptr;     // device node -> caller node
     uint32_t* d_inv = nullptr;      // caller node -> device node
     std::vector<uint32_t> inv_host;
     uint64_t n_chunks = 0;
-    uint32_t* d_win_medium = nullptr;           // first medium node of every window
-    uint32_t* d_win_light = nullptr;            // first light node of every window
+    uint32_t* d_light_bits = nullptr;           // light nodes (device ids)
+    uint32_t* d_medium_bits = nullptr;          // medium nodes (device ids)
     unsigned long long* d_word_cnt = nullptr;   // systolic lists: per bitmap word counts
     uint64_t* d_word_off = nullptr;             // their exclusive prefix sum (+ totals)
     unsigned long long* d_list_scratch = nullptr;
@@ -190,43 +201,59 @@ void release(hb_handle* h) {
 }
 
 // Static work order of the union kernels (the graph does not change), and the
-// node renumbering that follows it. Nodes are cut into windows of `win_nodes`
-// consecutive ids; inside a window the heavy nodes (out-degree > medium_max),
-// the medium nodes (small_max < out-degree <= medium_max) and the light nodes
-// (out-degree <= small_max) take the window's ids in that order, each kind by
-// decreasing out-degree, ties by id: perm[new] = caller id, inv[caller] = new.
-// The light and medium runs are cut into chunks of one warp-step (`per_light`
-// or `per_medium` nodes); heavy nodes are listed by decreasing degree. Windows
-// are processed by all host threads.
+// node renumbering that follows it. Nodes are cut into segments of at most
+// `win_nodes` consecutive ids, which also end at every instance boundary of a
+// batch (`bounds`: sorted instance starts, or empty); inside a segment the
+// heavy nodes (out-degree > medium_max), the medium nodes (small_max <
+// out-degree <= medium_max) and the light nodes (out-degree <= small_max)
+// take the segment's ids in that order, each kind by decreasing out-degree,
+// ties by id: perm[new] = caller id, inv[caller] = new. Renumbering never
+// leaves a segment, so an instance keeps its id range. The light and medium
+// runs are cut into chunks of one warp-step (`per_light` or `per_medium`
+// nodes); heavy nodes are listed by decreasing degree; `light_bits` /
+// `medium_bits` mark the light / medium nodes (device ids). Segments are
+// processed by all host threads.
 struct WorkPartition {
-    std::vector<uint32_t> tiles, perm, inv, heavy, win_medium, win_light;
+    std::vector<uint32_t> tiles, perm, inv, heavy, light_bits, medium_bits;
     std::vector<uint2> chunks;
 };
 
 void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium_max,
                      uint32_t win_nodes, uint32_t per_light, uint32_t per_medium,
-                     WorkPartition& out) {
+                     const std::vector<uint64_t>& bounds, WorkPartition& out) {
     const uint64_t n = g->num_nodes;
     const uint64_t* off = g->offsets;
-    const uint64_t nwin = (n + win_nodes - 1) / win_nodes;
-    struct WinCount {
+    // segment starts
+    std::vector<uint64_t> seg;
+    {
+        size_t bi = 0;
+        for (uint64_t w0 = 0; w0 < n;) {
+            while (bi < bounds.size() && bounds[bi] <= w0) bi++;
+            uint64_t w1 = std::min<uint64_t>(n, w0 + win_nodes);
+            if (bi < bounds.size() && bounds[bi] < w1) w1 = bounds[bi];
+            seg.push_back(w0);
+            w0 = w1;
+        }
+        seg.push_back(n);
+    }
+    const uint64_t nseg = seg.size() - 1;
+    struct SegCount {
         uint64_t light, medium, heavy;
     };
-    std::vector<WinCount> cnt(nwin);
+    std::vector<SegCount> cnt(nseg);
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const uint64_t nthreads = std::min<uint64_t>(std::min<uint64_t>(hw, 64), std::max<uint64_t>(nwin, 1));
-    auto parallel = [&](auto&& body) {
+    auto parallel = [&](uint64_t count, auto&& body) {
+        const uint64_t nthreads = std::min<uint64_t>(std::min<uint64_t>(hw, 64), std::max<uint64_t>(count, 1));
         std::vector<std::thread> th;
         for (uint64_t t = 0; t < nthreads; t++)
             th.emplace_back([&, t] {
-                for (uint64_t w = nwin * t / nthreads; w < nwin * (t + 1) / nthreads; w++) body(w);
+                for (uint64_t w = count * t / nthreads; w < count * (t + 1) / nthreads; w++) body(w);
             });
         for (auto& x : th) x.join();
     };
-    parallel([&](uint64_t w) {
-        WinCount c{0, 0, 0};
-        const uint64_t w0 = w * win_nodes, w1 = std::min<uint64_t>(n, w0 + win_nodes);
-        for (uint64_t v = w0; v < w1; v++) {
+    parallel(nseg, [&](uint64_t w) {
+        SegCount c{0, 0, 0};
+        for (uint64_t v = seg[w]; v < seg[w + 1]; v++) {
             const uint64_t d = off[v + 1] - off[v];
             if (d > medium_max)
                 c.heavy++;
@@ -237,28 +264,23 @@ void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium
         }
         cnt[w] = c;
     });
-    // window offsets into chunks and heavy
-    std::vector<uint64_t> chunk_at(nwin + 1, 0), heavy_at(nwin + 1, 0);
-    for (uint64_t w = 0; w < nwin; w++) {
-        const WinCount& c = cnt[w];
+    // segment offsets into chunks and heavy
+    std::vector<uint64_t> chunk_at(nseg + 1, 0), heavy_at(nseg + 1, 0);
+    for (uint64_t w = 0; w < nseg; w++) {
+        const SegCount& c = cnt[w];
         chunk_at[w + 1] = chunk_at[w] + (c.medium + per_medium - 1) / per_medium +
                           (c.light + per_light - 1) / per_light;
         heavy_at[w + 1] = heavy_at[w] + c.heavy;
     }
-    out.tiles.resize(n ? nwin + 1 : 0);
-    for (uint64_t w = 0; n && w <= nwin; w++) out.tiles[w] = (uint32_t)std::min<uint64_t>(n, w * win_nodes);
-    out.win_medium.resize(nwin);
-    out.win_light.resize(nwin);
-    for (uint64_t w = 0; w < nwin; w++) {
-        out.win_medium[w] = (uint32_t)(w * win_nodes + cnt[w].heavy);
-        out.win_light[w] = (uint32_t)(w * win_nodes + cnt[w].heavy + cnt[w].medium);
-    }
+    out.tiles.resize(n ? nseg + 1 : 0);
+    for (uint64_t w = 0; n && w <= nseg; w++) out.tiles[w] = (uint32_t)seg[w];
     out.perm.resize(n);
     out.inv.resize(n);
-    out.chunks.resize(chunk_at[nwin]);
-    out.heavy.resize(heavy_at[nwin]);
-    parallel([&](uint64_t w) {
-        const uint64_t w0 = w * win_nodes, w1 = std::min<uint64_t>(n, w0 + win_nodes);
+    out.chunks.resize(chunk_at[nseg]);
+    out.heavy.resize(heavy_at[nseg]);
+    std::vector<uint8_t> kind_of(n);  // device id -> 0 heavy, 1 medium, 2 light
+    parallel(nseg, [&](uint64_t w) {
+        const uint64_t w0 = seg[w], w1 = seg[w + 1];
         // sort key: (inverted clamped degree, node): decreasing degree, ties by id
         std::vector<uint64_t> kind[3];
         for (uint64_t v = w0; v < w1; v++) {
@@ -273,6 +295,7 @@ void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium
             for (uint64_t key : kind[k]) {
                 out.perm[next] = (uint32_t)key;
                 out.inv[(uint32_t)key] = (uint32_t)next;
+                kind_of[next] = (uint8_t)k;
                 if (k == 0) out.heavy[hp++] = (uint32_t)next;
                 next++;
             }
@@ -284,6 +307,18 @@ void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium
                 out.chunks[cp++] = make_uint2((uint32_t)(first + i), c | flag);
             }
         }
+    });
+    const uint64_t words = (n + 31) / 32;
+    out.light_bits.assign(words, 0u);
+    out.medium_bits.assign(words, 0u);
+    parallel(words, [&](uint64_t wi) {
+        uint32_t lb = 0, mb = 0;
+        for (uint64_t v = wi * 32; v < std::min<uint64_t>(n, wi * 32 + 32); v++) {
+            if (kind_of[v] == 2) lb |= 1u << (v & 31);
+            if (kind_of[v] == 1) mb |= 1u << (v & 31);
+        }
+        out.light_bits[wi] = lb;
+        out.medium_bits[wi] = mb;
     });
     std::stable_sort(out.heavy.begin(), out.heavy.end(), [&](uint32_t x, uint32_t y) {
         const uint32_t ux = out.perm[x], uy = out.perm[y];
@@ -481,6 +516,7 @@ int do_init(hb_handle* h) {
     h->pending_visited = h->m - h->self_loops;
     hbk::InitArgs ia{};
     ia.perm = h->d_perm;
+    ia.hash_id = h->d_hash_id;
     ia.curr = h->d_cnt[0];
     ia.est = h->d_est;
     ia.n = n;
@@ -517,6 +553,16 @@ int do_init(hb_handle* h) {
     h->relative_increment = 0.0;
     h->nf.assign(1, h->last);
     h->stats.clear();
+    const size_t ni = h->inst_start.empty() ? 0 : h->inst_start.size() - 1;
+    h->inst_iters.assign(ni, 0);
+    h->inst_done.assign(ni, 0);
+    h->inst_nf.assign(ni, std::vector<double>());
+    for (size_t i = 0; i < ni; i++) {
+        const uint64_t ni_nodes = h->inst_start[i + 1] - h->inst_start[i];
+        h->inst_nf[i].assign(1, (double)ni_nodes);
+        // run() caps the iterations at the number of nodes (HB:541)
+        h->inst_done[i] = ni_nodes == 0;
+    }
     h->initialised = true;
     return HB_OK;
 }
@@ -556,7 +602,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     a.gather_all = !h->systolic && prev_mod >= n - n / 8;
     if (h->systolic && h->n_tiles) {
         // the chunks of the windows holding a node to check or to copy
-        HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_win_medium, h->d_win_light, n,
+        HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_medium_bits, h->d_light_bits, n,
                                             h->d_word_cnt, h->d_word_off, h->d_list_scratch,
                                             h->list_scratch_len, h->d_light_list,
                                             h->d_medium_list, s));
@@ -578,6 +624,15 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     // the neighbourhood-function parts, in a fixed order, into partials[0].nf
     HB_LAUNCH(h, hbk::launch_sum_f64(h->d_nf_items, h->n_chunks + h->n_heavy, h->d_nf_scratch,
                                      &h->d_partials[0].nf, s));
+    const size_t n_inst = h->inst_start.empty() ? 0 : h->inst_start.size() - 1;
+    if (n_inst) {
+        HB_LAUNCH(h, hbk::launch_inst_stats(h->d_bits[h->mod_cur ^ 1], h->d_est, h->d_inst_start,
+                                            (uint32_t)n_inst, h->d_inst_mod, h->d_inst_nf, s));
+        h->inst_mod.resize(n_inst);
+        h->inst_sum.resize(n_inst);
+        HB_CUDA(h, cudaMemcpyAsync(h->inst_mod.data(), h->d_inst_mod, n_inst * 8, cudaMemcpyDeviceToHost, s));
+        HB_CUDA(h, cudaMemcpyAsync(h->inst_sum.data(), h->d_inst_nf, n_inst * 8, cudaMemcpyDeviceToHost, s));
+    }
     hbk::TilePartial tot{};
     HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partials, sizeof(tot), cudaMemcpyDeviceToHost, s));
     HB_CUDA(h, cudaEventRecord(h->ev[3], s));
@@ -603,6 +658,17 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     h->relative_increment = current_nf / last_output;
     h->nf.push_back(current_nf);
     h->iteration += 1;
+    // batch instances still running: the reference's output for each
+    // (HB:916-944: monotone neighbourhood function; it stops after the first
+    // iteration that modifies no counter of the instance)
+    for (size_t i = 0; i < n_inst; i++) {
+        if (h->inst_done[i]) continue;
+        std::vector<double>& f = h->inst_nf[i];
+        f.push_back(std::max(h->inst_sum[i], f.back()));
+        h->inst_iters[i] = h->iteration;
+        const uint64_t ni_nodes = h->inst_start[i + 1] - h->inst_start[i];
+        if (h->inst_mod[i] == 0 || h->iteration >= ni_nodes) h->inst_done[i] = 1;
+    }
 
     hb_iter_stats st{};
     st.iteration = h->iteration;
@@ -640,21 +706,51 @@ int copy_d2h(const hb_handle* h, const void* src, void* dst, size_t bytes) {
     return HB_OK;
 }
 
-// A per-node device array (device node order) into caller order on the host.
-int copy_nodes_d2h(const hb_handle* h, const double* src, double* dst) {
+// Caller nodes [start, start + count) of a per-node device array (device node
+// order) into dst on the host, in caller order.
+int copy_nodes_range(const hb_handle* h, const double* src, double* dst, uint64_t start,
+                     uint64_t count) {
     hb_handle* hh = const_cast<hb_handle*>(h);
-    if (h->n == 0) return HB_OK;
+    if (count == 0) return HB_OK;
     HB_CUDA(hh, cudaSetDevice(h->device));
     double* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&tmp, h->n * 8, h->stream);
+    cudaError_t e = cudaMallocAsync((void**)&tmp, count * 8, h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return cuda_err(hh, e, "cudaMallocAsync");
     }
-    int r = hbk::launch_gather_f64(src, h->d_inv, tmp, h->n, h->stream);
-    if (r == 0) r = copy_d2h(h, tmp, dst, h->n * 8);
+    int r = hbk::launch_gather_f64(src, h->d_inv + start, tmp, count, h->stream);
+    if (r == 0) r = copy_d2h(h, tmp, dst, count * 8);
     else r = cuda_err(hh, (cudaError_t)r, "launch_gather_f64");
     cudaFreeAsync(tmp, h->stream);
+    cudaStreamSynchronize(h->stream);
+    return r;
+}
+
+// A per-node device array into caller order on the host.
+int copy_nodes_d2h(const hb_handle* h, const double* src, double* dst) {
+    return copy_nodes_range(h, src, dst, 0, h->n);
+}
+
+// Counters of caller nodes [start, start + count) of one state, packed in the
+// reference layout, into dst (count * counter_bytes bytes).
+int copy_registers_range(const hb_handle* h, int which, void* dst, uint64_t start, uint64_t count) {
+    if (count == 0) return HB_OK;
+    const int idx = which == HB_CURRENT_STATE ? h->cur : (h->cur ^ 1);
+    hb_handle* hh = const_cast<hb_handle*>(h);
+    HB_CUDA(hh, cudaSetDevice(h->device));
+    const size_t bytes = count * h->counter_bytes;
+    void* packed = nullptr;
+    cudaError_t e = cudaMallocAsync(&packed, bytes, h->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_err(hh, e, "cudaMallocAsync");
+    }
+    int r = hbk::launch_pack_counters(h->log2m, h->d_cnt[idx], h->d_inv + start, (uint8_t*)packed,
+                                      count, h->stream);
+    if (r == 0) r = copy_d2h(h, packed, dst, bytes);
+    else r = cuda_err(hh, (cudaError_t)r, "launch_pack_counters");
+    cudaFreeAsync(packed, h->stream);
     cudaStreamSynchronize(h->stream);
     return r;
 }
@@ -677,6 +773,252 @@ void hb_options_default(hb_options* o) {
     o->hash_kind = HB_HASH_SIP13;
     o->small_max_degree = HB_AUTO;
     o->medium_max_degree = HB_AUTO;
+}
+
+// ---- batches ------------------------------------------------------------------
+static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpose,
+                       const hb_options* opts, const std::vector<uint64_t>* inst, hb_handle** out);
+
+// Instances with the same log2m run as one disjoint union of their graphs
+// (instance i's nodes are a contiguous id range; an arc never leaves its
+// instance), so every iteration of the union is one pass of the union kernels
+// over all of them. The counters, and therefore every output, of an instance
+// do not depend on the others; the mode of an iteration (standard, systolic,
+// local) changes only which nodes are scanned, not the counters. Each
+// instance hashes its own node ids and reports its own neighbourhood function
+// and iteration count (the first iteration that modifies none of its
+// counters).
+struct hb_batch {
+    struct Group {
+        hb_handle* h = nullptr;
+        cudaStream_t stream = nullptr;
+        bool own_stream = false;
+    };
+    struct Member {
+        uint32_t group = 0, inst = 0;
+        uint64_t start = 0, n = 0;
+    };
+    std::vector<Group> groups;
+    std::vector<Member> members;
+    int device = 0;
+    bool ran = false;
+};
+
+static void batch_free(hb_batch* b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    for (auto& g : b->groups) {
+        if (g.h) hb_destroy(g.h);
+        if (g.own_stream && g.stream) cudaStreamDestroy(g.stream);
+    }
+    delete b;
+}
+
+int hb_batch_create(const hb_graph_view* graphs, uint32_t count, const int32_t* log2m,
+                    const hb_options* opts, hb_batch** out) {
+    if (!out) return set_err(nullptr, HB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!graphs || !log2m || count == 0)
+        return set_err(nullptr, HB_ERR_INVALID, "graphs and log2m must hold count > 0 entries");
+    hb_options o;
+    hb_options_default(&o);
+    if (opts) {
+        if (opts->struct_size != sizeof(hb_options))
+            return set_err(nullptr, HB_ERR_INVALID, "hb_options.struct_size mismatch");
+        o = *opts;
+    }
+    if (o.weights) return set_err(nullptr, HB_ERR_INVALID, "weights are not supported in batches");
+    std::string why;
+    std::map<int, std::vector<uint32_t>> by_log2m;
+    for (uint32_t i = 0; i < count; i++) {
+        if (!check_view(&graphs[i], why))
+            return set_err(nullptr, HB_ERR_INVALID, "graph " + std::to_string(i) + ": " + why);
+        if (log2m[i] < 4 || log2m[i] > 10)
+            return set_err(nullptr, HB_ERR_INVALID, "graph " + std::to_string(i) + ": log2m must be in [4, 10]");
+        by_log2m[log2m[i]].push_back(i);
+    }
+    std::unique_ptr<hb_batch, void (*)(hb_batch*)> b(new hb_batch(), batch_free);
+    b->device = o.device;
+    b->members.resize(count);
+    cudaError_t ce = cudaSetDevice(o.device);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_NO_DEVICE, "no CUDA device available (this library has no CPU path)");
+    }
+    for (auto& kv : by_log2m) {
+        const std::vector<uint32_t>& idx = kv.second;
+        // the disjoint union: instance k's nodes start at inst[k]
+        std::vector<uint64_t> inst(idx.size() + 1, 0), arc0(idx.size() + 1, 0);
+        for (size_t k = 0; k < idx.size(); k++) {
+            inst[k + 1] = inst[k] + graphs[idx[k]].num_nodes;
+            arc0[k + 1] = arc0[k] + graphs[idx[k]].num_arcs;
+        }
+        const uint64_t n = inst.back(), m = arc0.back();
+        if (n > 0xffffffffull)
+            return set_err(nullptr, HB_ERR_INVALID, "a batch group has more than 2^32 nodes");
+        std::vector<uint64_t> off(n + 1);
+        std::vector<uint32_t> succ(m);
+        {
+            const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+            const size_t nt = std::min<size_t>(std::min<size_t>(hw, 64), idx.size());
+            std::vector<std::thread> th;
+            for (size_t t = 0; t < nt; t++)
+                th.emplace_back([&, t] {
+                    for (size_t k = idx.size() * t / nt; k < idx.size() * (t + 1) / nt; k++) {
+                        const hb_graph_view& gv = graphs[idx[k]];
+                        for (uint64_t v = 0; v < gv.num_nodes; v++) off[inst[k] + v] = arc0[k] + gv.offsets[v];
+                        for (uint64_t e = 0; e < gv.num_arcs; e++)
+                            succ[arc0[k] + e] = (uint32_t)(gv.successors[e] + inst[k]);
+                    }
+                });
+            for (auto& x : th) x.join();
+        }
+        off[n] = m;
+        hb_graph_view uv{n, m, off.data(), succ.data()};
+        hb_batch::Group g;
+        if (o.stream) {
+            g.stream = (cudaStream_t)o.stream;
+        } else {
+            ce = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+            if (ce != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(nullptr, HB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+            }
+            g.own_stream = true;
+        }
+        hb_options go = o;
+        go.log2m = kv.first;
+        go.stream = g.stream;
+        go.num_elements = 0;
+        b->groups.push_back(g);
+        int r = create_impl(&uv, nullptr, &go, &inst, &b->groups.back().h);
+        if (r) return r;
+        for (size_t k = 0; k < idx.size(); k++) {
+            hb_batch::Member& mb = b->members[idx[k]];
+            mb.group = (uint32_t)(b->groups.size() - 1);
+            mb.inst = (uint32_t)k;
+            mb.start = inst[k];
+            mb.n = inst[k + 1] - inst[k];
+        }
+    }
+    *out = b.release();
+    return HB_OK;
+}
+
+void hb_batch_destroy(hb_batch* b) { batch_free(b); }
+
+int hb_batch_run_until_done(hb_batch* b) {
+    if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
+    // groups run side by side, each on its own stream
+    std::vector<int> rc(b->groups.size(), HB_OK);
+    std::vector<std::string> msg(b->groups.size());
+    std::vector<std::thread> th;
+    for (size_t gi = 0; gi < b->groups.size(); gi++)
+        th.emplace_back([&, gi] {
+            cudaSetDevice(b->device);
+            rc[gi] = hb_run_until_done(b->groups[gi].h);
+            if (rc[gi]) msg[gi] = b->groups[gi].h->err;
+        });
+    for (auto& x : th) x.join();
+    for (size_t gi = 0; gi < b->groups.size(); gi++)
+        if (rc[gi]) return set_err(nullptr, rc[gi], msg[gi]);
+    b->ran = true;
+    return HB_OK;
+}
+
+static int batch_member(const hb_batch* b, uint32_t graph, const hb_batch::Member** mb,
+                        const hb_handle** h) {
+    if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
+    if (graph >= b->members.size()) return set_err(nullptr, HB_ERR_INVALID, "graph index out of range");
+    if (!b->ran)
+        return set_err(nullptr, HB_ERR_NOT_RUN,
+                       "HyperBall was not run. Please call hb_batch_run_until_done before accessing computed fields");
+    *mb = &b->members[graph];
+    *h = b->groups[(*mb)->group].h;
+    return HB_OK;
+}
+
+// as ensure_iteration (HB:624-630) for one instance: a graph that ran no
+// iteration (no nodes) has no computed fields
+static int batch_ran(const hb_handle* h, const hb_batch::Member* mb) {
+    if (h->inst_iters[mb->inst] == 0)
+        return set_err(nullptr, HB_ERR_NOT_RUN,
+                       "HyperBall was not run. Please call hb_batch_run_until_done before accessing computed fields");
+    return HB_OK;
+}
+
+uint32_t hb_batch_num_graphs(const hb_batch* b) { return b ? (uint32_t)b->members.size() : 0; }
+
+uint64_t hb_batch_num_iterations(const hb_batch* b, uint32_t graph) {
+    const hb_batch::Member* mb;
+    const hb_handle* h;
+    if (batch_member(b, graph, &mb, &h)) return 0;
+    return h->inst_iters[mb->inst];
+}
+
+int hb_batch_get_neighborhood_function(const hb_batch* b, uint32_t graph, double* dst,
+                                       size_t capacity, size_t* len) {
+    const hb_batch::Member* mb;
+    const hb_handle* h;
+    int r = batch_member(b, graph, &mb, &h);
+    if (r || (r = batch_ran(h, mb))) return r;
+    const std::vector<double>& f = h->inst_nf[mb->inst];
+    if (len) *len = f.size();
+    if (dst) std::copy(f.begin(), f.begin() + std::min(capacity, f.size()), dst);
+    return HB_OK;
+}
+
+static int batch_sums(const hb_batch* b, uint32_t graph, double* dst, size_t len, bool harm) {
+    const hb_batch::Member* mb;
+    const hb_handle* h;
+    int r = batch_member(b, graph, &mb, &h);
+    if (r || (r = batch_ran(h, mb))) return r;
+    const double* src = harm ? h->d_harm : h->d_sod;
+    if (!src)
+        return set_err(nullptr, HB_ERR_NOT_REQUESTED,
+                       harm ? "Sum of inverse distances were not requested. Set HB_SUM_OF_INVERSE_DISTANCES while building the batch"
+                            : "Sum of distances were not requested. Set HB_SUM_OF_DISTANCES while building the batch");
+    if (!dst || len != mb->n)
+        return set_err(nullptr, HB_ERR_INVALID, "output length must equal the graph's num_nodes");
+    return copy_nodes_range(h, src, dst, mb->start, mb->n);
+}
+
+int hb_batch_get_sum_of_distances(const hb_batch* b, uint32_t graph, double* dst, size_t len) {
+    return batch_sums(b, graph, dst, len, false);
+}
+
+int hb_batch_get_harmonic_centralities(const hb_batch* b, uint32_t graph, double* dst, size_t len) {
+    return batch_sums(b, graph, dst, len, true);
+}
+
+int hb_batch_get_registers(const hb_batch* b, uint32_t graph, void* dst, size_t bytes) {
+    const hb_batch::Member* mb;
+    const hb_handle* h;
+    int r = batch_member(b, graph, &mb, &h);
+    if (r) return r;
+    if (!dst || bytes != mb->n * h->counter_bytes)
+        return set_err(nullptr, HB_ERR_INVALID, "bytes must be the graph's num_nodes * counter bytes");
+    return copy_registers_range(h, HB_CURRENT_STATE, dst, mb->start, mb->n);
+}
+
+int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_arcs,
+                   uint64_t* register_updates, double* device_ms) {
+    if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
+    uint64_t it = 0, vis = 0, upd = 0;
+    double ms = 0.0;
+    for (const auto& g : b->groups) {
+        it = std::max<uint64_t>(it, g.h->iteration);
+        for (const auto& s : g.h->stats) {
+            vis += s.visited_arcs;
+            upd += s.visited_arcs << g.h->log2m;
+            ms += s.iteration_ms;
+        }
+    }
+    if (iterations) *iterations = it;
+    if (visited_arcs) *visited_arcs = vis;
+    if (register_updates) *register_updates = upd;
+    if (device_ms) *device_ms = ms;
+    return HB_OK;
 }
 
 // ---- device CSR utilities ----------------------------------------------------
@@ -788,8 +1130,10 @@ uint64_t hb_kernel_launches(const hb_handle* h) { return h ? h->launches : 0; }
 const char* hb_global_last_error(void) { return g_global_err.c_str(); }
 const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_global_err.c_str(); }
 
-int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const hb_options* opts,
-              hb_handle** out) {
+// hb_create, optionally for a batch: `inst` holds the instance starts (caller
+// ids, ascending, starting at 0) followed by num_nodes.
+static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpose,
+                       const hb_options* opts, const std::vector<uint64_t>* inst, hb_handle** out) {
     if (!out) return set_err(nullptr, HB_ERR_INVALID, "out is NULL");
     *out = nullptr;
     hb_options o;
@@ -824,6 +1168,7 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         return set_err(nullptr, HB_ERR_INVALID, "unknown hash_kind");
 
     std::unique_ptr<hb_handle> h(new hb_handle());
+    if (inst) h->inst_start = *inst;
     h->device = o.device;
     h->stream = (cudaStream_t)o.stream;
     h->n = graph->num_nodes;
@@ -894,7 +1239,8 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
         hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
         WorkPartition wp;
-        build_partition(graph, h->small_max, h->medium_max, win_nodes, per_light, per_medium, wp);
+        build_partition(graph, h->small_max, h->medium_max, win_nodes, per_light, per_medium,
+                        h->inst_start, wp);
         h->n_tiles = h->n ? wp.tiles.size() - 1 : 0;
         h->n_chunks = wp.chunks.size();
         h->n_heavy = wp.heavy.size();
@@ -911,8 +1257,8 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         if ((r = upload(&h->d_perm, wp.perm))) return fail(r);
         if ((r = upload(&h->d_inv, wp.inv))) return fail(r);
         if (h->n_heavy && (r = upload(&h->d_heavy, wp.heavy))) return fail(r);
-        if ((r = upload(&h->d_win_medium, wp.win_medium))) return fail(r);
-        if ((r = upload(&h->d_win_light, wp.win_light))) return fail(r);
+        if ((r = upload(&h->d_medium_bits, wp.medium_bits))) return fail(r);
+        if ((r = upload(&h->d_light_bits, wp.light_bits))) return fail(r);
         const uint64_t words = (h->n + 31) / 32;
         if ((r = dalloc(hp, &h->d_word_cnt, words + 1))) return fail(r);
         if ((r = dalloc(hp, &h->d_word_off, words + 1))) return fail(r);
@@ -920,6 +1266,18 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
         if ((r = dalloc(hp, &h->d_list_scratch, h->list_scratch_len))) return fail(r);
         if ((r = dalloc(hp, &h->d_light_list, h->n + 1))) return fail(r);
         if ((r = dalloc(hp, &h->d_medium_list, h->n + 1))) return fail(r);
+        if (!h->inst_start.empty()) {
+            // batch: each instance hashes its own node ids, and reports per instance
+            const size_t ni = h->inst_start.size() - 1;
+            std::vector<uint32_t> hid(h->n);
+            for (size_t i = 0; i < ni; i++)
+                for (uint64_t u = h->inst_start[i]; u < h->inst_start[i + 1]; u++)
+                    hid[wp.inv[u]] = (uint32_t)(u - h->inst_start[i]);
+            if ((r = upload(&h->d_hash_id, hid))) return fail(r);
+            if ((r = upload(&h->d_inst_start, h->inst_start))) return fail(r);
+            if ((r = dalloc(hp, &h->d_inst_mod, ni))) return fail(r);
+            if ((r = dalloc(hp, &h->d_inst_nf, ni))) return fail(r);
+        }
         h->inv_host = std::move(wp.inv);
     }
     {
@@ -1004,6 +1362,11 @@ int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const 
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     *out = h.release();
     return HB_OK;
+}
+
+int hb_create(const hb_graph_view* graph, const hb_graph_view* transpose, const hb_options* opts,
+              hb_handle** out) {
+    return create_impl(graph, transpose, opts, nullptr, out);
 }
 
 int hb_add_discount_function(hb_handle* h, hb_discount_fn fn, void* ctx) {
@@ -1168,24 +1531,8 @@ int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes) {
         return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "bytes must be num_nodes * counter bytes");
     if (which != HB_CURRENT_STATE && which != HB_NEXT_STATE)
         return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "which must be HB_CURRENT_STATE or HB_NEXT_STATE");
-    const int idx = which == HB_CURRENT_STATE ? h->cur : (h->cur ^ 1);
-    if (bytes == 0) return HB_OK;
     // the device keeps a byte per register; pack into the reference's layout
-    hb_handle* hh = const_cast<hb_handle*>(h);
-    HB_CUDA(hh, cudaSetDevice(h->device));
-    void* packed = nullptr;
-    cudaError_t e = cudaMallocAsync(&packed, bytes, h->stream);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return cuda_err(hh, e, "cudaMallocAsync");
-    }
-    int r = hbk::launch_pack_counters(h->log2m, h->d_cnt[idx], h->d_inv, (uint8_t*)packed, h->n,
-                                      h->stream);
-    if (r == 0) r = copy_d2h(h, packed, dst, bytes);
-    else r = cuda_err(hh, (cudaError_t)r, "launch_pack_counters");
-    cudaFreeAsync(packed, h->stream);
-    cudaStreamSynchronize(h->stream);
-    return r;
+    return copy_registers_range(h, which, dst, 0, h->n);
 }
 
 int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* reg_size) {

@@ -92,6 +92,7 @@ struct UnionArgs {
 
 struct InitArgs {
     const uint32_t* perm;     // device node -> caller node (the id that is hashed)
+    const uint32_t* hash_id;  // batches: device node -> id hashed (its instance's own id), or null
     uint8_t* curr;
     double* est;
     uint64_t n;
@@ -132,14 +133,17 @@ int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);
 // heavy nodes, one CTA each
 int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream);
 int heavy_grid(int log2m, int device);
+// batches: per instance [starts[i], starts[i+1]) the modified counters of the
+// iteration (next_mod) and the sum of the cached estimates
+int launch_inst_stats(const uint32_t* next_mod, const double* est, const uint64_t* starts,
+                      uint32_t count, unsigned long long* mods, double* nfs, void* stream);
 // fixed-order sum of count doubles into *out (scratch: 256 doubles)
 int launch_sum_f64(const double* in, uint64_t count, double* scratch, double* out, void* stream);
 // systolic work lists: every light / medium node set in mbc | curr_mod, in
-// node order (win_medium[w], win_light[w]: first medium / light node of
-// window w). cnt and off hold nwords + 1 words; off[nwords] gets the counts
-// (light | medium << 32).
-int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* win_medium,
-                      const uint32_t* win_light, uint64_t n, unsigned long long* cnt, uint64_t* off,
+// node order (medium_bits / light_bits: the medium / light nodes). cnt and
+// off hold nwords + 1 words; off[nwords] gets the counts (light | medium << 32).
+int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* medium_bits,
+                      const uint32_t* light_bits, uint64_t n, unsigned long long* cnt, uint64_t* off,
                       unsigned long long* scratch, uint64_t scratch_len, uint32_t* light_list,
                       uint32_t* medium_list, void* stream);
 // nodes per chunk of the union kernel: light nodes (lane-group each) and

@@ -701,7 +701,8 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
          v += (uint64_t)gridDim.x * blockDim.x) {
         uint8_t* counter = a.curr + v * (uint64_t)Gm::COUNTER_BYTES;
         if (a.weights == nullptr) {
-            const uint64_t u = __ldg(a.perm + v);  // the caller's id is hashed
+            // the caller's id is hashed (an instance's own id in a batch)
+            const uint64_t u = a.hash_id ? __ldg(a.hash_id + v) : __ldg(a.perm + v);
             const uint64_t x = a.hash_kind == 1 ? hash_jenkins(u, a.seed) : hash_sip13(u);
             const uint32_t val = add_hash<LOG2M>(counter, x);
             saw31 |= val == 31u;
@@ -713,7 +714,7 @@ __global__ void __launch_bounds__(256) k_init(InitArgs a) {
         } else {
             // HB:1167-1174 adds random values; here value k of node v is
             // SplitMix64 step k from weight_seed ^ v * golden, hashed as usual.
-            const uint64_t u = __ldg(a.perm + v);
+            const uint64_t u = a.hash_id ? __ldg(a.hash_id + v) : __ldg(a.perm + v);
             uint64_t s = a.weight_seed ^ (u * 0x9e3779b97f4a7c15ull);
             const uint64_t w = a.weights[u];
             for (uint64_t k = 0; k < w; k++) {
@@ -809,6 +810,35 @@ __global__ void k_sum_f64(const double* __restrict__ in, uint64_t count, double*
         __syncthreads();
     }
     if (threadIdx.x == 0) out[blockIdx.x] = s[0];
+}
+
+// ---------------------------------------------------------------------------
+// batches: per instance (a device id range) the number of modified counters
+// and the neighbourhood function (sum of the cached estimates) of the
+// iteration just run; one warp per instance, fixed order
+// ---------------------------------------------------------------------------
+__global__ void k_inst_stats(const uint32_t* __restrict__ next_mod, const double* __restrict__ est,
+                             const uint64_t* __restrict__ starts, uint32_t count,
+                             unsigned long long* __restrict__ mods, double* __restrict__ nfs) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t i = gw; i < count; i += nw) {
+        const uint64_t b = __ldg(starts + i), e = __ldg(starts + i + 1);
+        unsigned long long mc = 0;
+        double s = 0.0;
+        for (uint64_t v = b + lane; v < e; v += 32) {
+            s = __dadd_rn(s, est[v]);
+            mc += (__ldg(next_mod + (v >> 5)) >> (v & 31)) & 1u;
+        }
+        s = warp_sum_f64(s);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) mc += __shfl_xor_sync(0xffffffffu, mc, off);
+        if (lane == 0) {
+            mods[i] = mc;
+            nfs[i] = s;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -916,22 +946,16 @@ __global__ void k_reduce_partials(const TilePartial* __restrict__ in, uint64_t c
 
 // Systolic iterations: flags the windows holding a node that must be checked
 // or copied; the union kernel skips the chunks of the other windows.
-// bits of word i (nodes 32i .. 32i+31, all in one window) split into light
-// and medium nodes
-__device__ __forceinline__ void split_word(uint64_t i, uint32_t bits, const uint32_t* win_medium,
-                                           const uint32_t* win_light, uint32_t& lb, uint32_t& mb) {
-    const uint64_t lo = i << 5, w = lo / WINDOW;
-    const uint64_t ms = __ldg(win_medium + w), ls = __ldg(win_light + w);
-    auto from = [&](uint64_t x) -> uint32_t {  // bits of nodes >= x
-        return x <= lo ? 0xffffffffu : x >= lo + 32 ? 0u : 0xffffffffu << (uint32_t)(x - lo);
-    };
-    lb = bits & from(ls);
-    mb = bits & from(ms) & ~from(ls);
+// bits of word i split into light and medium nodes
+__device__ __forceinline__ void split_word(uint64_t i, uint32_t bits, const uint32_t* medium_bits,
+                                           const uint32_t* light_bits, uint32_t& lb, uint32_t& mb) {
+    lb = bits & __ldg(light_bits + i);
+    mb = bits & __ldg(medium_bits + i);
 }
 
 __global__ void k_list_count(const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
-                             const uint32_t* __restrict__ win_medium,
-                             const uint32_t* __restrict__ win_light, uint64_t nwords,
+                             const uint32_t* __restrict__ medium_bits,
+                             const uint32_t* __restrict__ light_bits, uint64_t nwords,
                              unsigned long long* __restrict__ cnt) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nwords;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -940,20 +964,20 @@ __global__ void k_list_count(const uint32_t* __restrict__ mbc, const uint32_t* _
             continue;
         }
         uint32_t lb, mb;
-        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), win_medium, win_light, lb, mb);
+        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), medium_bits, light_bits, lb, mb);
         cnt[i] = (unsigned long long)__popc(lb) | ((unsigned long long)__popc(mb) << 32);
     }
 }
 
 __global__ void k_list_fill(const uint32_t* __restrict__ mbc, const uint32_t* __restrict__ curr_mod,
-                            const uint32_t* __restrict__ win_medium,
-                            const uint32_t* __restrict__ win_light, uint64_t nwords,
+                            const uint32_t* __restrict__ medium_bits,
+                            const uint32_t* __restrict__ light_bits, uint64_t nwords,
                             const uint64_t* __restrict__ off, uint32_t* __restrict__ light_list,
                             uint32_t* __restrict__ medium_list) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t lb, mb;
-        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), win_medium, win_light, lb, mb);
+        split_word(i, __ldg(mbc + i) | __ldg(curr_mod + i), medium_bits, light_bits, lb, mb);
         const uint64_t o = off[i];
         uint32_t ol = (uint32_t)o, om = (uint32_t)(o >> 32);
         const uint32_t lo = (uint32_t)(i << 5);
@@ -1167,6 +1191,14 @@ int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, u
     return (int)cudaGetLastError();
 }
 
+int launch_inst_stats(const uint32_t* next_mod, const double* est, const uint64_t* starts,
+                      uint32_t count, unsigned long long* mods, double* nfs, void* stream) {
+    const int grid = (int)std::min<uint64_t>(((uint64_t)count * 32 + 255) / 256 + 1, 8192);
+    ++t_launches;
+    k_inst_stats<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, est, starts, count, mods, nfs);
+    return (int)cudaGetLastError();
+}
+
 int launch_sum_f64(const double* in, uint64_t count, double* scratch, double* out, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     ++t_launches;
@@ -1246,21 +1278,21 @@ int chunk_nodes(int log2m, uint32_t* light, uint32_t* medium) {
 #undef CALL
 }
 
-int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* win_medium,
-                      const uint32_t* win_light, uint64_t n, unsigned long long* cnt, uint64_t* off,
+int launch_work_lists(const uint32_t* mbc, const uint32_t* curr_mod, const uint32_t* medium_bits,
+                      const uint32_t* light_bits, uint64_t n, unsigned long long* cnt, uint64_t* off,
                       unsigned long long* scratch, uint64_t scratch_len, uint32_t* light_list,
                       uint32_t* medium_list, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const uint64_t nwords = (n + 31) / 32;
     const int grid = (int)std::min<uint64_t>((nwords + 256) / 256 + 1, 8192);
     ++t_launches;
-    k_list_count<<<grid, 256, 0, s>>>(mbc, curr_mod, win_medium, win_light, nwords, cnt);
+    k_list_count<<<grid, 256, 0, s>>>(mbc, curr_mod, medium_bits, light_bits, nwords, cnt);
     int e = (int)cudaGetLastError();
     if (e) return e;
     e = launch_exclusive_scan_u64(cnt, off, nwords + 1, scratch, scratch_len, stream);
     if (e) return e;
     ++t_launches;
-    k_list_fill<<<grid, 256, 0, s>>>(mbc, curr_mod, win_medium, win_light, nwords, off, light_list,
+    k_list_fill<<<grid, 256, 0, s>>>(mbc, curr_mod, medium_bits, light_bits, nwords, off, light_list,
                                      medium_list);
     return (int)cudaGetLastError();
 }

@@ -180,6 +180,21 @@ EXPORTS = [
     ("hb_graph_free", None, [_H]),
     ("hb_version", ctypes.c_char_p, []),
     ("hb_kernel_launches", ctypes.c_uint64, [_H]),
+    ("hb_batch_create", ctypes.c_int,
+     [_P(GraphView), ctypes.c_uint32, _P(ctypes.c_int32), _P(Options), _P(_H)]),
+    ("hb_batch_run_until_done", ctypes.c_int, [_H]),
+    ("hb_batch_num_graphs", ctypes.c_uint32, [_H]),
+    ("hb_batch_num_iterations", ctypes.c_uint64, [_H, ctypes.c_uint32]),
+    ("hb_batch_get_neighborhood_function", ctypes.c_int,
+     [_H, ctypes.c_uint32, _P(ctypes.c_double), ctypes.c_size_t, _P(ctypes.c_size_t)]),
+    ("hb_batch_get_sum_of_distances", ctypes.c_int,
+     [_H, ctypes.c_uint32, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_batch_get_harmonic_centralities", ctypes.c_int,
+     [_H, ctypes.c_uint32, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_batch_get_registers", ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t]),
+    ("hb_batch_stats", ctypes.c_int,
+     [_H, _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_double)]),
+    ("hb_batch_destroy", None, [_H]),
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
@@ -643,3 +658,93 @@ class HyperBall:
         out = np.zeros((self.num_nodes, self.counter_bytes), dtype=np.uint8)
         _check(self._lib.hb_get_registers(self._h, which, out.ctypes.data, out.nbytes), self._h)
         return out
+
+
+# ---------------------------------------------------------------------------
+# batches (no reference counterpart): many independent instances in one pass
+# ---------------------------------------------------------------------------
+class HyperBallBatch:
+    """Independent HyperBall instances run together: graphs[i] with log2m[i];
+    the hasher and the requested outputs are shared. For each graph the
+    results equal those of HyperBallBuilder(...).build().run_until_done()."""
+
+    def __init__(self, graphs, log2ms, hasher=None, sum_of_distances=False,
+                 sum_of_inverse_distances=False, transpose_on_device=True, device=0,
+                 stream=None):
+        lib = load_library()
+        self._lib = lib
+        self._graphs = list(graphs)
+        if len(log2ms) != len(self._graphs):
+            raise InvalidArgumentError(HB_ERR_INVALID, "one log2m per graph")
+        hasher = hasher or DefaultHasher()
+        o = Options()
+        lib.hb_options_default(ctypes.byref(o))
+        o.hash_kind = hasher.kind
+        o.hash_seed = hasher.seed
+        o.device = device
+        o.stream = stream
+        flags = 0
+        if sum_of_distances:
+            flags |= HB_SUM_OF_DISTANCES
+        if sum_of_inverse_distances:
+            flags |= HB_SUM_OF_INVERSE_DISTANCES
+        if transpose_on_device:
+            flags |= HB_TRANSPOSE_ON_DEVICE
+        o.flags = flags
+        self._views = (GraphView * len(self._graphs))(*[g.view() for g in self._graphs])
+        self._log2m = (ctypes.c_int32 * len(self._graphs))(*[int(x) for x in log2ms])
+        self.num_nodes = [g.num_nodes for g in self._graphs]
+        self.counter_bytes = [(1 << int(x)) * 5 // 8 for x in log2ms]
+        h = ctypes.c_void_p()
+        _check(lib.hb_batch_create(self._views, len(self._graphs), self._log2m, ctypes.byref(o),
+                                   ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.hb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __len__(self):
+        return len(self._graphs)
+
+    def run_until_done(self):
+        _check(self._lib.hb_batch_run_until_done(self._h))
+
+    def iterations(self, i):
+        return int(self._lib.hb_batch_num_iterations(self._h, i))
+
+    def neighborhood_function(self, i):
+        n = ctypes.c_size_t()
+        _check(self._lib.hb_batch_get_neighborhood_function(self._h, i, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        _check(self._lib.hb_batch_get_neighborhood_function(
+            self._h, i, out.ctypes.data_as(_P(ctypes.c_double)), n.value, ctypes.byref(n)))
+        return out
+
+    def _vec(self, fn, i):
+        out = np.zeros(self.num_nodes[i], dtype=np.float64)
+        _check(fn(self._h, i, out.ctypes.data_as(_P(ctypes.c_double)), self.num_nodes[i]))
+        return out
+
+    def sum_of_distances(self, i):
+        return self._vec(self._lib.hb_batch_get_sum_of_distances, i)
+
+    def harmonic_centralities(self, i):
+        return self._vec(self._lib.hb_batch_get_harmonic_centralities, i)
+
+    def registers(self, i):
+        out = np.zeros((self.num_nodes[i], self.counter_bytes[i]), dtype=np.uint8)
+        _check(self._lib.hb_batch_get_registers(self._h, i, out.ctypes.data, out.size))
+        return out
+
+    def stats(self):
+        it, vis, upd, ms = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        _check(self._lib.hb_batch_stats(self._h, ctypes.byref(it), ctypes.byref(vis),
+                                        ctypes.byref(upd), ctypes.byref(ms)))
+        return {"iterations": it.value, "visited_arcs": vis.value, "register_updates": upd.value,
+                "device_ms": ms.value}
+
