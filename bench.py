@@ -52,11 +52,15 @@ def parse_args():
     p.add_argument("--log2n", type=int, default=26, help="graph size (2^log2n nodes)")
     p.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: --steps)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["weblike", "batched"], default="weblike",
-                   help="weblike: the 2^26 web-like graph (default); batched: many small graphs")
+    p.add_argument("--workload", choices=["weblike", "batched", "served"], default="weblike",
+                   help="weblike: the 2^26 web-like graph (default); batched: many small graphs; "
+                        "served: a Poisson stream of jobs through the job server")
     p.add_argument("--batch-count", type=int, default=4096, help="graphs in the batched workload")
     p.add_argument("--alone-sample", type=int, default=192,
                    help="graphs of the batch also run one at a time")
+    p.add_argument("--jobs", type=int, default=300, help="jobs of the served stream")
+    p.add_argument("--rate", type=float, default=200.0, help="job arrivals per second")
+    p.add_argument("--pool", type=int, default=48, help="distinct graphs the served jobs draw from")
     return p.parse_args()
 
 
@@ -526,12 +530,92 @@ def run_batched(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# served workload: a Poisson stream of jobs through the job server
+# ---------------------------------------------------------------------------
+def served_specs(count, pool, rate, seed=2025):
+    """Jobs of the stream: arrival time (Poisson, `rate` per second), a graph
+    of the pool and log2m in {4, 6, 8}. Pool graphs: node counts log-uniform in
+    [10^3, 10^7]; even ones R-MAT (.57,.19,.19,.05) with arcs per node uniform in
+    [4, 32] (2^scale nodes), odd ones web-like (mean out-degree 12)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    graphs = []
+    for i in range(pool):
+        n = int(round(10 ** rng.uniform(3.0, 7.0)))
+        if i % 2 == 0:
+            graphs.append(("rmat", int(round(np.log2(n))), int(rng.integers(4, 33)), 100 + i))
+        else:
+            graphs.append(("weblike", n, 12, 100 + i))
+    t, jobs = 0.0, []
+    for _ in range(count):
+        t += rng.exponential(1.0 / rate)
+        jobs.append((t, int(rng.integers(0, pool)), int(rng.choice([4, 6, 8]))))
+    return graphs, jobs
+
+
+def run_served(args):
+    import numpy as np
+    import hyperball_gb300 as hb
+    from concurrent.futures import ThreadPoolExecutor
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    gspecs, jobs = served_specs(args.jobs, args.pool, args.rate)
+
+    def make(sp):
+        kind, size, deg, seed = sp
+        if kind == "rmat":
+            return hb.Graph.rmat(size, deg, seed=seed)
+        return hb.Graph.weblike(size, seed=seed)
+
+    with ThreadPoolExecutor(max_workers=host_cores()) as ex:
+        graphs = list(ex.map(make, gspecs))
+    server = hb.HyperBallServer()
+    # warm-up: one job of each log2m
+    for l2m in (4, 6, 8):
+        j = server.submit(graphs[0], l2m, sum_of_distances=True, sum_of_inverse_distances=True)
+        server.wait(j)
+        server.release(j)
+    t0 = time.perf_counter()
+    ids = []
+    for at, gi, l2m in jobs:
+        delay = t0 + at - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(server.submit(graphs[gi], l2m, sum_of_distances=True, sum_of_inverse_distances=True))
+    for j in ids:
+        server.wait(j)
+    wall = time.perf_counter() - t0
+    infos = [server.info(j) for j in ids]
+    server.close()
+    lat = np.array([i["latency_ms"] for i in infos])
+    units = sum(i["register_updates"] for i in infos)
+    line = {
+        "metric": METRIC + " (served)", "value": units / wall, "unit": UNIT, "n_gpus": 1,
+        "steps": 1, "warmup": 3, "ms_per_step": 1e3 * wall, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{len(jobs)} jobs, Poisson arrivals at {args.rate}/s",
+                   "graphs": f"{len(graphs)} pool graphs, n log-uniform in [1e3, 1e7]; R-MAT with "
+                             "arcs/node U[4,32] or web-like; log2m in {4,6,8}",
+                   "budget_bytes": 150 * 10**9, "max_active": 16,
+                   "arcs_per_job_mean": float(np.mean([graphs[gi].num_arcs for _, gi, _ in jobs]))},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max())},
+        "queue_ms_p50": float(np.percentile([i["queue_ms"] for i in infos], 50)),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_gb300(args)
 
 

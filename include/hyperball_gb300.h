@@ -243,6 +243,68 @@ int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_ar
                    uint64_t* register_updates, double* device_ms);
 void hb_batch_destroy(hb_batch* b);
 
+/* ---- served jobs: continuous admission against a device-memory budget --------- */
+
+/* Job states. */
+#define HB_JOB_QUEUED 0
+#define HB_JOB_RUNNING 1
+#define HB_JOB_DONE 2
+#define HB_JOB_FAILED 3
+
+typedef struct hb_server hb_server;
+
+typedef struct hb_server_options {
+    uint32_t struct_size;      /* sizeof(hb_server_options) */
+    int32_t device;            /* CUDA device ordinal */
+    uint64_t hbm_budget_bytes; /* device bytes the running jobs may hold together; default 150e9 */
+    uint32_t max_active;       /* jobs on the device at once; default 16 */
+    uint32_t keep_registers;   /* 1: keep each finished job's counters for hb_server_get_registers */
+} hb_server_options;
+
+typedef struct hb_job_info {
+    int32_t state;             /* HB_JOB_* */
+    int32_t error;             /* status of a failed job */
+    uint64_t iterations;
+    uint64_t visited_arcs;     /* summed over the iterations */
+    uint64_t register_updates; /* visited arcs * 2^log2m */
+    uint64_t footprint_bytes;  /* device bytes reserved for the job */
+    double queue_ms;           /* submission to admission */
+    double run_ms;             /* admission to results on the host */
+    double latency_ms;         /* submission to results on the host */
+} hb_job_info;
+
+/* Fills defaults: device 0, 150 GB budget, 16 active jobs, no registers kept. */
+void hb_server_options_default(hb_server_options* opts);
+/* Starts a server. No reference counterpart. Jobs wait in arrival order. The
+ * head job is admitted when a slot is free and its device footprint fits the
+ * budget next to the running jobs. Each admitted job runs on its own stream,
+ * so running jobs overlap on the device. A job's results equal those of
+ * hb_create + hb_run_until_done on its graph alone. */
+int hb_server_create(const hb_server_options* opts, hb_server** out);
+/* Queues a job (the graph is copied; options as for hb_create, except that
+ * weights, the stream and the device come from the server). HB_ERR_INVALID
+ * when the job alone exceeds the budget. */
+int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options* opts,
+                     uint64_t* job);
+/* Waits until the job finished (timeout_s < 0: no limit); HB_ERR_TIMEOUT when
+ * the limit passed first, the job's own status when it failed. */
+int hb_server_wait(hb_server* s, uint64_t job, double timeout_s);
+int hb_server_job_info(hb_server* s, uint64_t job, hb_job_info* info);
+/* Results of a finished job, as the single-instance getters. */
+int hb_server_get_neighborhood_function(hb_server* s, uint64_t job, double* dst, size_t capacity,
+                                        size_t* len);
+int hb_server_get_sum_of_distances(hb_server* s, uint64_t job, double* dst, size_t len);
+int hb_server_get_harmonic_centralities(hb_server* s, uint64_t job, double* dst, size_t len);
+int hb_server_get_registers(hb_server* s, uint64_t job, void* dst, size_t bytes);
+/* Forgets a finished job and its host results. */
+int hb_server_release(hb_server* s, uint64_t job);
+/* Cancels queued jobs, waits for running ones, frees the server. */
+void hb_server_destroy(hb_server* s);
+/* Device bytes the server reserves for a job of this size. */
+uint64_t hb_job_footprint(uint64_t num_nodes, uint64_t num_arcs, int log2m);
+/* Last error of a server call on this thread (never NULL). */
+const char* hb_server_last_error(void);
+
 /* ---- device CSR utilities ----------------------------------------------------- */
 
 /* Transpose of a device-resident CSR graph: d_offsets[num_nodes + 1] and

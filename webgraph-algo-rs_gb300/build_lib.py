@@ -44,7 +44,7 @@ def _units():
         cmd = [os.path.join(cuda, "bin", "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17",
                "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj]
         units.append((src, obj, cmd))
-    for name in ("hb_engine.cpp", "graph_host.cpp"):
+    for name in ("hb_engine.cpp", "graph_host.cpp", "hb_server.cpp"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OBJ, name + ".o")
         cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall",

@@ -182,10 +182,13 @@ int dalloc(hb_handle* h, T** out, size_t count) {
     *out = nullptr;
     size_t bytes = std::max<size_t>(count * sizeof(T), 256);
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    // stream-ordered: freeing never synchronises the whole device, so other
+    // work (other handles, other jobs of a server) keeps running
+    cudaError_t e = cudaMallocAsync(&p, bytes, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return cuda_err(h, e, "cudaMalloc");
+        return cuda_err(h, e, "cudaMallocAsync");
     }
     h->bufs.push_back({p, bytes});
     *out = (T*)p;
@@ -194,7 +197,8 @@ int dalloc(hb_handle* h, T** out, size_t count) {
 
 void release(hb_handle* h) {
     if (!h) return;
-    for (auto& b : h->bufs) cudaFree(b.p);
+    for (auto& b : h->bufs) cudaFreeAsync(b.p, h->stream);
+    cudaStreamSynchronize(h->stream);
     h->bufs.clear();
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
@@ -375,7 +379,8 @@ int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t*
 void dfree(hb_handle* h, void* p) {
     for (auto it = h->bufs.begin(); it != h->bufs.end(); ++it)
         if (it->p == p) {
-            cudaFree(p);
+            cudaFreeAsync(p, h->stream);
+            cudaStreamSynchronize(h->stream);
             h->bufs.erase(it);
             return;
         }
@@ -434,14 +439,8 @@ int build_transpose_on_device(hb_handle* h) {
                               h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     // temporaries are released right away
-    for (auto it = h->bufs.begin(); it != h->bufs.end();) {
-        if (it->p == (void*)indeg || it->p == (void*)scratch) {
-            cudaFree(it->p);
-            it = h->bufs.erase(it);
-        } else {
-            ++it;
-        }
-    }
+    dfree(h, indeg);
+    dfree(h, scratch);
     h->has_transpose = true;
     return HB_OK;
 }

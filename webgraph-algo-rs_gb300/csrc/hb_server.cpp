@@ -1,0 +1,374 @@
+// HyperBall job server: continuous admission of independent HyperBall jobs
+// against a device-memory budget (no reference counterpart; each job returns
+// what HyperBallBuilder::build + run_until_done returns for its graph alone).
+//
+// Jobs wait in a FIFO queue. A scheduler thread admits the head job as soon as
+// a slot is free (at most max_active jobs on the device) and its estimated
+// device footprint fits the budget next to the jobs already running. Each
+// admitted job runs on its own CUDA stream from its own host thread, so the
+// iterations of all running jobs overlap on the device; when a job finishes,
+// its results are copied to the host, its device memory is released and the
+// scheduler admits the next jobs. Latency is measured from submission to the
+// moment the results are on the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "hb_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+    uint64_t id = 0;
+    Csr graph;
+    hb_options opts{};
+    uint64_t footprint = 0;
+    int state = HB_JOB_QUEUED;
+    int error = HB_OK;
+    std::string message;
+    Clock::time_point submitted, started, finished;
+    // results
+    uint64_t iterations = 0, visited_arcs = 0;
+    std::vector<double> nf, sod, harm;
+    std::vector<uint8_t> registers;
+};
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+struct hb_server {
+    hb_server_options opts{};
+    std::mutex mu;
+    std::condition_variable cv;        // scheduler wake-ups and job completions
+    std::deque<std::shared_ptr<Job>> queue;
+    std::map<uint64_t, std::shared_ptr<Job>> jobs;
+    std::thread scheduler;
+    uint64_t next_id = 1, used = 0;
+    uint32_t active = 0;
+    bool stopping = false;
+    std::string err;
+};
+
+static thread_local std::string t_server_err;
+
+static int server_err(int code, const std::string& msg) {
+    t_server_err = msg;
+    return code;
+}
+
+// Device bytes a job needs at most: CSR and transpose (u64 offsets, u32
+// successors), the CSR's original copy while it is renumbered, both counter
+// arrays (one byte per register), the per-node arrays (estimates, two sums,
+// in-degrees, renumbering, work lists) and the bitmaps, plus a fixed margin.
+uint64_t hb_job_footprint(uint64_t num_nodes, uint64_t num_arcs, int log2m) {
+    const uint64_t n = num_nodes, m = num_arcs;
+    const uint64_t csr = 8 * (n + 1) + 4 * m;
+    return 3 * csr + 2 * n * (1ull << log2m) + 64 * n + (64ull << 20);
+}
+
+static void run_job(hb_server* s, std::shared_ptr<Job> job) {
+    cudaStream_t stream = nullptr;
+    int r = HB_OK;
+    std::string msg;
+    hb_handle* h = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        r = HB_ERR_NO_DEVICE;
+        msg = "no CUDA device available (this library has no CPU path)";
+    } else if (cudaSetDevice(s->opts.device) != cudaSuccess ||
+               cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        r = HB_ERR_CUDA;
+        msg = "cudaStreamCreate failed";
+    }
+    if (!r) {
+        hb_options o = job->opts;
+        o.stream = stream;
+        hb_graph_view v{job->graph.n, job->graph.m, job->graph.offsets.data(),
+                        job->graph.successors.data()};
+        r = hb_create(&v, nullptr, &o, &h);
+        if (r) msg = hb_global_last_error();
+    }
+    if (!r) {
+        r = hb_run_until_done(h);
+        if (r) msg = hb_last_error(h);
+    }
+    if (!r) {
+        job->iterations = hb_num_iterations(h);
+        for (uint64_t i = 0; i < job->iterations; i++) {
+            hb_iter_stats st{};
+            hb_get_iteration_stats(h, i, &st);
+            job->visited_arcs += st.visited_arcs;
+        }
+        const uint64_t n = job->graph.n;
+        if (job->iterations) {
+            size_t len = 0;
+            hb_get_neighborhood_function(h, nullptr, 0, &len);
+            job->nf.resize(len);
+            r = hb_get_neighborhood_function(h, job->nf.data(), len, &len);
+            if (!r && (job->opts.flags & HB_SUM_OF_DISTANCES)) {
+                job->sod.resize(n);
+                r = hb_get_sum_of_distances(h, job->sod.data(), n);
+            }
+            if (!r && (job->opts.flags & HB_SUM_OF_INVERSE_DISTANCES)) {
+                job->harm.resize(n);
+                r = hb_get_harmonic_centralities(h, job->harm.data(), n);
+            }
+        }
+        if (!r && s->opts.keep_registers) {
+            uint64_t cb = 0;
+            int rs = 0;
+            hb_counter_layout(h, &cb, &rs);
+            job->registers.resize(n * cb);
+            r = hb_get_registers(h, HB_CURRENT_STATE, job->registers.data(), job->registers.size());
+        }
+        if (r) msg = hb_last_error(h);
+    }
+    if (h) hb_destroy(h);
+    if (stream) cudaStreamDestroy(stream);
+    // the last touch of the server happens under its lock, so a shutdown
+    // waiting for active == 0 cannot free it under this thread
+    std::lock_guard<std::mutex> lock(s->mu);
+    job->finished = Clock::now();
+    job->error = r;
+    job->message = msg;
+    job->state = r ? HB_JOB_FAILED : HB_JOB_DONE;
+    job->graph = Csr();  // the graph is no longer needed
+    s->used -= job->footprint;
+    s->active--;
+    s->cv.notify_all();
+}
+
+static void schedule(hb_server* s) {
+    std::unique_lock<std::mutex> lock(s->mu);
+    for (;;) {
+        s->cv.wait(lock, [&] {
+            if (s->stopping) return true;
+            if (s->queue.empty() || s->active >= s->opts.max_active) return false;
+            return s->used + s->queue.front()->footprint <= s->opts.hbm_budget_bytes;
+        });
+        if (s->stopping) return;
+        // admit in arrival order while the head fits
+        while (!s->queue.empty() && s->active < s->opts.max_active &&
+               s->used + s->queue.front()->footprint <= s->opts.hbm_budget_bytes) {
+            std::shared_ptr<Job> job = s->queue.front();
+            s->queue.pop_front();
+            s->used += job->footprint;
+            s->active++;
+            job->state = HB_JOB_RUNNING;
+            job->started = Clock::now();
+            std::thread(run_job, s, job).detach();
+        }
+    }
+}
+
+void hb_server_options_default(hb_server_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->struct_size = sizeof(hb_server_options);
+    o->device = 0;
+    o->hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
+    o->max_active = 16;
+    o->keep_registers = 0;
+}
+
+int hb_server_create(const hb_server_options* opts, hb_server** out) {
+    if (!out) return server_err(HB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    hb_server_options o;
+    hb_server_options_default(&o);
+    if (opts) {
+        if (opts->struct_size != sizeof(hb_server_options))
+            return server_err(HB_ERR_INVALID, "hb_server_options.struct_size mismatch");
+        o = *opts;
+    }
+    if (o.max_active == 0) return server_err(HB_ERR_INVALID, "max_active must be at least 1");
+    hb_server* s = new hb_server();
+    s->opts = o;
+    s->scheduler = std::thread(schedule, s);
+    *out = s;
+    return HB_OK;
+}
+
+int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options* opts, uint64_t* job) {
+    if (!s || !graph || !opts || !job) return server_err(HB_ERR_INVALID, "NULL argument");
+    if (opts->struct_size != sizeof(hb_options))
+        return server_err(HB_ERR_INVALID, "hb_options.struct_size mismatch");
+    if (!graph->offsets || (graph->num_arcs && !graph->successors))
+        return server_err(HB_ERR_INVALID, "graph arrays must not be NULL");
+    if (opts->weights) return server_err(HB_ERR_INVALID, "weights are not supported by the server");
+    if (opts->log2m < 4 || opts->log2m > 10) return server_err(HB_ERR_INVALID, "log2m must be in [4, 10]");
+    auto j = std::make_shared<Job>();
+    j->footprint = hb_job_footprint(graph->num_nodes, graph->num_arcs, opts->log2m);
+    if (j->footprint > s->opts.hbm_budget_bytes)
+        return server_err(HB_ERR_INVALID, "the job alone needs " + std::to_string(j->footprint) +
+                                              " device bytes, more than the budget");
+    j->graph.n = graph->num_nodes;
+    j->graph.m = graph->num_arcs;
+    j->graph.offsets.assign(graph->offsets, graph->offsets + graph->num_nodes + 1);
+    j->graph.successors.assign(graph->successors, graph->successors + graph->num_arcs);
+    j->opts = *opts;
+    j->opts.device = s->opts.device;
+    j->opts.stream = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        if (s->stopping) return server_err(HB_ERR_INVALID, "server is shutting down");
+        j->id = s->next_id++;
+        j->submitted = Clock::now();
+        s->jobs[j->id] = j;
+        s->queue.push_back(j);
+        *job = j->id;
+    }
+    s->cv.notify_all();
+    return HB_OK;
+}
+
+static std::shared_ptr<Job> find_job(hb_server* s, uint64_t id) {
+    auto it = s->jobs.find(id);
+    return it == s->jobs.end() ? nullptr : it->second;
+}
+
+int hb_server_wait(hb_server* s, uint64_t job, double timeout_s) {
+    if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
+    std::unique_lock<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j = find_job(s, job);
+    if (!j) return server_err(HB_ERR_INVALID, "unknown job");
+    auto done = [&] { return j->state == HB_JOB_DONE || j->state == HB_JOB_FAILED; };
+    if (timeout_s < 0) {
+        s->cv.wait(lock, done);
+    } else if (!s->cv.wait_for(lock, std::chrono::duration<double>(timeout_s), done)) {
+        return server_err(HB_ERR_TIMEOUT, "job not finished within the timeout");
+    }
+    if (j->state == HB_JOB_FAILED) return server_err(j->error, j->message);
+    return HB_OK;
+}
+
+int hb_server_job_info(hb_server* s, uint64_t job, hb_job_info* info) {
+    if (!s || !info) return server_err(HB_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j = find_job(s, job);
+    if (!j) return server_err(HB_ERR_INVALID, "unknown job");
+    std::memset(info, 0, sizeof(*info));
+    info->state = j->state;
+    info->error = j->error;
+    info->iterations = j->iterations;
+    info->visited_arcs = j->visited_arcs;
+    info->register_updates = j->visited_arcs << j->opts.log2m;
+    info->footprint_bytes = j->footprint;
+    const Clock::time_point now = Clock::now();
+    const bool started = j->state != HB_JOB_QUEUED;
+    const bool ended = j->state == HB_JOB_DONE || j->state == HB_JOB_FAILED;
+    info->queue_ms = ms_between(j->submitted, started ? j->started : now);
+    info->run_ms = started ? ms_between(j->started, ended ? j->finished : now) : 0.0;
+    info->latency_ms = ms_between(j->submitted, ended ? j->finished : now);
+    return HB_OK;
+}
+
+static int finished_job(hb_server* s, uint64_t job, std::shared_ptr<Job>& j) {
+    if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
+    j = find_job(s, job);
+    if (!j) return server_err(HB_ERR_INVALID, "unknown job");
+    if (j->state != HB_JOB_DONE) return server_err(HB_ERR_NOT_RUN, "job has not finished");
+    return HB_OK;
+}
+
+int hb_server_get_neighborhood_function(hb_server* s, uint64_t job, double* dst, size_t capacity,
+                                        size_t* len) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j;
+    int r = finished_job(s, job, j);
+    if (r) return r;
+    if (j->iterations == 0)
+        return server_err(HB_ERR_NOT_RUN, "HyperBall was not run (the graph has no nodes)");
+    if (len) *len = j->nf.size();
+    if (dst) std::copy(j->nf.begin(), j->nf.begin() + std::min(capacity, j->nf.size()), dst);
+    return HB_OK;
+}
+
+static int server_vec(hb_server* s, uint64_t job, double* dst, size_t len, bool harm) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j;
+    int r = finished_job(s, job, j);
+    if (r) return r;
+    if (j->iterations == 0)
+        return server_err(HB_ERR_NOT_RUN, "HyperBall was not run (the graph has no nodes)");
+    const std::vector<double>& v = harm ? j->harm : j->sod;
+    const uint32_t flag = harm ? HB_SUM_OF_INVERSE_DISTANCES : HB_SUM_OF_DISTANCES;
+    if (!(j->opts.flags & flag)) return server_err(HB_ERR_NOT_REQUESTED, "output was not requested");
+    if (!dst || len != v.size()) return server_err(HB_ERR_INVALID, "len must equal the graph's num_nodes");
+    std::copy(v.begin(), v.end(), dst);
+    return HB_OK;
+}
+
+int hb_server_get_sum_of_distances(hb_server* s, uint64_t job, double* dst, size_t len) {
+    return server_vec(s, job, dst, len, false);
+}
+
+int hb_server_get_harmonic_centralities(hb_server* s, uint64_t job, double* dst, size_t len) {
+    return server_vec(s, job, dst, len, true);
+}
+
+int hb_server_get_registers(hb_server* s, uint64_t job, void* dst, size_t bytes) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j;
+    int r = finished_job(s, job, j);
+    if (r) return r;
+    if (!s->opts.keep_registers)
+        return server_err(HB_ERR_NOT_REQUESTED, "the server does not keep registers (keep_registers = 0)");
+    if (!dst || bytes != j->registers.size()) return server_err(HB_ERR_INVALID, "bytes must equal num_nodes * counter bytes");
+    std::memcpy(dst, j->registers.data(), bytes);
+    return HB_OK;
+}
+
+int hb_server_release(hb_server* s, uint64_t job) {
+    if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::shared_ptr<Job> j = find_job(s, job);
+    if (!j) return server_err(HB_ERR_INVALID, "unknown job");
+    if (j->state != HB_JOB_DONE && j->state != HB_JOB_FAILED)
+        return server_err(HB_ERR_INVALID, "job has not finished");
+    s->jobs.erase(job);
+    return HB_OK;
+}
+
+void hb_server_destroy(hb_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stopping = true;
+        // queued jobs are cancelled
+        for (auto& j : s->queue) {
+            j->state = HB_JOB_FAILED;
+            j->error = HB_ERR_INVALID;
+            j->message = "cancelled: the server shut down";
+        }
+        s->queue.clear();
+    }
+    s->cv.notify_all();
+    if (s->scheduler.joinable()) s->scheduler.join();
+    {
+        // running jobs finish
+        std::unique_lock<std::mutex> lock(s->mu);
+        s->cv.wait(lock, [&] { return s->active == 0; });
+    }
+    delete s;
+}
+
+const char* hb_server_last_error(void) { return t_server_err.c_str(); }

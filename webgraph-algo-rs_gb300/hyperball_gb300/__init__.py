@@ -52,6 +52,11 @@ HB_NO_I32_SHIFT_QUIRK = 1 << 3
 HB_CURRENT_STATE = 0
 HB_NEXT_STATE = 1
 
+HB_JOB_QUEUED = 0
+HB_JOB_RUNNING = 1
+HB_JOB_DONE = 2
+HB_JOB_FAILED = 3
+
 
 class HyperBallError(RuntimeError):
     """Base error; `code` is the C status."""
@@ -111,6 +116,33 @@ class Options(ctypes.Structure):
         ("small_max_degree", ctypes.c_uint32),
         ("medium_max_degree", ctypes.c_uint32),
     ]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("device", ctypes.c_int32),
+        ("hbm_budget_bytes", ctypes.c_uint64),
+        ("max_active", ctypes.c_uint32),
+        ("keep_registers", ctypes.c_uint32),
+    ]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [
+        ("state", ctypes.c_int32),
+        ("error", ctypes.c_int32),
+        ("iterations", ctypes.c_uint64),
+        ("visited_arcs", ctypes.c_uint64),
+        ("register_updates", ctypes.c_uint64),
+        ("footprint_bytes", ctypes.c_uint64),
+        ("queue_ms", ctypes.c_double),
+        ("run_ms", ctypes.c_double),
+        ("latency_ms", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class IterStats(ctypes.Structure):
@@ -195,6 +227,22 @@ EXPORTS = [
     ("hb_batch_stats", ctypes.c_int,
      [_H, _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_double)]),
     ("hb_batch_destroy", None, [_H]),
+    ("hb_server_options_default", None, [_P(ServerOptions)]),
+    ("hb_server_create", ctypes.c_int, [_P(ServerOptions), _P(_H)]),
+    ("hb_server_submit", ctypes.c_int, [_H, _P(GraphView), _P(Options), _P(ctypes.c_uint64)]),
+    ("hb_server_wait", ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double]),
+    ("hb_server_job_info", ctypes.c_int, [_H, ctypes.c_uint64, _P(JobInfo)]),
+    ("hb_server_get_neighborhood_function", ctypes.c_int,
+     [_H, ctypes.c_uint64, _P(ctypes.c_double), ctypes.c_size_t, _P(ctypes.c_size_t)]),
+    ("hb_server_get_sum_of_distances", ctypes.c_int,
+     [_H, ctypes.c_uint64, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_server_get_harmonic_centralities", ctypes.c_int,
+     [_H, ctypes.c_uint64, _P(ctypes.c_double), ctypes.c_size_t]),
+    ("hb_server_get_registers", ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_size_t]),
+    ("hb_server_release", ctypes.c_int, [_H, ctypes.c_uint64]),
+    ("hb_server_destroy", None, [_H]),
+    ("hb_job_footprint", ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]),
+    ("hb_server_last_error", ctypes.c_char_p, []),
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
@@ -747,4 +795,103 @@ class HyperBallBatch:
                                         ctypes.byref(upd), ctypes.byref(ms)))
         return {"iterations": it.value, "visited_arcs": vis.value, "register_updates": upd.value,
                 "device_ms": ms.value}
+
+
+# ---------------------------------------------------------------------------
+# served jobs (no reference counterpart)
+# ---------------------------------------------------------------------------
+def _scheck(code):
+    if code == HB_OK:
+        return
+    msg = load_library().hb_server_last_error() or b""
+    raise _ERRORS.get(code, HyperBallError)(code, msg.decode(errors="replace"))
+
+
+class HyperBallServer:
+    """Continuous admission of HyperBall jobs against a device-memory budget;
+    every job returns what HyperBallBuilder(...).build().run_until_done()
+    returns for its graph alone."""
+
+    def __init__(self, hbm_budget_bytes=150 * 10**9, max_active=16, keep_registers=False,
+                 device=0):
+        lib = load_library()
+        self._lib = lib
+        o = ServerOptions()
+        lib.hb_server_options_default(ctypes.byref(o))
+        o.hbm_budget_bytes = int(hbm_budget_bytes)
+        o.max_active = int(max_active)
+        o.keep_registers = 1 if keep_registers else 0
+        o.device = int(device)
+        h = ctypes.c_void_p()
+        _scheck(lib.hb_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._nodes = {}
+
+    def submit(self, graph, log2m, hasher=None, sum_of_distances=False,
+               sum_of_inverse_distances=False, transpose_on_device=True):
+        hasher = hasher or DefaultHasher()
+        o = Options()
+        self._lib.hb_options_default(ctypes.byref(o))
+        o.log2m = int(log2m)
+        o.hash_kind = hasher.kind
+        o.hash_seed = hasher.seed
+        o.num_elements = graph.num_nodes
+        o.flags = ((HB_SUM_OF_DISTANCES if sum_of_distances else 0)
+                   | (HB_SUM_OF_INVERSE_DISTANCES if sum_of_inverse_distances else 0)
+                   | (HB_TRANSPOSE_ON_DEVICE if transpose_on_device else 0))
+        v = graph.view()
+        job = ctypes.c_uint64()
+        _scheck(self._lib.hb_server_submit(self._h, ctypes.byref(v), ctypes.byref(o), ctypes.byref(job)))
+        self._nodes[job.value] = (graph.num_nodes, (1 << int(log2m)) * 5 // 8)
+        return job.value
+
+    def wait(self, job, timeout=None):
+        _scheck(self._lib.hb_server_wait(self._h, job, -1.0 if timeout is None else float(timeout)))
+
+    def info(self, job):
+        i = JobInfo()
+        _scheck(self._lib.hb_server_job_info(self._h, job, ctypes.byref(i)))
+        return i.as_dict()
+
+    def neighborhood_function(self, job):
+        n = ctypes.c_size_t()
+        _scheck(self._lib.hb_server_get_neighborhood_function(self._h, job, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        _scheck(self._lib.hb_server_get_neighborhood_function(
+            self._h, job, out.ctypes.data_as(_P(ctypes.c_double)), n.value, ctypes.byref(n)))
+        return out
+
+    def _vec(self, fn, job):
+        out = np.zeros(self._nodes[job][0], dtype=np.float64)
+        _scheck(fn(self._h, job, out.ctypes.data_as(_P(ctypes.c_double)), len(out)))
+        return out
+
+    def sum_of_distances(self, job):
+        return self._vec(self._lib.hb_server_get_sum_of_distances, job)
+
+    def harmonic_centralities(self, job):
+        return self._vec(self._lib.hb_server_get_harmonic_centralities, job)
+
+    def registers(self, job):
+        n, cb = self._nodes[job]
+        out = np.zeros((n, cb), dtype=np.uint8)
+        _scheck(self._lib.hb_server_get_registers(self._h, job, out.ctypes.data, out.size))
+        return out
+
+    def release(self, job):
+        _scheck(self._lib.hb_server_release(self._h, job))
+        self._nodes.pop(job, None)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.hb_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def job_footprint(num_nodes, num_arcs, log2m):
+    """Device bytes a server reserves for a job of this size."""
+    return int(load_library().hb_job_footprint(num_nodes, num_arcs, log2m))
 
