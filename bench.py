@@ -49,32 +49,61 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--log2n", type=int, default=26, help="graph size (2^log2n nodes)")
+    p.add_argument("--log2n", type=int, default=None,
+                   help="graph size (2^log2n nodes; default 26 web-like, 24 R-MAT)")
     p.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: --steps)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["weblike", "batched", "served"], default="weblike",
-                   help="weblike: the 2^26 web-like graph (default); batched: many small graphs; "
-                        "served: a Poisson stream of jobs through the job server")
+    p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served"], default="weblike",
+                   help="weblike: the 2^26 web-like graph (default); rmat: R-MAT 2^24 x 16, "
+                        "log2m 8; batched: many small graphs; served: a Poisson stream of jobs "
+                        "through the job server")
     p.add_argument("--batch-count", type=int, default=4096, help="graphs in the batched workload")
     p.add_argument("--alone-sample", type=int, default=192,
                    help="graphs of the batch also run one at a time")
     p.add_argument("--jobs", type=int, default=300, help="jobs of the served stream")
     p.add_argument("--rate", type=float, default=200.0, help="job arrivals per second")
     p.add_argument("--pool", type=int, default=48, help="distinct graphs the served jobs draw from")
-    return p.parse_args()
+    args = p.parse_args()
+    set_workload(args)
+    return args
 
 
-def workload(log2n):
+def set_workload(args):
+    """Graph size and counter size of the single-graph workloads."""
+    global LOG2M, COUNTER_BYTES
+    if args.workload == "rmat":
+        LOG2M = 8
+        if args.log2n is None:
+            args.log2n = 24
+    elif args.log2n is None:
+        args.log2n = 26
+    COUNTER_BYTES = (1 << LOG2M) * 5 // 8
+
+
+def make_graph(args):
+    import hyperball_gb300 as hb
+    if args.workload == "rmat":
+        return hb.Graph.rmat(args.log2n, 16, 0.57, 0.19, 0.19, seed=1)
+    return hb.Graph.weblike(1 << args.log2n)
+
+
+def workload(args):
+    if args.workload == "rmat":
+        name = f"rmat-2^{args.log2n} HyperBall to stabilisation"
+        graph = "R-MAT (0.57, 0.19, 0.19, 0.05), 16 arcs drawn per node, seed 1, duplicates and self-loops removed"
+    else:
+        name = f"weblike-2^{args.log2n} HyperBall to stabilisation"
+        graph = ("web-like: Zipf(2.1) out-degree, mean 12, cap 1e5; 80% of successors within "
+                 "+/-1024 of the source, 20% uniform; seed 2")
     return {
-        "workload": f"weblike-2^{log2n} HyperBall to stabilisation",
-        "nodes": 1 << log2n,
-        "graph": "web-like: Zipf(2.1) out-degree, mean 12, cap 1e5; 80% of successors within "
-                 "+/-1024 of the source, 20% uniform; seed 2",
+        "workload": name,
+        "nodes": 1 << args.log2n,
+        "graph": graph,
         "log2m": LOG2M,
         "hash": "SipHash-1-3, seed 0",
         "mode": "systolic, transpose built on device",
         "outputs": "neighbourhood function, sum of distances, harmonic centrality",
-        "l2": "inputs larger than L2 (two 2^n x 40 B counter arrays, CSR 4 B/arc)",
+        "l2": f"inputs larger than L2 (two 2^n x {COUNTER_BYTES} B counter arrays, CSR 4 B/arc)",
     }
 
 
@@ -253,7 +282,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     import hyperball_gb300 as hb
-    g = hb.Graph.weblike(1 << args.log2n)
+    g = make_graph(args)
     cpu = CpuSample(g)
     for _ in range(args.warmup):
         cpu.step()
@@ -271,7 +300,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": workload(args.log2n),
+        "config": workload(args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": "port",
                          "sample": "C++ restatement of the reference algorithm (oracle), "
                                    "threaded engine; " + sample},
@@ -295,9 +324,8 @@ def run_gb300(args):
     ranks = Ranks(world, "nccl", torch.device("cuda", local))
     barrier, max_over_ranks = ranks.barrier, ranks.max
 
-    n = 1 << args.log2n
-    g = hb.Graph.weblike(n)
-    m = g.num_arcs
+    g = make_graph(args)
+    n, m = g.num_nodes, g.num_arcs
     stream = torch.cuda.Stream()
     logic = hb.HyperLogLogBuilder(n).log_2_num_reg(LOG2M).build()
     h = (hb.HyperBallBuilder.new(g, logic).transpose_on_device(True)
@@ -417,7 +445,7 @@ def run_gb300(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": dict(workload(args.log2n), arcs=m, iterations=len(ref_stats),
+            "config": dict(workload(args), arcs=m, iterations=len(ref_stats),
                            parallelism=f"replicas x{world}"),
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
             "clocks": clk, "gpu_launches": launches,

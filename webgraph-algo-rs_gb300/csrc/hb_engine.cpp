@@ -17,8 +17,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <map>
@@ -283,34 +285,67 @@ void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium
     out.chunks.resize(chunk_at[nseg]);
     out.heavy.resize(heavy_at[nseg]);
     std::vector<uint8_t> kind_of(n);  // device id -> 0 heavy, 1 medium, 2 light
+    // light nodes are placed by a counting sort over their degrees when the
+    // light bound is small (the default 32); anything else by key sorting
+    constexpr uint64_t COUNTING_MAX = 64;
+    const bool counting = small_max <= COUNTING_MAX;
     parallel(nseg, [&](uint64_t w) {
         const uint64_t w0 = seg[w], w1 = seg[w + 1];
         // sort key: (inverted clamped degree, node): decreasing degree, ties by id
-        std::vector<uint64_t> kind[3];
+        static thread_local std::vector<uint64_t> kind[3];
+        for (auto& k : kind) k.clear();
+        uint32_t hist[COUNTING_MAX + 2] = {0};
         for (uint64_t v = w0; v < w1; v++) {
             const uint64_t d = off[v + 1] - off[v];
-            const uint64_t key = ((uint64_t)(0xffffffffu - (uint32_t)std::min<uint64_t>(d, 0xffffffffu)) << 32) | v;
-            kind[d > medium_max ? 0 : d > small_max ? 1 : 2].push_back(key);
+            const int k = d > medium_max ? 0 : d > small_max ? 1 : 2;
+            if (k == 2 && counting) {
+                hist[d]++;
+                continue;
+            }
+            kind[k].push_back(((uint64_t)(0xffffffffu - (uint32_t)std::min<uint64_t>(d, 0xffffffffu)) << 32) | v);
         }
         uint64_t next = w0, cp = chunk_at[w], hp = heavy_at[w];
-        for (int k = 0; k < 3; k++) {
-            std::sort(kind[k].begin(), kind[k].end());
-            const uint64_t first = next;
-            for (uint64_t key : kind[k]) {
-                out.perm[next] = (uint32_t)key;
-                out.inv[(uint32_t)key] = (uint32_t)next;
-                kind_of[next] = (uint8_t)k;
-                if (k == 0) out.heavy[hp++] = (uint32_t)next;
-                next++;
-            }
-            if (k == 0) continue;
-            const uint32_t per = k == 1 ? per_medium : per_light;
-            const uint32_t flag = k == 1 ? 0x80000000u : 0u;
-            for (uint64_t i = 0; i < kind[k].size(); i += per) {
-                const uint32_t c = (uint32_t)std::min<uint64_t>(per, kind[k].size() - i);
+        auto place = [&](uint64_t v, int k) {
+            out.perm[next] = (uint32_t)v;
+            out.inv[v] = (uint32_t)next;
+            kind_of[next] = (uint8_t)k;
+            if (k == 0) out.heavy[hp++] = (uint32_t)next;
+            next++;
+        };
+        auto cut = [&](uint64_t first, uint64_t count, uint32_t per, uint32_t flag) {
+            for (uint64_t i = 0; i < count; i += per) {
+                const uint32_t c = (uint32_t)std::min<uint64_t>(per, count - i);
                 out.chunks[cp++] = make_uint2((uint32_t)(first + i), c | flag);
             }
+        };
+        for (int k = 0; k < 2; k++) {
+            std::sort(kind[k].begin(), kind[k].end());
+            const uint64_t first = next;
+            for (uint64_t key : kind[k]) place((uint32_t)key, k);
+            if (k == 1) cut(first, kind[1].size(), per_medium, 0x80000000u);
         }
+        const uint64_t first = next;
+        if (counting) {
+            // bucket starts, largest degree first; nodes in id order within a bucket
+            uint64_t start[COUNTING_MAX + 2], acc = first;
+            for (int64_t d = (int64_t)small_max; d >= 0; d--) {
+                start[d] = acc;
+                acc += hist[d];
+            }
+            for (uint64_t v = w0; v < w1; v++) {
+                const uint64_t d = off[v + 1] - off[v];
+                if (d > small_max) continue;
+                const uint64_t pos = start[d]++;
+                out.perm[pos] = (uint32_t)v;
+                out.inv[v] = (uint32_t)pos;
+                kind_of[pos] = 2;
+            }
+            next = acc;
+        } else {
+            std::sort(kind[2].begin(), kind[2].end());
+            for (uint64_t key : kind[2]) place((uint32_t)key, 2);
+        }
+        cut(first, next - first, per_light, 0u);
     });
     const uint64_t words = (n + 31) / 32;
     out.light_bits.assign(words, 0u);
@@ -1131,9 +1166,24 @@ const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_gl
 
 // hb_create, optionally for a batch: `inst` holds the instance starts (caller
 // ids, ascending, starting at 0) followed by num_nodes.
+// HB_TRACE=1 in the environment prints the duration of each creation phase
+// to stderr (the reference's progress-logger role for building).
+struct PhaseTrace {
+    bool on = std::getenv("HB_TRACE") != nullptr;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char* phase) {
+        if (!on) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "hb_create %-28s %8.2f ms\n", phase,
+                     std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
+
 static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpose,
                        const hb_options* opts, const std::vector<uint64_t>* inst, hb_handle** out) {
     if (!out) return set_err(nullptr, HB_ERR_INVALID, "out is NULL");
+    PhaseTrace trace;
     *out = nullptr;
     hb_options o;
     hb_options_default(&o);
@@ -1238,8 +1288,10 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
         hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
         WorkPartition wp;
+        trace.mark("setup");
         build_partition(graph, h->small_max, h->medium_max, win_nodes, per_light, per_medium,
                         h->inst_start, wp);
+        trace.mark("work partition (host)");
         h->n_tiles = h->n ? wp.tiles.size() - 1 : 0;
         h->n_chunks = wp.chunks.size();
         h->n_heavy = wp.heavy.size();
@@ -1282,8 +1334,11 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     {
         uint64_t* off0 = nullptr;
         uint32_t* succ0 = nullptr;
+        trace.mark("partition upload");
         if ((r = upload_csr(hp, graph, &off0, &succ0))) return fail(r);
+        trace.mark("CSR upload + check");
         if ((r = relabel_csr(hp, off0, succ0, &h->d_off, &h->d_succ))) return fail(r);
+        trace.mark("renumbering");
         dfree(hp, off0);
         dfree(hp, succ0);
     }
@@ -1314,7 +1369,9 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         dfree(hp, succ0);
         h->has_transpose = true;
     } else if (o.flags & HB_TRANSPOSE_ON_DEVICE) {
+        trace.mark("in-degrees");
         if ((r = build_transpose_on_device(hp))) return fail(r);
+        trace.mark("transpose");
     }
     const uint64_t n = h->n;
     if ((r = dalloc(hp, &h->d_cnt[0], n * h->stride))) return fail(r);
@@ -1341,6 +1398,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
                           "cudaMemcpy")))
             return fail(r);
     }
+    trace.mark("state arrays");
     h->grid_tile = hbk::tile_grid(h->log2m, h->device);
     {
         // one warp per chunk, 8 warps per block
@@ -1359,6 +1417,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     if ((r = dalloc(hp, &h->d_any31, 1))) return fail(r);
     if ((r = dalloc(hp, &h->d_cursor, 1))) return fail(r);
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
+    trace.mark("launch setup");
     *out = h.release();
     return HB_OK;
 }
