@@ -395,6 +395,9 @@ def run_gb300(args):
     h.close()
     del h
     nf_len = len(ref_stats) + 1
+    # per-node results land in page-locked host buffers
+    sod_pin = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+    harm_pin = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
 
     def e2e_step():
         hh = (hb.HyperBallBuilder.new(view, logic).transpose_on_device(True)
@@ -402,8 +405,8 @@ def run_gb300(args):
               .stream(stream.cuda_stream).device(local).build())
         hh.run_until_done()
         nf = hh.neighborhood_function()
-        hh.sum_of_distances()
-        hh.harmonic_centralities()
+        hh.sum_of_distances(out=sod_pin)
+        hh.harmonic_centralities(out=harm_pin)
         k = hh.kernel_launches()
         hh.close()
         return len(nf), k

@@ -345,6 +345,14 @@ const char* hb_version(void);
  * every iteration). No reference counterpart: a diagnostic for benchmarks. */
 uint64_t hb_kernel_launches(const hb_handle* h);
 
+/* ---- device memory ------------------------------------------------------------ */
+/* Handles, batches and served jobs take device memory from a pool the library
+ * keeps per device; memory a destroyed handle gave back stays reserved there
+ * for the next one, so creating and destroying handles in a loop maps no new
+ * memory. This returns the reserved, unused memory of `device` to the device
+ * (memory in use is untouched). No reference counterpart. */
+int hb_release_cached_memory(int device);
+
 #ifdef __cplusplus
 }
 #endif

@@ -105,6 +105,27 @@ def test_run_api_matches_oracle(hb, oracle):
         for name in ("sum_of_distances", "harmonic_centralities", "closeness_centrality",
                      "lin_centrality", "nieminen_centrality", "reachable_nodes"):
             assert_close(getattr(gpu, name)(), getattr(orc, name)(), 1e-12, name)
+        # caller buffers and single-node lookups give the same values
+        buf = np.full(g.num_nodes, np.nan)
+        assert gpu.sum_of_distances(out=buf) is buf
+        assert_close(buf, orc.sum_of_distances(), 1e-12, "sum_of_distances(out=)")
+        reach = orc.reachable_nodes()
+        for v in (0, 17, g.num_nodes - 1):
+            assert_close(np.array([gpu.reachable_nodes_from(v)]), reach[v:v + 1], 1e-12, "from")
+    with pytest.raises(ValueError):
+        gpu.harmonic_centralities(out=np.zeros(g.num_nodes, dtype=np.float32))
+
+
+def test_cached_memory_release(hb, oracle):
+    """Handles reuse the library's pooled device memory; returning it to the
+    device leaves later handles correct."""
+    g = hb.Graph.rmat(11, 8, seed=9)
+    first, _, _ = lockstep(hb, oracle, g, 6, transpose_on_device=True)
+    hb.release_cached_memory(0)
+    again, _, _ = lockstep(hb, oracle, g, 6, transpose_on_device=True)
+    np.testing.assert_array_equal(first.registers(), again.registers())
+    with pytest.raises(hb.InvalidArgumentError):
+        hb.release_cached_memory(1 << 20)
 
 
 def test_errors(hb):

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <memory>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -53,6 +54,42 @@ struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
 };
+
+// The library's device-memory pool of `device`, created on first use. Freed
+// blocks are kept (no release threshold) for later allocations.
+cudaError_t lib_pool(int device, cudaMemPool_t* out) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static cudaMemPool_t pools[MAX_DEVICES] = {};
+    if (device < 0 || device >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[device]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        cudaMemPool_t p = nullptr;
+        cudaError_t e = cudaMemPoolCreate(&p, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(p);
+            return e;
+        }
+        pools[device] = p;
+    }
+    *out = pools[device];
+    return cudaSuccess;
+}
+
+cudaError_t pool_alloc(int device, void** p, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = lib_pool(device, &pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
 
 }  // namespace
 
@@ -113,7 +150,6 @@ struct hb_handle {
     uint64_t pending_visited = 0;   // arcs the next iteration visits
     uint32_t* d_perm = nullptr;     // device node -> caller node
     uint32_t* d_inv = nullptr;      // caller node -> device node
-    std::vector<uint32_t> inv_host;
     uint64_t n_chunks = 0;
     uint32_t* d_light_bits = nullptr;           // light nodes (device ids)
     uint32_t* d_medium_bits = nullptr;          // medium nodes (device ids)
@@ -186,11 +222,11 @@ int dalloc(hb_handle* h, T** out, size_t count) {
     void* p = nullptr;
     // stream-ordered: freeing never synchronises the whole device, so other
     // work (other handles, other jobs of a server) keeps running
-    cudaError_t e = cudaMallocAsync(&p, bytes, h->stream);
+    cudaError_t e = pool_alloc(h->device, &p, bytes, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return cuda_err(h, e, "cudaMallocAsync");
+        return cuda_err(h, e, "cudaMallocFromPoolAsync");
     }
     h->bufs.push_back({p, bytes});
     *out = (T*)p;
@@ -209,160 +245,103 @@ void release(hb_handle* h) {
 // Static work order of the union kernels (the graph does not change), and the
 // node renumbering that follows it. Nodes are cut into segments of at most
 // `win_nodes` consecutive ids, which also end at every instance boundary of a
-// batch (`bounds`: sorted instance starts, or empty); inside a segment the
-// heavy nodes (out-degree > medium_max), the medium nodes (small_max <
+// batch (h->inst_start: sorted instance starts, or empty); inside a segment
+// the heavy nodes (out-degree > medium_max), the medium nodes (small_max <
 // out-degree <= medium_max) and the light nodes (out-degree <= small_max)
 // take the segment's ids in that order, each kind by decreasing out-degree,
 // ties by id: perm[new] = caller id, inv[caller] = new. Renumbering never
 // leaves a segment, so an instance keeps its id range. The light and medium
 // runs are cut into chunks of one warp-step (`per_light` or `per_medium`
-// nodes); heavy nodes are listed by decreasing degree; `light_bits` /
-// `medium_bits` mark the light / medium nodes (device ids). Segments are
-// processed by all host threads.
-struct WorkPartition {
-    std::vector<uint32_t> tiles, perm, inv, heavy, light_bits, medium_bits;
-    std::vector<uint2> chunks;
-};
+// nodes); heavy nodes are listed by decreasing degree, ties in id order;
+// light / medium bitmaps mark the light / medium nodes (device ids). The
+// segment cuts are made on the host, everything per node on the device from
+// the uploaded offsets `off0` (caller ids).
+void dfree(hb_handle* h, void* p);
 
-void build_partition(const hb_graph_view* g, uint64_t small_max, uint64_t medium_max,
-                     uint32_t win_nodes, uint32_t per_light, uint32_t per_medium,
-                     const std::vector<uint64_t>& bounds, WorkPartition& out) {
-    const uint64_t n = g->num_nodes;
-    const uint64_t* off = g->offsets;
-    // segment starts
-    std::vector<uint64_t> seg;
+int device_partition(hb_handle* h, const uint64_t* off0, uint32_t win_nodes, uint32_t per_light,
+                     uint32_t per_medium) {
+    const uint64_t n = h->n;
+    const std::vector<uint64_t>& bounds = h->inst_start;
+    std::vector<uint32_t> seg, base;
     {
         size_t bi = 0;
+        uint64_t inst0 = 0;
         for (uint64_t w0 = 0; w0 < n;) {
-            while (bi < bounds.size() && bounds[bi] <= w0) bi++;
+            while (bi < bounds.size() && bounds[bi] <= w0) inst0 = bounds[bi++];
             uint64_t w1 = std::min<uint64_t>(n, w0 + win_nodes);
             if (bi < bounds.size() && bounds[bi] < w1) w1 = bounds[bi];
-            seg.push_back(w0);
+            seg.push_back((uint32_t)w0);
+            base.push_back((uint32_t)inst0);
             w0 = w1;
         }
-        seg.push_back(n);
+        seg.push_back((uint32_t)n);
     }
     const uint64_t nseg = seg.size() - 1;
-    struct SegCount {
-        uint64_t light, medium, heavy;
-    };
-    std::vector<SegCount> cnt(nseg);
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    auto parallel = [&](uint64_t count, auto&& body) {
-        const uint64_t nthreads = std::min<uint64_t>(std::min<uint64_t>(hw, 64), std::max<uint64_t>(count, 1));
-        std::vector<std::thread> th;
-        for (uint64_t t = 0; t < nthreads; t++)
-            th.emplace_back([&, t] {
-                for (uint64_t w = count * t / nthreads; w < count * (t + 1) / nthreads; w++) body(w);
-            });
-        for (auto& x : th) x.join();
-    };
-    parallel(nseg, [&](uint64_t w) {
-        SegCount c{0, 0, 0};
-        for (uint64_t v = seg[w]; v < seg[w + 1]; v++) {
-            const uint64_t d = off[v + 1] - off[v];
-            if (d > medium_max)
-                c.heavy++;
-            else if (d > small_max)
-                c.medium++;
-            else
-                c.light++;
-        }
-        cnt[w] = c;
-    });
-    // segment offsets into chunks and heavy
-    std::vector<uint64_t> chunk_at(nseg + 1, 0), heavy_at(nseg + 1, 0);
-    for (uint64_t w = 0; w < nseg; w++) {
-        const SegCount& c = cnt[w];
-        chunk_at[w + 1] = chunk_at[w] + (c.medium + per_medium - 1) / per_medium +
-                          (c.light + per_light - 1) / per_light;
-        heavy_at[w + 1] = heavy_at[w] + c.heavy;
-    }
-    out.tiles.resize(n ? nseg + 1 : 0);
-    for (uint64_t w = 0; n && w <= nseg; w++) out.tiles[w] = (uint32_t)seg[w];
-    out.perm.resize(n);
-    out.inv.resize(n);
-    out.chunks.resize(chunk_at[nseg]);
-    out.heavy.resize(heavy_at[nseg]);
-    std::vector<uint8_t> kind_of(n);  // device id -> 0 heavy, 1 medium, 2 light
-    // light nodes are placed by a counting sort over their degrees when the
-    // light bound is small (the default 32); anything else by key sorting
-    constexpr uint64_t COUNTING_MAX = 64;
-    const bool counting = small_max <= COUNTING_MAX;
-    parallel(nseg, [&](uint64_t w) {
-        const uint64_t w0 = seg[w], w1 = seg[w + 1];
-        // sort key: (inverted clamped degree, node): decreasing degree, ties by id
-        static thread_local std::vector<uint64_t> kind[3];
-        for (auto& k : kind) k.clear();
-        uint32_t hist[COUNTING_MAX + 2] = {0};
-        for (uint64_t v = w0; v < w1; v++) {
-            const uint64_t d = off[v + 1] - off[v];
-            const int k = d > medium_max ? 0 : d > small_max ? 1 : 2;
-            if (k == 2 && counting) {
-                hist[d]++;
-                continue;
-            }
-            kind[k].push_back(((uint64_t)(0xffffffffu - (uint32_t)std::min<uint64_t>(d, 0xffffffffu)) << 32) | v);
-        }
-        uint64_t next = w0, cp = chunk_at[w], hp = heavy_at[w];
-        auto place = [&](uint64_t v, int k) {
-            out.perm[next] = (uint32_t)v;
-            out.inv[v] = (uint32_t)next;
-            kind_of[next] = (uint8_t)k;
-            if (k == 0) out.heavy[hp++] = (uint32_t)next;
-            next++;
-        };
-        auto cut = [&](uint64_t first, uint64_t count, uint32_t per, uint32_t flag) {
-            for (uint64_t i = 0; i < count; i += per) {
-                const uint32_t c = (uint32_t)std::min<uint64_t>(per, count - i);
-                out.chunks[cp++] = make_uint2((uint32_t)(first + i), c | flag);
-            }
-        };
-        for (int k = 0; k < 2; k++) {
-            std::sort(kind[k].begin(), kind[k].end());
-            const uint64_t first = next;
-            for (uint64_t key : kind[k]) place((uint32_t)key, k);
-            if (k == 1) cut(first, kind[1].size(), per_medium, 0x80000000u);
-        }
-        const uint64_t first = next;
-        if (counting) {
-            // bucket starts, largest degree first; nodes in id order within a bucket
-            uint64_t start[COUNTING_MAX + 2], acc = first;
-            for (int64_t d = (int64_t)small_max; d >= 0; d--) {
-                start[d] = acc;
-                acc += hist[d];
-            }
-            for (uint64_t v = w0; v < w1; v++) {
-                const uint64_t d = off[v + 1] - off[v];
-                if (d > small_max) continue;
-                const uint64_t pos = start[d]++;
-                out.perm[pos] = (uint32_t)v;
-                out.inv[v] = (uint32_t)pos;
-                kind_of[pos] = 2;
-            }
-            next = acc;
-        } else {
-            std::sort(kind[2].begin(), kind[2].end());
-            for (uint64_t key : kind[2]) place((uint32_t)key, 2);
-        }
-        cut(first, next - first, per_light, 0u);
-    });
     const uint64_t words = (n + 31) / 32;
-    out.light_bits.assign(words, 0u);
-    out.medium_bits.assign(words, 0u);
-    parallel(words, [&](uint64_t wi) {
-        uint32_t lb = 0, mb = 0;
-        for (uint64_t v = wi * 32; v < std::min<uint64_t>(n, wi * 32 + 32); v++) {
-            if (kind_of[v] == 2) lb |= 1u << (v & 31);
-            if (kind_of[v] == 1) mb |= 1u << (v & 31);
-        }
-        out.light_bits[wi] = lb;
-        out.medium_bits[wi] = mb;
-    });
-    std::stable_sort(out.heavy.begin(), out.heavy.end(), [&](uint32_t x, uint32_t y) {
-        const uint32_t ux = out.perm[x], uy = out.perm[y];
-        return off[ux + 1] - off[ux] > off[uy + 1] - off[uy];
-    });
+    int r;
+    h->n_tiles = nseg;
+    if ((r = dalloc(h, &h->d_tiles, seg.size()))) return r;
+    if ((r = dalloc(h, &h->d_perm, n))) return r;
+    if ((r = dalloc(h, &h->d_inv, n))) return r;
+    if ((r = dalloc(h, &h->d_light_bits, words))) return r;
+    if ((r = dalloc(h, &h->d_medium_bits, words))) return r;
+    const bool batch = !bounds.empty();
+    uint32_t* d_base = nullptr;
+    if (batch) {
+        if ((r = dalloc(h, &h->d_hash_id, n))) return r;
+        if ((r = dalloc(h, &d_base, base.size()))) return r;
+        HB_CUDA(h, cudaMemcpyAsync(d_base, base.data(), base.size() * 4, cudaMemcpyHostToDevice,
+                                   h->stream));
+    }
+    HB_CUDA(h, cudaMemcpyAsync(h->d_tiles, seg.data(), seg.size() * 4, cudaMemcpyHostToDevice,
+                               h->stream));
+    HB_CUDA(h, cudaMemsetAsync(h->d_light_bits, 0, words * 4, h->stream));
+    HB_CUDA(h, cudaMemsetAsync(h->d_medium_bits, 0, words * 4, h->stream));
+    unsigned long long *seg_chunks = nullptr, *seg_heavy = nullptr, *scratch = nullptr;
+    uint64_t *chunk_at = nullptr, *heavy_at = nullptr;
+    const uint64_t sl = hbk::scan_scratch_len(nseg + 1);
+    if ((r = dalloc(h, &seg_chunks, nseg + 1))) return r;
+    if ((r = dalloc(h, &seg_heavy, nseg + 1))) return r;
+    if ((r = dalloc(h, &chunk_at, nseg + 1))) return r;
+    if ((r = dalloc(h, &heavy_at, nseg + 1))) return r;
+    if ((r = dalloc(h, &scratch, sl))) return r;
+    HB_LAUNCH(h, hbk::launch_part_count(off0, h->d_tiles, nseg, h->small_max, h->medium_max, per_light,
+                                        per_medium, seg_chunks, seg_heavy, h->stream));
+    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(seg_chunks, chunk_at, nseg + 1, scratch, sl, h->stream));
+    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(seg_heavy, heavy_at, nseg + 1, scratch, sl, h->stream));
+    uint64_t totals[2] = {0, 0};
+    HB_CUDA(h, cudaMemcpyAsync(&totals[0], chunk_at + nseg, 8, cudaMemcpyDeviceToHost, h->stream));
+    HB_CUDA(h, cudaMemcpyAsync(&totals[1], heavy_at + nseg, 8, cudaMemcpyDeviceToHost, h->stream));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->n_chunks = totals[0];
+    h->n_heavy = totals[1];
+    unsigned long long* heavy_keys = nullptr;
+    if ((r = dalloc(h, &h->d_chunks, h->n_chunks))) return r;
+    if ((r = dalloc(h, &heavy_keys, h->n_heavy))) return r;
+    HB_LAUNCH(h, hbk::launch_part_place(off0, h->d_tiles, nseg, h->small_max, h->medium_max, per_light,
+                                        per_medium, (const unsigned long long*)chunk_at,
+                                        (const unsigned long long*)heavy_at, d_base, h->d_perm,
+                                        h->d_inv, h->d_chunks, heavy_keys, h->d_light_bits,
+                                        h->d_medium_bits, h->d_hash_id, h->stream));
+    if (h->n_heavy) {
+        // all heavy nodes by decreasing degree, ties in segment order (few
+        // nodes: sorted on the host)
+        std::vector<unsigned long long> keys(h->n_heavy);
+        HB_CUDA(h, cudaMemcpyAsync(keys.data(), heavy_keys, h->n_heavy * 8, cudaMemcpyDeviceToHost,
+                                   h->stream));
+        HB_CUDA(h, cudaStreamSynchronize(h->stream));
+        std::sort(keys.begin(), keys.end());
+        std::vector<uint32_t> heavy(h->n_heavy);
+        for (uint64_t i = 0; i < h->n_heavy; i++) heavy[i] = (uint32_t)keys[i];
+        if ((r = dalloc(h, &h->d_heavy, h->n_heavy))) return r;
+        HB_CUDA(h, cudaMemcpyAsync(h->d_heavy, heavy.data(), h->n_heavy * 4, cudaMemcpyHostToDevice,
+                                   h->stream));
+    }
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (void* p : {(void*)seg_chunks, (void*)seg_heavy, (void*)chunk_at, (void*)heavy_at,
+                    (void*)scratch, (void*)heavy_keys, (void*)d_base})
+        if (p) dfree(h, p);
+    return HB_OK;
 }
 
 bool check_view(const hb_graph_view* g, std::string& why) {
@@ -443,38 +422,49 @@ int relabel_csr(hb_handle* h, const uint64_t* off0, const uint32_t* succ0, uint6
     return HB_OK;
 }
 
-// Transpose of a device CSR (n nodes, m arcs) into toff[n + 1] / tsucc[m]:
-// in-degrees into `cursor` (n + 1 words, zeroed here), exclusive scan into
-// toff (`scan`: scan_scratch_len(n + 1) words), scatter with `cursor` as the
+// Transpose rows from their lengths: `cursor` (n + 1 words) holds the row
+// lengths of the transpose (cursor[n] = 0); exclusive scan into toff
+// (`scan`: scan_scratch_len(n + 1) words), then a scatter with `cursor` as the
 // per-row write position. Rows of the result are in no particular order.
+cudaError_t transpose_rows(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
+                           uint64_t* toff, uint32_t* tsucc, unsigned long long* cursor,
+                           unsigned long long* scan, uint64_t scan_len, cudaStream_t s) {
+    int r = hbk::launch_exclusive_scan_u64(cursor, toff, n + 1, scan, scan_len, s);
+    if (r || n == 0 || m == 0) return (cudaError_t)r;
+    cudaError_t e = cudaMemcpyAsync(cursor, toff, n * 8, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    return (cudaError_t)hbk::launch_transpose_scatter(off, succ, n, cursor, tsucc, s);
+}
+
+// Transpose of a device CSR (n nodes, m arcs) into toff[n + 1] / tsucc[m]:
+// in-degrees into `cursor` (n + 1 words, zeroed here), then transpose_rows.
 cudaError_t transpose_core(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
                            uint64_t* toff, uint32_t* tsucc, unsigned long long* cursor,
                            unsigned long long* scan, uint64_t scan_len, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(cursor, 0, (n + 1) * 8, s);
     if (e != cudaSuccess) return e;
     int r = m ? hbk::launch_transpose_count(succ, m, cursor, s) : 0;
-    if (!r) r = hbk::launch_exclusive_scan_u64(cursor, toff, n + 1, scan, scan_len, s);
-    if (r || n == 0 || m == 0) return (cudaError_t)r;
-    e = cudaMemcpyAsync(cursor, toff, n * 8, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return e;
-    return (cudaError_t)hbk::launch_transpose_scatter(off, succ, n, cursor, tsucc, s);
+    if (r) return (cudaError_t)r;
+    return transpose_rows(off, succ, n, m, toff, tsucc, cursor, scan, scan_len, s);
 }
 
-int build_transpose_on_device(hb_handle* h) {
+// The transpose of the renumbered graph; `rows` (n + 1 words) holds each
+// node's self-loops (from the in-degree pass), to which the in-degrees
+// without self-loops are added. `rows` is released here.
+int build_transpose_on_device(hb_handle* h, unsigned long long* rows) {
     const uint64_t n = h->n, m = h->m;
     int r;
-    unsigned long long* indeg = nullptr;
-    if ((r = dalloc(h, &indeg, n + 1))) return r;
     if ((r = dalloc(h, &h->d_toff, n + 1))) return r;
     if ((r = dalloc(h, &h->d_tsucc, m))) return r;
     const uint64_t sl = hbk::scan_scratch_len(n + 1);
     unsigned long long* scratch = nullptr;
     if ((r = dalloc(h, &scratch, sl))) return r;
-    HB_CUDA(h, transpose_core(h->d_off, h->d_succ, n, m, h->d_toff, h->d_tsucc, indeg, scratch, sl,
+    HB_LAUNCH(h, hbk::launch_add_indeg(rows, h->d_indeg, n, h->stream));
+    HB_CUDA(h, transpose_rows(h->d_off, h->d_succ, n, m, h->d_toff, h->d_tsucc, rows, scratch, sl,
                               h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     // temporaries are released right away
-    dfree(h, indeg);
+    dfree(h, rows);
     dfree(h, scratch);
     h->has_transpose = true;
     return HB_OK;
@@ -748,10 +738,10 @@ int copy_nodes_range(const hb_handle* h, const double* src, double* dst, uint64_
     if (count == 0) return HB_OK;
     HB_CUDA(hh, cudaSetDevice(h->device));
     double* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&tmp, count * 8, h->stream);
+    cudaError_t e = pool_alloc(h->device, (void**)&tmp, count * 8, h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return cuda_err(hh, e, "cudaMallocAsync");
+        return cuda_err(hh, e, "cudaMallocFromPoolAsync");
     }
     int r = hbk::launch_gather_f64(src, h->d_inv + start, tmp, count, h->stream);
     if (r == 0) r = copy_d2h(h, tmp, dst, count * 8);
@@ -775,10 +765,10 @@ int copy_registers_range(const hb_handle* h, int which, void* dst, uint64_t star
     HB_CUDA(hh, cudaSetDevice(h->device));
     const size_t bytes = count * h->counter_bytes;
     void* packed = nullptr;
-    cudaError_t e = cudaMallocAsync(&packed, bytes, h->stream);
+    cudaError_t e = pool_alloc(h->device, &packed, bytes, h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return cuda_err(hh, e, "cudaMallocAsync");
+        return cuda_err(hh, e, "cudaMallocFromPoolAsync");
     }
     int r = hbk::launch_pack_counters(h->log2m, h->d_cnt[idx], h->d_inv + start, (uint8_t*)packed,
                                       count, h->stream);
@@ -1161,6 +1151,23 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
 const char* hb_version(void) { return "hyperball_gb300 0.1 sm_103a"; }
 
 uint64_t hb_kernel_launches(const hb_handle* h) { return h ? h->launches : 0; }
+
+int hb_release_cached_memory(int device) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_NO_DEVICE, "no CUDA device available (this library has no CPU path)");
+    }
+    if (device < 0 || device >= ndev) return set_err(nullptr, HB_ERR_INVALID, "no such device");
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = lib_pool(device, &pool);
+    if (e == cudaSuccess) e = cudaMemPoolTrimTo(pool, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, HB_ERR_CUDA, std::string("cudaMemPoolTrimTo: ") + cudaGetErrorString(e));
+    }
+    return HB_OK;
+}
 const char* hb_global_last_error(void) { return g_global_err.c_str(); }
 const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_global_err.c_str(); }
 
@@ -1287,29 +1294,13 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         uint32_t win_nodes = 0, win_arcs = 0, per_light = 0, per_medium = 0;
         hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
         hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
-        WorkPartition wp;
+        uint64_t* off0 = nullptr;
+        uint32_t* succ0 = nullptr;
         trace.mark("setup");
-        build_partition(graph, h->small_max, h->medium_max, win_nodes, per_light, per_medium,
-                        h->inst_start, wp);
-        trace.mark("work partition (host)");
-        h->n_tiles = h->n ? wp.tiles.size() - 1 : 0;
-        h->n_chunks = wp.chunks.size();
-        h->n_heavy = wp.heavy.size();
-        auto upload = [&](auto** dst, const auto& src) {
-            int rr = dalloc(hp, dst, src.size());
-            if (rr) return rr;
-            if (src.empty()) return (int)HB_OK;
-            return cuda_err(hp,
-                            cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice),
-                            "cudaMemcpy");
-        };
-        if ((r = upload(&h->d_tiles, wp.tiles))) return fail(r);
-        if ((r = upload(&h->d_chunks, wp.chunks))) return fail(r);
-        if ((r = upload(&h->d_perm, wp.perm))) return fail(r);
-        if ((r = upload(&h->d_inv, wp.inv))) return fail(r);
-        if (h->n_heavy && (r = upload(&h->d_heavy, wp.heavy))) return fail(r);
-        if ((r = upload(&h->d_medium_bits, wp.medium_bits))) return fail(r);
-        if ((r = upload(&h->d_light_bits, wp.light_bits))) return fail(r);
+        if ((r = upload_csr(hp, graph, &off0, &succ0))) return fail(r);
+        trace.mark("CSR upload + check");
+        if ((r = device_partition(hp, off0, win_nodes, per_light, per_medium))) return fail(r);
+        trace.mark("work partition");
         const uint64_t words = (h->n + 31) / 32;
         if ((r = dalloc(hp, &h->d_word_cnt, words + 1))) return fail(r);
         if ((r = dalloc(hp, &h->d_word_off, words + 1))) return fail(r);
@@ -1318,39 +1309,39 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         if ((r = dalloc(hp, &h->d_light_list, h->n + 1))) return fail(r);
         if ((r = dalloc(hp, &h->d_medium_list, h->n + 1))) return fail(r);
         if (!h->inst_start.empty()) {
-            // batch: each instance hashes its own node ids, and reports per instance
+            // batch: per-instance bookkeeping (the hashed ids came with the partition)
             const size_t ni = h->inst_start.size() - 1;
-            std::vector<uint32_t> hid(h->n);
-            for (size_t i = 0; i < ni; i++)
-                for (uint64_t u = h->inst_start[i]; u < h->inst_start[i + 1]; u++)
-                    hid[wp.inv[u]] = (uint32_t)(u - h->inst_start[i]);
-            if ((r = upload(&h->d_hash_id, hid))) return fail(r);
-            if ((r = upload(&h->d_inst_start, h->inst_start))) return fail(r);
+            if ((r = dalloc(hp, &h->d_inst_start, h->inst_start.size()))) return fail(r);
+            if ((r = cuda_err(hp, cudaMemcpyAsync(h->d_inst_start, h->inst_start.data(),
+                                                  h->inst_start.size() * 8, cudaMemcpyHostToDevice,
+                                                  h->stream),
+                              "cudaMemcpyAsync")))
+                return fail(r);
             if ((r = dalloc(hp, &h->d_inst_mod, ni))) return fail(r);
             if ((r = dalloc(hp, &h->d_inst_nf, ni))) return fail(r);
         }
-        h->inv_host = std::move(wp.inv);
-    }
-    {
-        uint64_t* off0 = nullptr;
-        uint32_t* succ0 = nullptr;
-        trace.mark("partition upload");
-        if ((r = upload_csr(hp, graph, &off0, &succ0))) return fail(r);
-        trace.mark("CSR upload + check");
         if ((r = relabel_csr(hp, off0, succ0, &h->d_off, &h->d_succ))) return fail(r);
         trace.mark("renumbering");
         dfree(hp, off0);
         dfree(hp, succ0);
     }
+    // in-degrees without self-loops; with a transpose to build, the same pass
+    // gives its row lengths
+    const bool device_transpose = !transpose && (o.flags & HB_TRANSPOSE_ON_DEVICE);
+    unsigned long long* trows = nullptr;
     {
         unsigned long long* loops = nullptr;
         if ((r = dalloc(hp, &h->d_indeg, h->n))) return fail(r);
         if ((r = dalloc(hp, &loops, 1))) return fail(r);
+        if (device_transpose && (r = dalloc(hp, &trows, h->n + 1))) return fail(r);
         if ((r = cuda_err(hp, cudaMemsetAsync(h->d_indeg, 0, h->n * 4, h->stream), "cudaMemsetAsync")))
             return fail(r);
         if ((r = cuda_err(hp, cudaMemsetAsync(loops, 0, 8, h->stream), "cudaMemsetAsync"))) return fail(r);
+        if (trows && (r = cuda_err(hp, cudaMemsetAsync(trows + h->n, 0, 8, h->stream), "cudaMemsetAsync")))
+            return fail(r);
         if (h->n && (r = cuda_err(hp, (cudaError_t)hbk::launch_indeg_noloop(h->d_off, h->d_succ, h->n,
-                                                                         h->d_indeg, loops, h->stream),
+                                                                         h->d_indeg, loops, trows,
+                                                                         h->stream),
                                   "launch_indeg_noloop")))
             return fail(r);
         unsigned long long nl = 0;
@@ -1368,9 +1359,9 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         dfree(hp, off0);
         dfree(hp, succ0);
         h->has_transpose = true;
-    } else if (o.flags & HB_TRANSPOSE_ON_DEVICE) {
+    } else if (device_transpose) {
         trace.mark("in-degrees");
-        if ((r = build_transpose_on_device(hp))) return fail(r);
+        if ((r = build_transpose_on_device(hp, trows))) return fail(r);
         trace.mark("transpose");
     }
     const uint64_t n = h->n;
@@ -1551,7 +1542,9 @@ int hb_reachable_nodes_from(const hb_handle* h, uint64_t node, double* out) {
     int r = ensure_iteration(h);
     if (r) return r;
     if (node >= h->n || !out) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "node out of range");
-    return copy_d2h(h, h->d_est + h->inv_host[node], out, 8);
+    uint32_t dev_node = 0;
+    if ((r = copy_d2h(h, h->d_inv + node, &dev_node, 4))) return r;
+    return copy_d2h(h, h->d_est + dev_node, out, 8);
 }
 
 static int lin_or_nieminen(const hb_handle* h, double* dst, size_t len, bool lin) {

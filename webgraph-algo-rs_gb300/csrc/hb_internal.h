@@ -112,9 +112,12 @@ int launch_init(int log2m, const InitArgs& a, void* stream);
 // in caller node order (inv: caller node -> device node)
 int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uint8_t* dst,
                          uint64_t n, void* stream);
-// in-degree without self-loops (indeg zeroed by the caller); *loops += self-loops
+// in-degree without self-loops (indeg zeroed by the caller); *loops += self-loops;
+// tloops (or null; n + 1 words): tloops[v] = self-loops of v, tloops[n] = 0
 int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
-                        unsigned long long* loops, void* stream);
+                        unsigned long long* loops, unsigned long long* tloops, void* stream);
+// rows[v] += indeg[v], v < n
+int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n, void* stream);
 // renumbering: deg[i] = out-degree of perm[i] (deg[n] = 0)
 int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
                        unsigned long long* deg, void* stream);
@@ -166,6 +169,21 @@ constexpr uint64_t NOALLOC_MAX_NODES = 1ull << 20;
 int noalloc_scratch(unsigned long long** out, uint64_t* words);
 int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t n,
                              unsigned long long* cursor, uint32_t* tsucc, void* stream);
+// work partition: per segment tiles[w] .. tiles[w + 1] (at most the tile
+// window of nodes) its chunk count and heavy count (index nseg: zeros) ...
+int launch_part_count(const uint64_t* off, const uint32_t* tiles, uint64_t nseg, uint64_t small_max,
+                      uint64_t medium_max, uint32_t per_light, uint32_t per_medium,
+                      unsigned long long* seg_chunks, unsigned long long* seg_heavy, void* stream);
+// ... then, from their exclusive scans, the renumbering (perm, inv), the chunk
+// table, the heavy keys (inverted degree << 32 | new id, segment order), the
+// kind bitmaps (zeroed by the caller) and, when seg_base is given, hash_id[new]
+// = caller id - seg_base[segment]
+int launch_part_place(const uint64_t* off, const uint32_t* tiles, uint64_t nseg, uint64_t small_max,
+                      uint64_t medium_max, uint32_t per_light, uint32_t per_medium,
+                      const unsigned long long* chunk_at, const unsigned long long* heavy_at,
+                      const uint32_t* seg_base, uint32_t* perm, uint32_t* inv, uint2* chunks,
+                      unsigned long long* heavy_keys, uint32_t* light_bits, uint32_t* medium_bits,
+                      uint32_t* hash_id, void* stream);
 int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m, int* bad,
                     void* stream);
 

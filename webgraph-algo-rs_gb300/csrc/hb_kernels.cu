@@ -772,27 +772,45 @@ __global__ void __launch_bounds__(256) k_pack_counters(const uint8_t* __restrict
 
 // ---------------------------------------------------------------------------
 // in-degree without self-loops (visited-arc accounting), and the number of
-// self-loops; one warp per node
+// self-loops; one warp per node. With `tloops`, also each node's own
+// self-loops (tloops[v], tloops[n] = 0): added to the in-degrees, they are the
+// row lengths of the transpose.
 // ---------------------------------------------------------------------------
 __global__ void k_indeg_noloop(const uint64_t* __restrict__ off, const uint32_t* __restrict__ succ,
                                uint64_t n, uint32_t* __restrict__ indeg,
-                               unsigned long long* __restrict__ loops) {
+                               unsigned long long* __restrict__ loops,
+                               unsigned long long* __restrict__ tloops) {
     const int lane = threadIdx.x & 31;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long nl = 0;
+    if (tloops && gw == 0 && lane == 0) tloops[n] = 0;
     for (uint64_t v = gw; v < n; v += nw) {
         const uint64_t s0 = __ldg(off + v), s1 = __ldg(off + v + 1);
+        uint32_t own = 0;
         for (uint64_t e = s0 + lane; e < s1; e += 32) {
             const uint32_t s = __ldg(succ + e);
             if (s == (uint32_t)v)
-                nl++;
+                own++;
             else
                 atomicAdd(indeg + s, 1u);
+        }
+        nl += own;
+        if (tloops) {
+            for (int o = 16; o > 0; o >>= 1) own += __shfl_xor_sync(0xffffffffu, own, o);
+            if (lane == 0) tloops[v] = own;
         }
     }
     for (int o = 16; o > 0; o >>= 1) nl += __shfl_xor_sync(0xffffffffu, nl, o);
     if (lane == 0 && nl) atomicAdd(loops, nl);
+}
+
+// rows[v] += indeg[v] for v < n
+__global__ void k_add_indeg(unsigned long long* __restrict__ rows, const uint32_t* __restrict__ indeg,
+                            uint64_t n) {
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x)
+        rows[v] += indeg[v];
 }
 
 // fixed-order sum of doubles: block b sums its contiguous range (strided by
@@ -1084,6 +1102,136 @@ __global__ void k_validate(const uint64_t* __restrict__ off, const uint32_t* __r
 }
 
 // ---------------------------------------------------------------------------
+// Work partition and renumbering. Segments (at most WINDOW consecutive caller
+// ids, tiles[w] .. tiles[w + 1]) are renumbered in place: heavy nodes
+// (out-degree > medium_max), then medium (> small_max), then light, each kind
+// by decreasing out-degree, ties by id.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int node_kind(uint64_t d, uint64_t small_max, uint64_t medium_max) {
+    return d > medium_max ? 0 : d > small_max ? 1 : 2;
+}
+
+// per segment: chunks of its medium and light runs, and its heavy nodes;
+// index nseg gets zeros (the scans' last input); one warp per segment
+__global__ void k_part_count(const uint64_t* __restrict__ off, const uint32_t* __restrict__ tiles,
+                             uint64_t nseg, uint64_t small_max, uint64_t medium_max,
+                             uint32_t per_light, uint32_t per_medium,
+                             unsigned long long* __restrict__ seg_chunks,
+                             unsigned long long* __restrict__ seg_heavy) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = gw; w <= nseg; w += nw) {
+        uint32_t c[3] = {0, 0, 0};
+        if (w < nseg)
+            for (uint64_t v = tiles[w] + lane; v < tiles[w + 1]; v += 32)
+                c[node_kind(__ldg(off + v + 1) - __ldg(off + v), small_max, medium_max)]++;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            for (int o = 16; o > 0; o >>= 1) c[k] += __shfl_xor_sync(0xffffffffu, c[k], o);
+        if (lane == 0) {
+            seg_chunks[w] = (c[1] + per_medium - 1) / per_medium + (c[2] + per_light - 1) / per_light;
+            seg_heavy[w] = c[0];
+        }
+    }
+}
+
+// one block per segment: a bitonic sort of the segment's keys (kind, inverted
+// degree, local id) in shared memory gives the new order; then perm / inv,
+// the chunk table, the heavy keys (inverted degree << 32 | new id), the kind
+// bitmaps (zeroed by the caller) and, for batches, the hashed ids
+__global__ void __launch_bounds__(256) k_part_place(
+    const uint64_t* __restrict__ off, const uint32_t* __restrict__ tiles, uint64_t nseg,
+    uint64_t small_max, uint64_t medium_max, uint32_t per_light, uint32_t per_medium,
+    const unsigned long long* __restrict__ chunk_at, const unsigned long long* __restrict__ heavy_at,
+    const uint32_t* __restrict__ seg_base, uint32_t* __restrict__ perm, uint32_t* __restrict__ inv,
+    uint2* __restrict__ chunks, unsigned long long* __restrict__ heavy_keys,
+    uint32_t* __restrict__ light_bits, uint32_t* __restrict__ medium_bits,
+    uint32_t* __restrict__ hash_id) {
+    __shared__ unsigned long long key[WINDOW];
+    __shared__ uint32_t cnt[3];
+    const int lane = threadIdx.x & 31;
+    for (uint64_t w = blockIdx.x; w < nseg; w += gridDim.x) {
+        const uint32_t v0 = tiles[w], size = tiles[w + 1] - v0;
+        uint32_t P = 32;
+        while (P < size) P <<= 1;
+        if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+            unsigned long long k = ~0ull;
+            int kind = 3;
+            if (i < size) {
+                const uint64_t d = __ldg(off + v0 + i + 1) - __ldg(off + v0 + i);
+                kind = node_kind(d, small_max, medium_max);
+                const uint64_t inv_d = 0xffffffffull - (d < 0xffffffffull ? d : 0xffffffffull);
+                k = ((unsigned long long)kind << 43) | (inv_d << 11) | i;
+            }
+            key[i] = k;
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                const uint32_t b = __ballot_sync(0xffffffffu, kind == q);
+                if (lane == 0 && b) atomicAdd(&cnt[q], (uint32_t)__popc(b));
+            }
+        }
+        __syncthreads();
+        for (uint32_t s = 2; s <= P; s <<= 1)
+            for (uint32_t j = s >> 1; j > 0; j >>= 1) {
+                for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+                    const uint32_t x = i ^ j;
+                    if (x > i) {
+                        const unsigned long long a = key[i], b = key[x];
+                        if ((a > b) == ((i & s) == 0)) {
+                            key[i] = b;
+                            key[x] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        const uint32_t nh = cnt[0], nm = cnt[1], nl = cnt[2];
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+            const uint32_t pos = v0 + i;
+            const unsigned long long k = key[i];
+            const int kind = i < size ? (int)(k >> 43) : 3;
+            if (i < size) {
+                const uint32_t v = v0 + (uint32_t)(k & 2047);
+                perm[pos] = v;
+                inv[v] = pos;
+                if (hash_id) hash_id[pos] = v - seg_base[w];
+                if (kind == 0) heavy_keys[heavy_at[w] + i] = (((k >> 11) & 0xffffffffull) << 32) | pos;
+            }
+            // kind bits: lanes sharing a bitmap word are contiguous; the
+            // lowest of them merges their bits into one atomic per word
+            const uint32_t word = pos >> 5;
+            const uint32_t grp = __match_any_sync(0xffffffffu, word);
+            const uint32_t lb = __ballot_sync(0xffffffffu, kind == 2);
+            const uint32_t mb = __ballot_sync(0xffffffffu, kind == 1);
+            const int l0 = __ffs(grp) - 1;
+            if (lane == l0) {
+                const uint32_t b0 = pos & 31;
+                const uint32_t lw = ((lb & grp) >> l0) << b0, mw = ((mb & grp) >> l0) << b0;
+                if (lw) atomicOr(light_bits + word, lw);
+                if (mw) atomicOr(medium_bits + word, mw);
+            }
+        }
+        // chunks: the medium run, then the light run, one warp-step each
+        const uint32_t cm = (nm + per_medium - 1) / per_medium, cl = (nl + per_light - 1) / per_light;
+        for (uint32_t j = threadIdx.x; j < cm + cl; j += blockDim.x) {
+            uint2 c;
+            if (j < cm) {
+                const uint32_t first = j * per_medium;
+                c = make_uint2(v0 + nh + first, min(per_medium, nm - first) | 0x80000000u);
+            } else {
+                const uint32_t first = (j - cm) * per_light;
+                c = make_uint2(v0 + nh + nm + first, min(per_light, nl - first));
+            }
+            chunks[chunk_at[w] + j] = c;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -1183,11 +1331,19 @@ int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uin
 #undef CALL
 }
 
+int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n, void* stream) {
+    if (n == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, 8192);
+    ++t_launches;
+    k_add_indeg<<<grid, 256, 0, (cudaStream_t)stream>>>(rows, indeg, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
-                        unsigned long long* loops, void* stream) {
+                        unsigned long long* loops, unsigned long long* tloops, void* stream) {
     const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256 + 1, 16384);
     ++t_launches;
-    k_indeg_noloop<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, indeg, loops);
+    k_indeg_noloop<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, indeg, loops, tloops);
     return (int)cudaGetLastError();
 }
 
@@ -1410,6 +1566,32 @@ int launch_transpose_scatter(const uint64_t* off, const uint32_t* succ, uint64_t
     const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256, 8192);
     ++t_launches;
     k_transpose_scatter<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, cursor, tsucc);
+    return (int)cudaGetLastError();
+}
+
+int launch_part_count(const uint64_t* off, const uint32_t* tiles, uint64_t nseg, uint64_t small_max,
+                      uint64_t medium_max, uint32_t per_light, uint32_t per_medium,
+                      unsigned long long* seg_chunks, unsigned long long* seg_heavy, void* stream) {
+    const int grid = (int)std::min<uint64_t>((nseg + 1 + 7) / 8, 8192);
+    ++t_launches;
+    k_part_count<<<grid, 256, 0, (cudaStream_t)stream>>>(off, tiles, nseg, small_max, medium_max,
+                                                         per_light, per_medium, seg_chunks, seg_heavy);
+    return (int)cudaGetLastError();
+}
+
+int launch_part_place(const uint64_t* off, const uint32_t* tiles, uint64_t nseg, uint64_t small_max,
+                      uint64_t medium_max, uint32_t per_light, uint32_t per_medium,
+                      const unsigned long long* chunk_at, const unsigned long long* heavy_at,
+                      const uint32_t* seg_base, uint32_t* perm, uint32_t* inv, uint2* chunks,
+                      unsigned long long* heavy_keys, uint32_t* light_bits, uint32_t* medium_bits,
+                      uint32_t* hash_id, void* stream) {
+    if (nseg == 0) return 0;
+    const int grid = (int)std::min<uint64_t>(nseg, 65535);
+    ++t_launches;
+    k_part_place<<<grid, 256, 0, (cudaStream_t)stream>>>(off, tiles, nseg, small_max, medium_max,
+                                                         per_light, per_medium, chunk_at, heavy_at,
+                                                         seg_base, perm, inv, chunks, heavy_keys,
+                                                         light_bits, medium_bits, hash_id);
     return (int)cudaGetLastError();
 }
 

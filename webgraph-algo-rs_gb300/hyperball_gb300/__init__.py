@@ -212,6 +212,7 @@ EXPORTS = [
     ("hb_graph_free", None, [_H]),
     ("hb_version", ctypes.c_char_p, []),
     ("hb_kernel_launches", ctypes.c_uint64, [_H]),
+    ("hb_release_cached_memory", ctypes.c_int, [ctypes.c_int]),
     ("hb_batch_create", ctypes.c_int,
      [_P(GraphView), ctypes.c_uint32, _P(ctypes.c_int32), _P(Options), _P(_H)]),
     ("hb_batch_run_until_done", ctypes.c_int, [_H]),
@@ -666,31 +667,37 @@ class HyperBall:
             self._h, out.ctypes.data_as(_P(ctypes.c_double)), ln.value, ctypes.byref(ln)), self._h)
         return out
 
-    def _vec(self, fn, *pre):
-        out = np.zeros(self.num_nodes, dtype=np.float64)
+    def _vec(self, fn, *pre, out=None):
+        # out: an optional C-contiguous float64 array of num_nodes elements
+        # to fill (for instance page-locked memory), else a new array
+        if out is None:
+            out = np.zeros(self.num_nodes, dtype=np.float64)
+        elif (out.dtype != np.float64 or out.shape != (self.num_nodes,)
+              or not out.flags.c_contiguous or not out.flags.writeable):
+            raise ValueError("out must be a writable C-contiguous float64 array of num_nodes elements")
         _check(fn(self._h, *pre, out.ctypes.data_as(_P(ctypes.c_double)), self.num_nodes), self._h)
         return out
 
-    def sum_of_distances(self):
-        return self._vec(self._lib.hb_get_sum_of_distances)
+    def sum_of_distances(self, out=None):
+        return self._vec(self._lib.hb_get_sum_of_distances, out=out)
 
-    def harmonic_centralities(self):
-        return self._vec(self._lib.hb_get_harmonic_centralities)
+    def harmonic_centralities(self, out=None):
+        return self._vec(self._lib.hb_get_harmonic_centralities, out=out)
 
-    def discounted_centrality(self, index):
-        return self._vec(self._lib.hb_get_discounted_centrality, index)
+    def discounted_centrality(self, index, out=None):
+        return self._vec(self._lib.hb_get_discounted_centrality, index, out=out)
 
-    def closeness_centrality(self):
-        return self._vec(self._lib.hb_get_closeness_centrality)
+    def closeness_centrality(self, out=None):
+        return self._vec(self._lib.hb_get_closeness_centrality, out=out)
 
-    def lin_centrality(self):
-        return self._vec(self._lib.hb_get_lin_centrality)
+    def lin_centrality(self, out=None):
+        return self._vec(self._lib.hb_get_lin_centrality, out=out)
 
-    def nieminen_centrality(self):
-        return self._vec(self._lib.hb_get_nieminen_centrality)
+    def nieminen_centrality(self, out=None):
+        return self._vec(self._lib.hb_get_nieminen_centrality, out=out)
 
-    def reachable_nodes(self):
-        return self._vec(self._lib.hb_get_reachable_nodes)
+    def reachable_nodes(self, out=None):
+        return self._vec(self._lib.hb_get_reachable_nodes, out=out)
 
     def reachable_nodes_from(self, node):
         v = ctypes.c_double()
@@ -894,4 +901,10 @@ class HyperBallServer:
 def job_footprint(num_nodes, num_arcs, log2m):
     """Device bytes a server reserves for a job of this size."""
     return int(load_library().hb_job_footprint(num_nodes, num_arcs, log2m))
+
+
+def release_cached_memory(device=0):
+    """Returns the device memory the library keeps for reuse (freed by
+    closed handles) to the device."""
+    _check(load_library().hb_release_cached_memory(device))
 
