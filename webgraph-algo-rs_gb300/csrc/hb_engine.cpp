@@ -133,6 +133,7 @@ struct hb_handle {
     double* d_lnt = nullptr;
     uint64_t* d_weights = nullptr;
     uint32_t* d_tiles = nullptr;  // window boundaries
+    uint32_t* d_arc_tiles = nullptr;  // creation only: first node of each arc tile of d_off
     uint64_t n_tiles = 0;         // number of windows
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
     uint32_t* d_indeg = nullptr;    // in-degree without self-loops
@@ -377,15 +378,17 @@ int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t*
     if (g->num_arcs)
         HB_CUDA(h, cudaMemcpyAsync(*d_succ, g->successors, g->num_arcs * 4, cudaMemcpyHostToDevice,
                                    h->stream));
-    // reject out-of-range successors before any kernel indexes with them
+    // reject decreasing offsets before any kernel sizes work by them (the
+    // successors are checked where they are renumbered)
     int* d_bad = nullptr;
     if ((r = dalloc(h, &d_bad, 1))) return r;
     HB_CUDA(h, cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream));
-    HB_LAUNCH(h, hbk::launch_validate(*d_off, *d_succ, g->num_nodes, g->num_arcs, d_bad, h->stream));
+    HB_LAUNCH(h, hbk::launch_validate(*d_off, *d_succ, g->num_nodes, 0, d_bad, h->stream));
     int bad = 0;
     HB_CUDA(h, cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (bad) return set_err(h, HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
+    dfree(h, d_bad);
+    if (bad) return set_err(h, HB_ERR_INVALID, "graph has decreasing offsets");
     return HB_OK;
 }
 
@@ -402,55 +405,69 @@ void dfree(hb_handle* h, void* p) {
 
 // CSR (caller ids) -> CSR of the renumbered graph: node i is caller node
 // perm[i], successor u becomes inv[u].
+// The renumbered CSR of a caller CSR (off0 / succ0, offsets checked): row i
+// is caller row perm[i], targets mapped through inv; out-of-range targets are
+// an error. With indeg (zeroed), the same pass counts the in-degrees without
+// self-loops, the self-loops into *loops and, with trows (zeroed), each node's
+// self-loops. With arc_tiles, the arc tiles of the result are returned there
+// (to be freed by the caller).
 int relabel_csr(hb_handle* h, const uint64_t* off0, const uint32_t* succ0, uint64_t** d_off,
-                uint32_t** d_succ) {
+                uint32_t** d_succ, uint32_t* indeg, unsigned long long* loops,
+                unsigned long long* trows, uint32_t** arc_tiles) {
     const uint64_t n = h->n, m = h->m;
     int r;
     unsigned long long* deg = nullptr;
     unsigned long long* scratch = nullptr;
+    uint32_t* tiles = nullptr;
+    int* bad = nullptr;
     const uint64_t sl = hbk::scan_scratch_len(n + 1);
     if ((r = dalloc(h, d_off, n + 1))) return r;
     if ((r = dalloc(h, d_succ, m))) return r;
     if ((r = dalloc(h, &deg, n + 1))) return r;
     if ((r = dalloc(h, &scratch, sl))) return r;
+    if ((r = dalloc(h, &tiles, hbk::arc_tiles(m) + 1))) return r;
+    if ((r = dalloc(h, &bad, 1))) return r;
+    HB_CUDA(h, cudaMemsetAsync(bad, 0, sizeof(int), h->stream));
     HB_LAUNCH(h, hbk::launch_perm_degree(off0, h->d_perm, n, deg, h->stream));
     HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(deg, *d_off, n + 1, scratch, sl, h->stream));
-    if (n) HB_LAUNCH(h, hbk::launch_relabel_succ(off0, succ0, h->d_perm, h->d_inv, *d_off, *d_succ, n, h->stream));
+    HB_LAUNCH(h, hbk::launch_tile_start(*d_off, n, tiles, h->stream));
+    HB_LAUNCH(h, hbk::launch_relabel_arcs(*d_off, n, m, tiles, h->d_perm, off0, succ0, h->d_inv, *d_succ,
+                                          indeg, loops, trows, bad, h->stream));
+    int bad_host = 0;
+    HB_CUDA(h, cudaMemcpyAsync(&bad_host, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     dfree(h, deg);
     dfree(h, scratch);
+    dfree(h, bad);
+    if (arc_tiles)
+        *arc_tiles = tiles;
+    else
+        dfree(h, tiles);
+    if (bad_host) return set_err(h, HB_ERR_INVALID, "graph has successors >= num_nodes");
     return HB_OK;
 }
 
-// Transpose rows from their lengths: `cursor` (n + 1 words) holds the row
-// lengths of the transpose (cursor[n] = 0); exclusive scan into toff
-// (`scan`: scan_scratch_len(n + 1) words), then a scatter with `cursor` as the
-// per-row write position. Rows of the result are in no particular order.
-cudaError_t transpose_rows(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
-                           uint64_t* toff, uint32_t* tsucc, unsigned long long* cursor,
-                           unsigned long long* scan, uint64_t scan_len, cudaStream_t s) {
-    int r = hbk::launch_exclusive_scan_u64(cursor, toff, n + 1, scan, scan_len, s);
-    if (r || n == 0 || m == 0) return (cudaError_t)r;
-    cudaError_t e = cudaMemcpyAsync(cursor, toff, n * 8, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return e;
-    return (cudaError_t)hbk::launch_transpose_scatter(off, succ, n, cursor, tsucc, s);
-}
-
 // Transpose of a device CSR (n nodes, m arcs) into toff[n + 1] / tsucc[m]:
-// in-degrees into `cursor` (n + 1 words, zeroed here), then transpose_rows.
+// in-degrees into `cursor` (n + 1 words, zeroed here), exclusive scan into
+// toff (`scan`: scan_scratch_len(n + 1) words), scatter with `cursor` as the
+// per-row write position. Rows of the result are in no particular order.
 cudaError_t transpose_core(const uint64_t* off, const uint32_t* succ, uint64_t n, uint64_t m,
                            uint64_t* toff, uint32_t* tsucc, unsigned long long* cursor,
                            unsigned long long* scan, uint64_t scan_len, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(cursor, 0, (n + 1) * 8, s);
     if (e != cudaSuccess) return e;
     int r = m ? hbk::launch_transpose_count(succ, m, cursor, s) : 0;
-    if (r) return (cudaError_t)r;
-    return transpose_rows(off, succ, n, m, toff, tsucc, cursor, scan, scan_len, s);
+    if (!r) r = hbk::launch_exclusive_scan_u64(cursor, toff, n + 1, scan, scan_len, s);
+    if (r || n == 0 || m == 0) return (cudaError_t)r;
+    e = cudaMemcpyAsync(cursor, toff, n * 8, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    return (cudaError_t)hbk::launch_transpose_scatter(off, succ, n, cursor, tsucc, s);
 }
 
 // The transpose of the renumbered graph; `rows` (n + 1 words) holds each
-// node's self-loops (from the in-degree pass), to which the in-degrees
-// without self-loops are added. `rows` is released here.
+// node's self-loops (from the renumbering pass), to which the in-degrees
+// without self-loops are added; the scatter walks the arc tiles of the
+// renumbering. `rows` is released here.
 int build_transpose_on_device(hb_handle* h, unsigned long long* rows) {
     const uint64_t n = h->n, m = h->m;
     int r;
@@ -460,8 +477,12 @@ int build_transpose_on_device(hb_handle* h, unsigned long long* rows) {
     unsigned long long* scratch = nullptr;
     if ((r = dalloc(h, &scratch, sl))) return r;
     HB_LAUNCH(h, hbk::launch_add_indeg(rows, h->d_indeg, n, h->stream));
-    HB_CUDA(h, transpose_rows(h->d_off, h->d_succ, n, m, h->d_toff, h->d_tsucc, rows, scratch, sl,
-                              h->stream));
+    HB_LAUNCH(h, hbk::launch_exclusive_scan_u64(rows, h->d_toff, n + 1, scratch, sl, h->stream));
+    if (n && m) {
+        HB_CUDA(h, cudaMemcpyAsync(rows, h->d_toff, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+        HB_LAUNCH(h, hbk::launch_scatter_arcs(h->d_off, n, m, h->d_arc_tiles, h->d_succ, rows, h->d_tsucc,
+                                              h->stream));
+    }
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     // temporaries are released right away
     dfree(h, rows);
@@ -1290,6 +1311,8 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
     h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
     if (h->medium_max < h->small_max) h->medium_max = h->small_max;
+    const bool device_transpose = !transpose && (o.flags & HB_TRANSPOSE_ON_DEVICE);
+    unsigned long long* trows = nullptr;
     {
         uint32_t win_nodes = 0, win_arcs = 0, per_light = 0, per_medium = 0;
         hbk::tile_capacity(h->log2m, &win_nodes, &win_arcs);
@@ -1320,16 +1343,9 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
             if ((r = dalloc(hp, &h->d_inst_mod, ni))) return fail(r);
             if ((r = dalloc(hp, &h->d_inst_nf, ni))) return fail(r);
         }
-        if ((r = relabel_csr(hp, off0, succ0, &h->d_off, &h->d_succ))) return fail(r);
-        trace.mark("renumbering");
-        dfree(hp, off0);
-        dfree(hp, succ0);
-    }
-    // in-degrees without self-loops; with a transpose to build, the same pass
-    // gives its row lengths
-    const bool device_transpose = !transpose && (o.flags & HB_TRANSPOSE_ON_DEVICE);
-    unsigned long long* trows = nullptr;
-    {
+        // renumbering; the same pass counts in-degrees without self-loops and,
+        // with a transpose to build, each node's self-loops (its row lengths
+        // are in-degree + self-loops)
         unsigned long long* loops = nullptr;
         if ((r = dalloc(hp, &h->d_indeg, h->n))) return fail(r);
         if ((r = dalloc(hp, &loops, 1))) return fail(r);
@@ -1337,13 +1353,15 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         if ((r = cuda_err(hp, cudaMemsetAsync(h->d_indeg, 0, h->n * 4, h->stream), "cudaMemsetAsync")))
             return fail(r);
         if ((r = cuda_err(hp, cudaMemsetAsync(loops, 0, 8, h->stream), "cudaMemsetAsync"))) return fail(r);
-        if (trows && (r = cuda_err(hp, cudaMemsetAsync(trows + h->n, 0, 8, h->stream), "cudaMemsetAsync")))
+        if (trows &&
+            (r = cuda_err(hp, cudaMemsetAsync(trows, 0, (h->n + 1) * 8, h->stream), "cudaMemsetAsync")))
             return fail(r);
-        if (h->n && (r = cuda_err(hp, (cudaError_t)hbk::launch_indeg_noloop(h->d_off, h->d_succ, h->n,
-                                                                         h->d_indeg, loops, trows,
-                                                                         h->stream),
-                                  "launch_indeg_noloop")))
+        if ((r = relabel_csr(hp, off0, succ0, &h->d_off, &h->d_succ, h->d_indeg, loops, trows,
+                             device_transpose ? &h->d_arc_tiles : nullptr)))
             return fail(r);
+        trace.mark("renumbering + in-degrees");
+        dfree(hp, off0);
+        dfree(hp, succ0);
         unsigned long long nl = 0;
         if ((r = cuda_err(hp, cudaMemcpyAsync(&nl, loops, 8, cudaMemcpyDeviceToHost, h->stream), "cudaMemcpy")))
             return fail(r);
@@ -1355,13 +1373,16 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         uint64_t* off0 = nullptr;
         uint32_t* succ0 = nullptr;
         if ((r = upload_csr(hp, transpose, &off0, &succ0))) return fail(r);
-        if ((r = relabel_csr(hp, off0, succ0, &h->d_toff, &h->d_tsucc))) return fail(r);
+        if ((r = relabel_csr(hp, off0, succ0, &h->d_toff, &h->d_tsucc, nullptr, nullptr, nullptr,
+                             nullptr)))
+            return fail(r);
         dfree(hp, off0);
         dfree(hp, succ0);
         h->has_transpose = true;
     } else if (device_transpose) {
-        trace.mark("in-degrees");
         if ((r = build_transpose_on_device(hp, trows))) return fail(r);
+        dfree(hp, h->d_arc_tiles);
+        h->d_arc_tiles = nullptr;
         trace.mark("transpose");
     }
     const uint64_t n = h->n;

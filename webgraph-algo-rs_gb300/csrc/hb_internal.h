@@ -112,19 +112,25 @@ int launch_init(int log2m, const InitArgs& a, void* stream);
 // in caller node order (inv: caller node -> device node)
 int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uint8_t* dst,
                          uint64_t n, void* stream);
-// in-degree without self-loops (indeg zeroed by the caller); *loops += self-loops;
-// tloops (or null; n + 1 words): tloops[v] = self-loops of v, tloops[n] = 0
-int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
-                        unsigned long long* loops, unsigned long long* tloops, void* stream);
 // rows[v] += indeg[v], v < n
 int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n, void* stream);
 // renumbering: deg[i] = out-degree of perm[i] (deg[n] = 0)
 int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
                        unsigned long long* deg, void* stream);
-// succ[off[i] ..] = inv[succ0[off0[perm[i]] ..]]
-int launch_relabel_succ(const uint64_t* off0, const uint32_t* succ0, const uint32_t* perm,
-                        const uint32_t* inv, const uint64_t* off, uint32_t* succ, uint64_t n,
-                        void* stream);
+// arc-parallel passes: tiles of consecutive arcs; tile_start[k] (arc_tiles(m)
+// words) = the node holding the first arc of tile k
+uint64_t arc_tiles(uint64_t m);
+int launch_tile_start(const uint64_t* off, uint64_t n, uint32_t* tile_start, void* stream);
+// succ[e] = inv[succ0[off0[perm[i]] + e - off[i]]] for every arc e of node i
+// (targets >= n set *bad); with indeg (zeroed): in-degrees without self-loops,
+// *loops += self-loops, and with trows (zeroed) trows[i] += self-loops of i
+int launch_relabel_arcs(const uint64_t* off, uint64_t n, uint64_t m, const uint32_t* tile_start,
+                        const uint32_t* perm, const uint64_t* off0, const uint32_t* succ0,
+                        const uint32_t* inv, uint32_t* succ, uint32_t* indeg, unsigned long long* loops,
+                        unsigned long long* trows, int* bad, void* stream);
+// transpose scatter with per-row cursors (positions of the next arc of each row)
+int launch_scatter_arcs(const uint64_t* off, uint64_t n, uint64_t m, const uint32_t* tile_start,
+                        const uint32_t* succ, unsigned long long* cursor, uint32_t* tsucc, void* stream);
 // dst[u] = src[inv[u]]: a per-node array back to caller order
 int launch_gather_f64(const double* src, const uint32_t* inv, double* dst, uint64_t n,
                       void* stream);

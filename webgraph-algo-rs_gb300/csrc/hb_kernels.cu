@@ -770,42 +770,7 @@ __global__ void __launch_bounds__(256) k_pack_counters(const uint8_t* __restrict
     }
 }
 
-// ---------------------------------------------------------------------------
-// in-degree without self-loops (visited-arc accounting), and the number of
-// self-loops; one warp per node. With `tloops`, also each node's own
-// self-loops (tloops[v], tloops[n] = 0): added to the in-degrees, they are the
-// row lengths of the transpose.
-// ---------------------------------------------------------------------------
-__global__ void k_indeg_noloop(const uint64_t* __restrict__ off, const uint32_t* __restrict__ succ,
-                               uint64_t n, uint32_t* __restrict__ indeg,
-                               unsigned long long* __restrict__ loops,
-                               unsigned long long* __restrict__ tloops) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    unsigned long long nl = 0;
-    if (tloops && gw == 0 && lane == 0) tloops[n] = 0;
-    for (uint64_t v = gw; v < n; v += nw) {
-        const uint64_t s0 = __ldg(off + v), s1 = __ldg(off + v + 1);
-        uint32_t own = 0;
-        for (uint64_t e = s0 + lane; e < s1; e += 32) {
-            const uint32_t s = __ldg(succ + e);
-            if (s == (uint32_t)v)
-                own++;
-            else
-                atomicAdd(indeg + s, 1u);
-        }
-        nl += own;
-        if (tloops) {
-            for (int o = 16; o > 0; o >>= 1) own += __shfl_xor_sync(0xffffffffu, own, o);
-            if (lane == 0) tloops[v] = own;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) nl += __shfl_xor_sync(0xffffffffu, nl, o);
-    if (lane == 0 && nl) atomicAdd(loops, nl);
-}
-
-// rows[v] += indeg[v] for v < n
+// rows[v] += indeg[v] for v < n: transpose row lengths from in-degrees and self-loops
 __global__ void k_add_indeg(unsigned long long* __restrict__ rows, const uint32_t* __restrict__ indeg,
                             uint64_t n) {
     for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
@@ -875,18 +840,128 @@ __global__ void k_perm_degree(const uint64_t* __restrict__ off0, const uint32_t*
     }
 }
 
-// one warp per renumbered node: its successor list, renumbered
-__global__ void k_relabel_succ(const uint64_t* __restrict__ off0, const uint32_t* __restrict__ succ0,
-                               const uint32_t* __restrict__ perm, const uint32_t* __restrict__ inv,
-                               const uint64_t* __restrict__ off, uint32_t* __restrict__ succ,
-                               uint64_t n) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t i = gw; i < n; i += nw) {
-        const uint32_t u = __ldg(perm + i);
-        const uint64_t s0 = __ldg(off0 + u), d = __ldg(off0 + u + 1) - s0, t0 = __ldg(off + i);
-        for (uint64_t j = lane; j < d; j += 32) succ[t0 + j] = __ldg(inv + __ldg(succ0 + s0 + j));
+// ---------------------------------------------------------------------------
+// Arc-parallel passes over a CSR: tiles of LBS_TILE consecutive arcs, every
+// thread on LBS_ITEMS arcs of its tile (coalesced), the source of each arc
+// found in shared memory: the nodes whose rows start inside the tile are
+// written at their start positions, and a running maximum over the tile
+// carries each of them to the rest of its row. tile_start[k] is the node
+// holding arc k * LBS_TILE.
+// ---------------------------------------------------------------------------
+constexpr int LBS_THREADS = 256, LBS_ITEMS = 8, LBS_TILE = LBS_THREADS * LBS_ITEMS;
+
+__global__ void k_tile_start(const uint64_t* __restrict__ off, uint64_t n, uint32_t* __restrict__ tile_start) {
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = __ldg(off + v), b = __ldg(off + v + 1);
+        for (uint64_t k = (a + LBS_TILE - 1) / LBS_TILE; k * LBS_TILE < b; k++) tile_start[k] = (uint32_t)v;
+    }
+}
+
+// src[i] = source node of arc base + i, i < LBS_TILE (entries past the last
+// arc are meaningless); ends with a barrier
+__device__ __forceinline__ void lbs_sources(const uint64_t* __restrict__ off, uint64_t n, uint64_t m,
+                                            const uint32_t* __restrict__ tile_start, uint64_t ntiles,
+                                            uint64_t k, uint32_t* src, uint32_t* warp_max) {
+    const uint64_t base = k * LBS_TILE;
+    const uint64_t lo = tile_start[k], hi = k + 1 < ntiles ? tile_start[k + 1] : n - 1;
+    for (int i = threadIdx.x; i < LBS_TILE; i += LBS_THREADS) src[i] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(src, (uint32_t)lo);
+    for (uint64_t v = lo + 1 + threadIdx.x; v <= hi; v += LBS_THREADS) {
+        const uint64_t o = __ldg(off + v);
+        if (o >= base && o < base + LBS_TILE && o < m) atomicMax(src + (o - base), (uint32_t)v);
+    }
+    __syncthreads();
+    // inclusive running maximum: per thread over its LBS_ITEMS entries, then
+    // across the warp and the block
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x[LBS_ITEMS], run = 0;
+#pragma unroll
+    for (int j = 0; j < LBS_ITEMS; j++) {
+        run = max(run, src[threadIdx.x * LBS_ITEMS + j]);
+        x[j] = run;
+    }
+    uint32_t w = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w = max(w, y);
+    }
+    if (lane == 31) warp_max[warp] = w;
+    __syncthreads();
+    uint32_t before = __shfl_up_sync(0xffffffffu, w, 1);
+    if (lane == 0) before = 0;
+    for (int q = 0; q < warp; q++) before = max(before, warp_max[q]);
+#pragma unroll
+    for (int j = 0; j < LBS_ITEMS; j++) src[threadIdx.x * LBS_ITEMS + j] = max(x[j], before);
+    __syncthreads();
+}
+
+// The renumbered successors: arc e of new node i is arc e - off[i] of caller
+// row perm[i], its target mapped through inv. Out-of-range targets set *bad
+// (and are written as 0). With indeg: in-degrees without self-loops, and the
+// self-loops into *loops and, with trows, trows[i] (zeroed by the caller).
+__global__ void __launch_bounds__(LBS_THREADS) k_relabel_arcs(
+    const uint64_t* __restrict__ off, uint64_t n, uint64_t m, const uint32_t* __restrict__ tile_start,
+    uint64_t ntiles, const uint32_t* __restrict__ perm, const uint64_t* __restrict__ off0,
+    const uint32_t* __restrict__ succ0, const uint32_t* __restrict__ inv, uint32_t* __restrict__ succ,
+    uint32_t* __restrict__ indeg, unsigned long long* __restrict__ loops,
+    unsigned long long* __restrict__ trows, int* __restrict__ bad) {
+    __shared__ uint32_t src[LBS_TILE];
+    __shared__ uint32_t warp_max[LBS_THREADS / 32];
+    uint32_t nl = 0;
+    for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        lbs_sources(off, n, m, tile_start, ntiles, k, src, warp_max);
+        const uint64_t base = k * LBS_TILE;
+#pragma unroll 4
+        for (int j = 0; j < LBS_ITEMS; j++) {
+            const uint64_t e = base + j * LBS_THREADS + threadIdx.x;
+            if (e >= m) break;
+            const uint32_t i = src[j * LBS_THREADS + threadIdx.x];
+            const uint32_t s0 = __ldg(succ0 + __ldg(off0 + __ldg(perm + i)) + (e - __ldg(off + i)));
+            uint32_t t = 0;
+            if (s0 < n)
+                t = __ldg(inv + s0);
+            else
+                *bad = 1;
+            succ[e] = t;
+            if (indeg && s0 < n) {
+                if (t == i) {
+                    nl++;
+                    if (trows) atomicAdd(trows + i, 1ull);
+                } else {
+                    atomicAdd(indeg + t, 1u);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (indeg) {
+        for (int o = 16; o > 0; o >>= 1) nl += __shfl_xor_sync(0xffffffffu, nl, o);
+        if ((threadIdx.x & 31) == 0 && nl) atomicAdd(loops, (unsigned long long)nl);
+    }
+}
+
+// transpose scatter: arc i -> s becomes s -> i at the row cursor of s
+__global__ void __launch_bounds__(LBS_THREADS) k_scatter_arcs(
+    const uint64_t* __restrict__ off, uint64_t n, uint64_t m, const uint32_t* __restrict__ tile_start,
+    uint64_t ntiles, const uint32_t* __restrict__ succ, unsigned long long* __restrict__ cursor,
+    uint32_t* __restrict__ tsucc) {
+    __shared__ uint32_t src[LBS_TILE];
+    __shared__ uint32_t warp_max[LBS_THREADS / 32];
+    for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        lbs_sources(off, n, m, tile_start, ntiles, k, src, warp_max);
+        const uint64_t base = k * LBS_TILE;
+#pragma unroll
+        for (int j = 0; j < LBS_ITEMS; j++) {
+            const uint64_t e = base + j * LBS_THREADS + threadIdx.x;
+            if (e < m) {
+                const unsigned long long pos = atomicAdd(cursor + __ldg(succ + e), 1ull);
+                tsucc[pos] = src[j * LBS_THREADS + threadIdx.x];
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1339,14 +1414,6 @@ int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n
     return (int)cudaGetLastError();
 }
 
-int launch_indeg_noloop(const uint64_t* off, const uint32_t* succ, uint64_t n, uint32_t* indeg,
-                        unsigned long long* loops, unsigned long long* tloops, void* stream) {
-    const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256 + 1, 16384);
-    ++t_launches;
-    k_indeg_noloop<<<grid, 256, 0, (cudaStream_t)stream>>>(off, succ, n, indeg, loops, tloops);
-    return (int)cudaGetLastError();
-}
-
 int launch_inst_stats(const uint32_t* next_mod, const double* est, const uint64_t* starts,
                       uint32_t count, unsigned long long* mods, double* nfs, void* stream) {
     const int grid = (int)std::min<uint64_t>(((uint64_t)count * 32 + 255) / 256 + 1, 8192);
@@ -1372,12 +1439,37 @@ int launch_perm_degree(const uint64_t* off0, const uint32_t* perm, uint64_t n,
     return (int)cudaGetLastError();
 }
 
-int launch_relabel_succ(const uint64_t* off0, const uint32_t* succ0, const uint32_t* perm,
-                        const uint32_t* inv, const uint64_t* off, uint32_t* succ, uint64_t n,
-                        void* stream) {
-    const int grid = (int)std::min<uint64_t>((n * 32 + 255) / 256 + 1, 16384);
+uint64_t arc_tiles(uint64_t m) { return (m + LBS_TILE - 1) / LBS_TILE; }
+
+int launch_tile_start(const uint64_t* off, uint64_t n, uint32_t* tile_start, void* stream) {
+    if (n == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, 8192);
     ++t_launches;
-    k_relabel_succ<<<grid, 256, 0, (cudaStream_t)stream>>>(off0, succ0, perm, inv, off, succ, n);
+    k_tile_start<<<grid, 256, 0, (cudaStream_t)stream>>>(off, n, tile_start);
+    return (int)cudaGetLastError();
+}
+
+static int arc_grid(uint64_t ntiles) { return (int)std::min<uint64_t>(ntiles, 1u << 20); }
+
+int launch_relabel_arcs(const uint64_t* off, uint64_t n, uint64_t m, const uint32_t* tile_start,
+                        const uint32_t* perm, const uint64_t* off0, const uint32_t* succ0,
+                        const uint32_t* inv, uint32_t* succ, uint32_t* indeg, unsigned long long* loops,
+                        unsigned long long* trows, int* bad, void* stream) {
+    const uint64_t nt = arc_tiles(m);
+    if (nt == 0) return 0;
+    ++t_launches;
+    k_relabel_arcs<<<arc_grid(nt), LBS_THREADS, 0, (cudaStream_t)stream>>>(
+        off, n, m, tile_start, nt, perm, off0, succ0, inv, succ, indeg, loops, trows, bad);
+    return (int)cudaGetLastError();
+}
+
+int launch_scatter_arcs(const uint64_t* off, uint64_t n, uint64_t m, const uint32_t* tile_start,
+                        const uint32_t* succ, unsigned long long* cursor, uint32_t* tsucc, void* stream) {
+    const uint64_t nt = arc_tiles(m);
+    if (nt == 0) return 0;
+    ++t_launches;
+    k_scatter_arcs<<<arc_grid(nt), LBS_THREADS, 0, (cudaStream_t)stream>>>(off, n, m, tile_start, nt,
+                                                                         succ, cursor, tsucc);
     return (int)cudaGetLastError();
 }
 
