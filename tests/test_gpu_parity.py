@@ -38,6 +38,21 @@ def test_jenkins_hash(hb, oracle, log2m):
     lockstep(hb, oracle, g, log2m, hash_kind=1, seed=42, transpose=g.transpose())
 
 
+@pytest.mark.parametrize("log2m", [4, 5, 6, 7, 8, 9])
+@pytest.mark.parametrize("far_rows", [1, 300])
+def test_tma_far_gathers(hb, oracle, log2m, far_rows):
+    """Successors farther than far_rows ids come by TMA gathers (four per arc
+    lane, the rest by plain loads): the counters stay bit-exact, in standard,
+    gather-all and systolic iterations and through the medium-node path."""
+    g = hb.Graph.weblike(6000, cap=200, window=512, seed=log2m)
+    lockstep(hb, oracle, g, log2m, transpose_on_device=True, far_rows=far_rows)
+
+
+def test_plain_loads_only(hb, oracle):
+    g = hb.Graph.rmat(12, 8, seed=6)
+    lockstep(hb, oracle, g, 6, transpose_on_device=True, tma=False)
+
+
 def test_transpose_on_device(hb, oracle):
     g = hb.Graph.rmat(12, 8, seed=5)
     lockstep(hb, oracle, g, 6, transpose_on_device=True)

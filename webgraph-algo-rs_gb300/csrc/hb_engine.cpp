@@ -134,6 +134,10 @@ struct hb_handle {
     uint64_t* d_weights = nullptr;
     uint32_t* d_tiles = nullptr;  // window boundaries
     uint32_t* d_arc_tiles = nullptr;  // creation only: first node of each arc tile of d_off
+    // TMA descriptors of d_cnt[0] / d_cnt[1] for the far gathers, when usable
+    CUtensorMap far_map[2];
+    bool far_ok = false;
+    uint32_t far_rows = 8192;
     uint64_t n_tiles = 0;         // number of windows
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
     uint32_t* d_indeg = nullptr;    // in-degree without self-loops
@@ -539,6 +543,9 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.acc_slot = (uint32_t)(h->n_partials - 1);
     a.cursor = h->d_cursor;
     a.partials = h->d_partials;
+    a.far_tma = h->far_ok ? 1 : 0;
+    a.far_rows = h->far_rows;
+    if (h->far_ok) a.far_map = h->far_map[h->cur];
     return a;
 }
 
@@ -682,6 +689,8 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partials, sizeof(tot), cudaMemcpyDeviceToHost, s));
     HB_CUDA(h, cudaEventRecord(h->ev[3], s));
     HB_CUDA(h, cudaStreamSynchronize(s));
+    if (tot.timeouts)
+        return set_err(h, HB_ERR_TIMEOUT, "a TMA gather did not complete within its bounded wait");
     struct {
         unsigned long long st[4];
         double nf;
@@ -1388,6 +1397,10 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     const uint64_t n = h->n;
     if ((r = dalloc(hp, &h->d_cnt[0], n * h->stride))) return fail(r);
     if ((r = dalloc(hp, &h->d_cnt[1], n * h->stride))) return fail(r);
+    if (o.far_rows) h->far_rows = std::min<uint32_t>(o.far_rows, 0x7fffffffu);
+    if (!(o.flags & HB_NO_TMA_GATHER))
+        h->far_ok = hbk::encode_far_map(h->log2m, h->d_cnt[0], n, &h->far_map[0]) == 0 &&
+                    hbk::encode_far_map(h->log2m, h->d_cnt[1], n, &h->far_map[1]) == 0;
     const uint64_t words = (n + 31) / 32;
     for (int b = 0; b < 4; b++)
         if ((r = dalloc(hp, &h->d_bits[b], words))) return fail(r);

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
 #include <vector_types.h>
 
 #include "../../include/hyperball_gb300.h"
@@ -41,10 +42,14 @@ struct TilePartial {
     unsigned long long mod;       // modified counters
     unsigned long long scanned;   // scanned nodes
     unsigned long long sarcs;     // arcs of the scanned nodes
+    unsigned long long timeouts;  // bounded mbarrier waits that gave up (an error)
 };
 
 // Everything the union kernels read or write in one iteration.
 struct UnionArgs {
+    CUtensorMap far_map;      // the current counters as rows of 2^log2m bytes (TMA gathers)
+    int far_tma;              // 1: far successors by TMA gathers (far_map valid)
+    uint32_t far_rows;        // a successor is far when more than this many ids from its node
     const uint64_t* off;      // CSR offsets, n+1
     const uint32_t* succ;     // CSR successors, m
     const uint8_t* curr;      // current counters, n * 2^log2m bytes (byte per register)
@@ -136,6 +141,10 @@ int launch_gather_f64(const double* src, const uint32_t* inv, double* dst, uint6
                       void* stream);
 // persistent tile kernel over the worklist (or all tiles)
 int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream);
+// A TMA descriptor for a counter array (n rows of 2^log2m bytes) as the union
+// kernel's far gathers read it; nonzero when the TMA path is not available
+// for this size (log2m > 8, n >= 2^31) or the driver cannot encode it.
+int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* out);
 int tile_grid(int log2m, int device);
 // nodes and staged arcs one tile holds at this log2m
 int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);

@@ -230,17 +230,32 @@ struct TileGeo {
     static constexpr int ARCS = 1 << 30;  // no per-window arc limit
 };
 
+// Far successors: more than far_rows ids away from the node (mostly not in
+// L2). The first FAR_SLOTS far successors of an arc lane that pass the filter
+// come by one TMA gather (see collect_far); gather_rolling then skips them.
+constexpr int FAR_SLOTS = 4;
+__device__ __forceinline__ bool is_far(uint32_t s, uint32_t v, uint32_t far_rows) {
+    return s - v + far_rows > 2 * far_rows;
+}
+
 // Merges into acc (chunk c) the counters of the successors e0, e0+stride, ...
 // (< e1) of node v: all of them, or (filter) only the non-loop ones modified
-// in the previous iteration. A rolling pipeline keeps PIPE counter loads in
-// flight per lane: slot k merges its counter, then reloads with the id that
-// was fetched one round earlier and fetches the id after it.
+// in the previous iteration; the first `skip` far ones that qualify are left
+// out (they arrive by TMA). PIPE counter loads stay in flight per lane.
 template <int LOG2M>
 __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
                                                uint64_t e1, uint32_t stride, bool filter,
-                                               uint32_t (&acc)[Geo<LOG2M>::NW]) {
+                                               uint32_t (&acc)[Geo<LOG2M>::NW], int skip) {
     using Gm = Geo<LOG2M>;
     constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIPE = pipe_depth<NW>();
+    auto wanted = [&](uint32_t s) {
+        bool w = !filter || (s != v && test_bit(a.curr_mod, s));
+        if (skip > 0 && w && is_far(s, v, a.far_rows)) {
+            skip--;
+            w = false;
+        }
+        return w;
+    };
     if constexpr (PIPE == 1) {
         // one counter in flight: the next successor id loads while the current
         // counter is merged
@@ -248,12 +263,12 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
         const uint32_t* sp = a.succ + e0;
         const uint32_t cnt = (uint32_t)((e1 - e0 + stride - 1) / stride);
         uint32_t s = __ldg(sp);
-        bool have = !filter || (s != v && test_bit(a.curr_mod, s));
+        bool have = wanted(s);
         uint32_t y[NW];
         if (have) load_chunk<LOG2M>(a.curr, s, c, y);
         for (uint32_t i = 1; i < cnt; i++) {
             const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
-            const bool nh = !filter || (ns != v && test_bit(a.curr_mod, ns));
+            const bool nh = wanted(ns);
             if (have) merge_chunk<REGS>(acc, y);
             if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
             have = nh;
@@ -269,7 +284,7 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
             const uint32_t sid = e < e1 ? __ldg(a.succ + e) : v;
             const uint64_t en = e + (uint64_t)PIPE * stride;
             nid[k] = en < e1 ? __ldg(a.succ + en) : v;
-            have[k] = e < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+            have[k] = e < e1 && wanted(sid);
             if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
         }
         for (uint64_t e = e0 + (uint64_t)PIPE * stride; e < e1 + (uint64_t)PIPE * stride;
@@ -281,7 +296,7 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
                 const uint32_t sid = nid[k];
                 const uint64_t en = ek + (uint64_t)PIPE * stride;
                 nid[k] = en < e1 ? __ldg(a.succ + en) : v;
-                have[k] = ek < e1 && (!filter || (sid != v && test_bit(a.curr_mod, sid)));
+                have[k] = ek < e1 && wanted(sid);
                 if (have[k]) load_chunk<LOG2M>(a.curr, sid, c, y[k]);
             }
         }
@@ -289,90 +304,111 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
 }
 
 // ---------------------------------------------------------------------------
-// Shared-memory ring for successor counters: every lane keeps RING counter
-// copies in flight with cp.async (16-byte pieces, cached in L1 as well), so
-// the gather depth per lane costs shared memory instead of registers and more
-// warps stay resident. Lane `lane`'s piece q of slot j sits at
-// ((j * PIECES + q) * 32 + lane) * 16 bytes of its warp's ring: the 32 lanes'
-// 16-byte accesses are contiguous, without bank conflicts.
+// TMA gathers of far successors. Every lane group (the G lanes of one counter)
+// owns FAR_SLOTS counter rows of its warp's shared memory; one
+// cp.async.bulk.tensor tile::gather4 copy fills them from the tensor map of
+// the current counters (rows of 2^log2m bytes), and the warp's mbarrier
+// counts the bytes in. The copies run while the lanes gather their near
+// successors with plain loads.
 // ---------------------------------------------------------------------------
-constexpr int RING = 0;
-
 template <int LOG2M>
-struct RingGeo {
-    static constexpr int PIECES = Geo<LOG2M>::CHUNK_BYTES / 16;
-    static constexpr int WARP_BYTES = RING * PIECES * 32 * 16;
+struct FarGeo {
+    static constexpr bool ON = LOG2M <= 8;  // a box row is at most 256 bytes
+    static constexpr int ROW = Geo<LOG2M>::COUNTER_BYTES;
+    static constexpr int GROUPS = 32 / Geo<LOG2M>::CHUNKS;
+    // a group's rows start on a 128-byte boundary
+    static constexpr int REGION = FAR_SLOTS * ROW < 128 ? 128 : FAR_SLOTS * ROW;
+    static constexpr int WARP_BYTES = ON ? GROUPS * REGION : 0;
 };
 
-__device__ __forceinline__ void cp_async_16(uint32_t smem, const void* g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem), "l"(g) : "memory");
+// the bounded wait gives up after this many polls (each poll may suspend the
+// thread for a while); the kernel then reports a timeout
+constexpr int MBAR_POLLS = 1 << 20;
+
+__device__ __forceinline__ void mbar_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_arrive_expect(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+    uint32_t done = 0;
+    for (int i = 0; i < MBAR_POLLS && !done; i++)
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(phase)
+            : "memory");
+    return done != 0;
+}
+// orders this thread's earlier shared-memory reads before later TMA writes
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tma_gather4(uint32_t dst, const CUtensorMap* map, uint32_t r0,
+                                            uint32_t r1, uint32_t r2, uint32_t r3, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(map), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(bar)
+        : "memory");
 }
 
-// gather_rolling with the successor counters staged in the lane's ring slots
-template <int LOG2M>
-__device__ __forceinline__ void gather_ring(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
-                                            uint64_t e1, uint32_t stride, bool filter,
-                                            uint32_t (&acc)[Geo<LOG2M>::NW], uint32_t ring) {
-    using Gm = Geo<LOG2M>;
-    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIECES = RingGeo<LOG2M>::PIECES;
-    const uint32_t lane16 = (threadIdx.x & 31) * 16;
-    auto issue = [&](int j, uint32_t s) {
-        const uint8_t* src =
-            a.curr + (uint64_t)s * Gm::COUNTER_BYTES + (uint64_t)c * Gm::CHUNK_BYTES;
+// The first FAR_SLOTS far successors among e0, e0+stride, ... (< e1) that
+// pass the filter, in arc order; unused slots repeat v. Returns how many.
+__device__ __forceinline__ int collect_far(const UnionArgs& a, uint32_t v, uint64_t e0, uint64_t e1,
+                                           uint32_t stride, bool filter, uint32_t (&f)[FAR_SLOTS]) {
+    int nf = 0;
 #pragma unroll
-        for (int q = 0; q < PIECES; q++)
-            cp_async_16(ring + (uint32_t)((j * PIECES + q) * 512) + lane16, src + 16 * q);
-    };
-    uint32_t have = 0;
-    uint32_t ids[RING];
+    for (int k = 0; k < FAR_SLOTS; k++) f[k] = v;
+    for (uint64_t e = e0; e < e1 && nf < FAR_SLOTS; e += stride) {
+        const uint32_t s = __ldg(a.succ + e);
+        if (is_far(s, v, a.far_rows) && (!filter || test_bit(a.curr_mod, s))) {
 #pragma unroll
-    for (int j = 0; j < RING; j++) {
-        const uint64_t e = e0 + (uint64_t)j * stride;
-        ids[j] = e < e1 ? __ldg(a.succ + e) : v;
-    }
-#pragma unroll
-    for (int j = 0; j < RING; j++) {
-        const uint64_t e = e0 + (uint64_t)j * stride;
-        const bool ok = e < e1 && (!filter || (ids[j] != v && test_bit(a.curr_mod, ids[j])));
-        if (ok) issue(j, ids[j]);
-        have |= (uint32_t)ok << j;
-        cp_async_commit();
-    }
-    uint64_t pos = e0 + (uint64_t)RING * stride;
-    uint32_t nid = pos < e1 ? __ldg(a.succ + pos) : v;
-    for (uint64_t base = e0; base < e1; base += (uint64_t)RING * stride) {
-#pragma unroll
-        for (int j = 0; j < RING; j++) {
-            cp_async_wait<RING - 1>();
-            if ((have >> j) & 1u) {
-                uint32_t y[NW];
-#pragma unroll
-                for (int q = 0; q < PIECES; q++) {
-                    uint32_t t0, t1, t2, t3;
-                    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
-                                 : "=r"(t0), "=r"(t1), "=r"(t2), "=r"(t3)
-                                 : "r"(ring + (uint32_t)((j * PIECES + q) * 512) + lane16));
-                    y[4 * q] = t0;
-                    y[4 * q + 1] = t1;
-                    y[4 * q + 2] = t2;
-                    y[4 * q + 3] = t3;
-                }
-                merge_chunk<REGS>(acc, y);
-            }
-            const bool ok = pos < e1 && (!filter || (nid != v && test_bit(a.curr_mod, nid)));
-            if (ok) issue(j, nid);
-            have = (have & ~(1u << j)) | ((uint32_t)ok << j);
-            cp_async_commit();
-            pos += stride;
-            nid = pos < e1 ? __ldg(a.succ + pos) : v;
+            for (int k = 0; k < FAR_SLOTS; k++)
+                if (k == nf) f[k] = s;
+            nf++;
         }
     }
+    return nf;
 }
+
+// Merges rows [0, nf) of the group's slots (chunk c of each) into acc.
+template <int LOG2M>
+__device__ __forceinline__ void merge_far(uint32_t region, int c, int nf,
+                                          uint32_t (&acc)[Geo<LOG2M>::NW]) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW;
+    for (int j = 0; j < nf; j++) {
+        const uint32_t p = region + (uint32_t)(j * FarGeo<LOG2M>::ROW + c * Gm::CHUNK_BYTES);
+        uint32_t y[NW];
+#pragma unroll
+        for (int q = 0; q < NW / 4; q++)
+            asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(y[4 * q]), "=r"(y[4 * q + 1]), "=r"(y[4 * q + 2]), "=r"(y[4 * q + 3])
+                         : "r"(p + 16 * q));
+        merge_chunk<Gm::CHUNK_REGS>(acc, y);
+    }
+}
+
+// A warp's far-gather slots and mbarrier (dynamic and static shared memory of
+// the union kernel), and its state: bit 0 the barrier's phase, bit 1 set when
+// a wait gave up.
+extern __shared__ __align__(128) uint8_t far_smem[];
+__shared__ __align__(8) unsigned long long far_bar[8];
+template <int LOG2M>
+__device__ __forceinline__ uint32_t far_region(int lane) {
+    return (uint32_t)__cvta_generic_to_shared(far_smem) +
+           (threadIdx.x >> 5) * (uint32_t)FarGeo<LOG2M>::WARP_BYTES +
+           (uint32_t)((lane / Geo<LOG2M>::CHUNKS) * FarGeo<LOG2M>::REGION);
+}
+__device__ __forceinline__ uint32_t far_barrier() {
+    return (uint32_t)__cvta_generic_to_shared(&far_bar[threadIdx.x >> 5]);
+}
+struct FarState {
+    uint32_t bits;
+};
 
 // true when chunk c of counter v in `base` differs from w (read 32 bytes at a
 // time, so few registers are live)
@@ -404,7 +440,7 @@ __device__ __forceinline__ bool differs_from(const uint8_t* __restrict__ base, u
 template <int LOG2M, int TB>
 __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
                                           uint32_t b, uint32_t e, uint32_t& modc, uint32_t& scanned,
-                                          uint32_t& sarcs, uint32_t& vis, double& nf, uint32_t ring) {
+                                          uint32_t& sarcs, uint32_t& vis, double& nf, FarState& fs) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, NW = Gm::NW;
     constexpr int PB = TB / G;   // arc lanes per node
@@ -424,9 +460,35 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
             else if (test_bit(a.curr_mod, v))
                 copy = true;
         }
+        uint64_t s0 = 0, s1 = 0;
+        if (scan) {
+            s0 = __ldg(a.off + v);
+            s1 = __ldg(a.off + v + 1);
+        }
+        // far successors: one TMA gather per lane group, in flight during the
+        // plain loads below
+        int nfar = 0;
+        bool far_used = false;
+        if constexpr (FarGeo<LOG2M>::ON) {
+            if (a.far_tma) {
+                uint32_t f[FAR_SLOTS];
+                if (scan) nfar = collect_far(a, v, s0 + p, s1, PB, filter, f);
+                const bool issue = nfar > 0 && c == 0;
+                const unsigned im = __ballot_sync(0xffffffffu, issue);
+                if (im) {
+                    far_used = true;
+                    if (lane == 0)
+                        mbar_arrive_expect(far_barrier(),
+                                           (uint32_t)__popc(im) * FAR_SLOTS * FarGeo<LOG2M>::ROW);
+                    __syncwarp();
+                    if (issue)
+                        tma_gather4(far_region<LOG2M>(lane), &a.far_map, f[0], f[1], f[2], f[3],
+                                    far_barrier());
+                }
+            }
+        }
         bool changed = false;
         if (scan) {
-            const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
             uint32_t acc[NW];
             if (PB == 1 || p == 0) {
                 load_chunk<LOG2M>(a.curr, v, c, acc);
@@ -434,10 +496,15 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
 #pragma unroll
                 for (int k = 0; k < NW; k++) acc[k] = 0u;
             }
-            if constexpr (RING > 0)
-                gather_ring<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc, ring);
-            else
-                gather_rolling<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc);
+            gather_rolling<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc, nfar);
+            if (nfar > 0) {
+                if (mbar_wait(far_barrier(), fs.bits & 1u)) {
+                    merge_far<LOG2M>(far_region<LOG2M>(lane), c, nfar, acc);
+                    fence_proxy_async();
+                } else {
+                    fs.bits |= 2u;
+                }
+            }
             if constexpr (PB > 1) {
                 __syncwarp(tmask);
 #pragma unroll
@@ -475,6 +542,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
             load_chunk<LOG2M>(a.curr, v, c, w);
             store_chunk<LOG2M>(a.next, v, c, w);
         }
+        if (far_used) fs.bits ^= 1u;
         // modified bits, aggregated over the lanes that hit the same word
         const bool flag = changed && p == 0 && c == 0;
         const unsigned want = __ballot_sync(0xffffffffu, flag);
@@ -493,8 +561,8 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
 template <int LOG2M, int TB>
 __device__ __forceinline__ void run_medium(const UnionArgs& a, uint32_t b, uint32_t e,
                                         uint32_t& modc, uint32_t& scanned, uint32_t& sarcs,
-                                        uint32_t& vis, double& nf) {
-    run_nodes<LOG2M, TB>(a, a.medium_list, b, e, modc, scanned, sarcs, vis, nf, 0u);
+                                        uint32_t& vis, double& nf, FarState& fs) {
+    run_nodes<LOG2M, TB>(a, a.medium_list, b, e, modc, scanned, sarcs, vis, nf, fs);
 }
 
 // Work item k: a chunk of the table, or (systolic) a run of the light list
@@ -533,14 +601,18 @@ __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
 }
 
 template <int LOG2M>
-__global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
+__global__ void __launch_bounds__(256, 3) k_union_window(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
     constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
     const int lane = threadIdx.x & 31;
-    extern __shared__ __align__(16) uint8_t ring_smem[];
-    const uint32_t ring = (uint32_t)__cvta_generic_to_shared(ring_smem) +
-                          (threadIdx.x >> 5) * (uint32_t)RingGeo<LOG2M>::WARP_BYTES;
+    // per warp: the mbarrier of its far-successor TMA copies
+    FarState fs{0u};
+    if (FarGeo<LOG2M>::ON && a.far_tma) {
+        if (lane == 0) mbar_init(far_barrier());
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        __syncwarp();
+    }
     constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
     // per-warp totals: at most one warp's share of the nodes and arcs of one
     // iteration, far below 2^32
@@ -565,9 +637,9 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
         const uint32_t cnt = d.y & 0x7fffffffu;
         double nf = 0.0;
         if (d.y >> 31)
-            run_medium<LOG2M, TB_MED>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf);
+            run_medium<LOG2M, TB_MED>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         else
-            run_nodes<LOG2M, G>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, ring);
+            run_nodes<LOG2M, G>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         // the item's neighbourhood-function part: fixed lanes, fixed order
         nf = warp_sum_f64(nf);
         if (lane == 0) a.nf_items[k - 1] = nf;
@@ -587,6 +659,8 @@ __global__ void __launch_bounds__(256, 3) k_union_window(UnionArgs a) {
         if (sarcs) atomicAdd(&t->sarcs, (unsigned long long)sarcs);
         if (vis) atomicAdd(&t->vis, (unsigned long long)vis);
     }
+    if (__any_sync(0xffffffffu, (fs.bits & 2u) != 0) && lane == 0)
+        atomicAdd(&a.partials[a.acc_slot].timeouts, 1ull);
 }
 
 // ---------------------------------------------------------------------------
@@ -622,7 +696,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
 #pragma unroll
                 for (int i = 0; i < NW; i++) acc[i] = prev[i] = 0u;
             }
-            gather_rolling<LOG2M>(a, (uint32_t)v, c, s0 + p, s1, P, !a.gather_all, acc);
+            gather_rolling<LOG2M>(a, (uint32_t)v, c, s0 + p, s1, P, !a.gather_all, acc, 0);
             __syncwarp();
 #pragma unroll
             for (int off = G; off < 32; off <<= 1) {
@@ -1347,15 +1421,63 @@ static int pack_impl(const uint8_t* src, const uint32_t* inv, uint8_t* dst, uint
 }
 
 template <int LOG2M>
-static int ring_bytes() { return RING > 0 ? 8 * RingGeo<LOG2M>::WARP_BYTES : 0; }
+static int far_bytes() { return 8 * FarGeo<LOG2M>::WARP_BYTES; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (EncodeTiledFn) nullptr;
+        }
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+template <int LOG2M>
+static int encode_far_impl(const uint8_t* counters, uint64_t n, CUtensorMap* out) {
+    if constexpr (!FarGeo<LOG2M>::ON) {
+        return 1;
+    } else {
+        if (n == 0 || n >= (1ull << 31) || ((uintptr_t)counters & 15u)) return 1;
+        EncodeTiledFn fn = encode_tiled();
+        if (!fn) return 1;
+        // rows of 2^log2m bytes; a box is one row (gather4 takes four rows)
+        const cuuint64_t dims[2] = {(cuuint64_t)FarGeo<LOG2M>::ROW, (cuuint64_t)n};
+        const cuuint64_t strides[1] = {(cuuint64_t)FarGeo<LOG2M>::ROW};
+        const cuuint32_t box[2] = {(cuuint32_t)FarGeo<LOG2M>::ROW, 1};
+        const cuuint32_t elem[2] = {1, 1};
+        const CUresult r = fn(out, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void*)counters, dims, strides, box,
+                              elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        return r == CUDA_SUCCESS ? 0 : 1;
+    }
+}
+
+int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* out) {
+#define CALL(L) encode_far_impl<L>(counters, n, out)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
 
 template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     static const cudaError_t attr = cudaFuncSetAttribute(
-        k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize, ring_bytes<LOG2M>());
+        k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize, far_bytes<LOG2M>());
     if (attr != cudaSuccess) return (int)attr;
     ++t_launches;
-    k_union_window<LOG2M><<<grid, 256, ring_bytes<LOG2M>(), s>>>(a);
+    k_union_window<LOG2M><<<grid, 256, far_bytes<LOG2M>(), s>>>(a);
     return (int)cudaGetLastError();
 }
 
@@ -1373,9 +1495,9 @@ template <int LOG2M>
 static int tile_grid_impl(int device) {
     int per_sm = 1;
     cudaFuncSetAttribute(k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         ring_bytes<LOG2M>());
+                         far_bytes<LOG2M>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M>, 256,
-                                                  ring_bytes<LOG2M>());
+                                                  far_bytes<LOG2M>());
     return std::max(1, per_sm) * num_sms(device);
 }
 

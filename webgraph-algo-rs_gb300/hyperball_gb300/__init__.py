@@ -48,6 +48,7 @@ HB_SUM_OF_DISTANCES = 1 << 0
 HB_SUM_OF_INVERSE_DISTANCES = 1 << 1
 HB_TRANSPOSE_ON_DEVICE = 1 << 2
 HB_NO_I32_SHIFT_QUIRK = 1 << 3
+HB_NO_TMA_GATHER = 1 << 4
 
 HB_CURRENT_STATE = 0
 HB_NEXT_STATE = 1
@@ -108,7 +109,7 @@ class Options(ctypes.Structure):
         ("hash_seed", ctypes.c_uint64),
         ("num_elements", ctypes.c_uint64),
         ("flags", ctypes.c_uint32),
-        ("reserved0", ctypes.c_uint32),
+        ("far_rows", ctypes.c_uint32),
         ("arc_granularity", ctypes.c_uint64),
         ("weights", ctypes.POINTER(ctypes.c_uint64)),
         ("weight_seed", ctypes.c_uint64),
@@ -479,6 +480,8 @@ class HyperBallBuilder:
         self._small = None
         self._medium = None
         self._quirk = True
+        self._tma = True
+        self._far_rows = None
 
     @staticmethod
     def new(graph, logic):
@@ -559,6 +562,14 @@ class HyperBallBuilder:
         self._quirk = bool(flag)
         return self
 
+    def tma_gather(self, flag, far_rows=None):
+        """Far successors (more than far_rows ids from their node, default
+        8192) by TMA gathers (default) or by plain loads; the results are the
+        same."""
+        self._tma = bool(flag)
+        self._far_rows = far_rows
+        return self
+
     def build(self):
         return HyperBall(self)
 
@@ -584,6 +595,10 @@ class HyperBall:
             flags |= HB_TRANSPOSE_ON_DEVICE
         if not b._quirk:
             flags |= HB_NO_I32_SHIFT_QUIRK
+        if not b._tma:
+            flags |= HB_NO_TMA_GATHER
+        if b._far_rows is not None:
+            o.far_rows = int(b._far_rows)
         o.flags = flags
         o.arc_granularity = b._gran
         o.device = b._device
