@@ -46,7 +46,7 @@ extern "C" {
 #define HB_SUM_OF_INVERSE_DISTANCES (1u << 1) /* HyperBallBuilder::sum_of_inverse_distances(true), HB:268-271 */
 #define HB_TRANSPOSE_ON_DEVICE (1u << 2)      /* build the transpose on the GPU (enables systolic iterations) */
 #define HB_NO_I32_SHIFT_QUIRK (1u << 3)       /* count() with +2^-31 for register value 31 instead of Rust's i32 wrap (HLL:178) */
-#define HB_NO_TMA_GATHER (1u << 4)            /* far successors by plain loads, not TMA gathers (tuning; same results) */
+#define HB_TMA_GATHER (1u << 4)               /* far successors by TMA gathers instead of plain loads (tuning; same results) */
 
 /* "choose automatically" value of the tuning fields of hb_options */
 #define HB_AUTO 0xffffffffu
@@ -79,7 +79,7 @@ typedef struct hb_options {
     uint64_t hash_seed;       /* seed of HB_HASH_JENKINS */
     uint64_t num_elements;    /* HLL upper bound on elements; 0 = num_nodes (or sum of weights) (HLL:346-350) */
     uint32_t flags;           /* HB_* flags above */
-    uint32_t far_rows;        /* successors more than this many ids from their node come by TMA gathers; 0 = 8192 (tuning; same results) */
+    uint32_t far_rows;        /* with HB_TMA_GATHER: successors more than this many ids from their node are far; 0 = 8192 */
     uint64_t arc_granularity; /* accepted for parity with HB:280-283; 0 = 16 Ki. The device balances work by degree buckets. */
     const uint64_t* weights;  /* optional node weights, host array of num_nodes (HB:286-290); NULL = all 1 */
     uint64_t weight_seed;     /* seeds the values added for weights (the reference uses a non-reproducible RNG, HB:1167-1174) */

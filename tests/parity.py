@@ -30,7 +30,7 @@ def assert_close(a, b, rtol, what):
 
 def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True, harm=True,
              transpose_on_device=False, buckets=None, max_iters=10_000, check_next=True,
-             discounts=(), tma=True, far_rows=None):
+             discounts=(), tma=False, far_rows=None):
     """Runs GPU and oracle side by side; returns (gpu, oracle, stats list)."""
     hasher = hb.JenkinsHasher(seed) if hash_kind == 1 else hb.DefaultHasher()
     logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(log2m).build_hasher(hasher).build()

@@ -45,12 +45,12 @@ def test_tma_far_gathers(hb, oracle, log2m, far_rows):
     lane, the rest by plain loads): the counters stay bit-exact, in standard,
     gather-all and systolic iterations and through the medium-node path."""
     g = hb.Graph.weblike(6000, cap=200, window=512, seed=log2m)
-    lockstep(hb, oracle, g, log2m, transpose_on_device=True, far_rows=far_rows)
+    lockstep(hb, oracle, g, log2m, transpose_on_device=True, tma=True, far_rows=far_rows)
 
 
-def test_plain_loads_only(hb, oracle):
-    g = hb.Graph.rmat(12, 8, seed=6)
-    lockstep(hb, oracle, g, 6, transpose_on_device=True, tma=False)
+def test_tma_far_gathers_rmat(hb, oracle):
+    g = hb.Graph.rmat(14, 8, seed=6)
+    lockstep(hb, oracle, g, 6, transpose_on_device=True, tma=True)
 
 
 def test_transpose_on_device(hb, oracle):

@@ -1398,7 +1398,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     if ((r = dalloc(hp, &h->d_cnt[0], n * h->stride))) return fail(r);
     if ((r = dalloc(hp, &h->d_cnt[1], n * h->stride))) return fail(r);
     if (o.far_rows) h->far_rows = std::min<uint32_t>(o.far_rows, 0x7fffffffu);
-    if (!(o.flags & HB_NO_TMA_GATHER))
+    if (o.flags & HB_TMA_GATHER)
         h->far_ok = hbk::encode_far_map(h->log2m, h->d_cnt[0], n, &h->far_map[0]) == 0 &&
                     hbk::encode_far_map(h->log2m, h->d_cnt[1], n, &h->far_map[1]) == 0;
     const uint64_t words = (n + 31) / 32;

@@ -437,7 +437,7 @@ __device__ __forceinline__ bool differs_from(const uint8_t* __restrict__ base, u
 // One warp-step over up to 32/TB nodes: the consecutive nodes [b, e), or
 // list[b .. e) when a list is given. Scan, copy or nothing; sets the modified
 // bits and counts scanned nodes, their arcs and the changed counters.
-template <int LOG2M, int TB>
+template <int LOG2M, int TB, bool FAR>
 __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
                                           uint32_t b, uint32_t e, uint32_t& modc, uint32_t& scanned,
                                           uint32_t& sarcs, uint32_t& vis, double& nf, FarState& fs) {
@@ -469,8 +469,8 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
         // plain loads below
         int nfar = 0;
         bool far_used = false;
-        if constexpr (FarGeo<LOG2M>::ON) {
-            if (a.far_tma) {
+        if constexpr (FAR && FarGeo<LOG2M>::ON) {
+            {
                 uint32_t f[FAR_SLOTS];
                 if (scan) nfar = collect_far(a, v, s0 + p, s1, PB, filter, f);
                 const bool issue = nfar > 0 && c == 0;
@@ -558,11 +558,11 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
 }
 
 // The medium path (measured: inlining it beats a separate call frame).
-template <int LOG2M, int TB>
+template <int LOG2M, int TB, bool FAR>
 __device__ __forceinline__ void run_medium(const UnionArgs& a, uint32_t b, uint32_t e,
                                         uint32_t& modc, uint32_t& scanned, uint32_t& sarcs,
                                         uint32_t& vis, double& nf, FarState& fs) {
-    run_nodes<LOG2M, TB>(a, a.medium_list, b, e, modc, scanned, sarcs, vis, nf, fs);
+    run_nodes<LOG2M, TB, FAR>(a, a.medium_list, b, e, modc, scanned, sarcs, vis, nf, fs);
 }
 
 // Work item k: a chunk of the table, or (systolic) a run of the light list
@@ -600,7 +600,9 @@ __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
     return make_uint2(f, min((uint32_t)NPW_M, w.n_medium - f) | 0x80000000u);
 }
 
-template <int LOG2M>
+// FAR: far successors by TMA gathers (an option: measured slower than plain
+// loads on the web-like and R-MAT workloads)
+template <int LOG2M, bool FAR>
 __global__ void __launch_bounds__(256, 3) k_union_window(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
@@ -608,7 +610,7 @@ __global__ void __launch_bounds__(256, 3) k_union_window(const __grid_constant__
     const int lane = threadIdx.x & 31;
     // per warp: the mbarrier of its far-successor TMA copies
     FarState fs{0u};
-    if (FarGeo<LOG2M>::ON && a.far_tma) {
+    if constexpr (FAR && FarGeo<LOG2M>::ON) {
         if (lane == 0) mbar_init(far_barrier());
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         __syncwarp();
@@ -637,9 +639,9 @@ __global__ void __launch_bounds__(256, 3) k_union_window(const __grid_constant__
         const uint32_t cnt = d.y & 0x7fffffffu;
         double nf = 0.0;
         if (d.y >> 31)
-            run_medium<LOG2M, TB_MED>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
+            run_medium<LOG2M, TB_MED, FAR>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         else
-            run_nodes<LOG2M, G>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
+            run_nodes<LOG2M, G, FAR>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         // the item's neighbourhood-function part: fixed lanes, fixed order
         nf = warp_sum_f64(nf);
         if (lane == 0) a.nf_items[k - 1] = nf;
@@ -1420,8 +1422,8 @@ static int pack_impl(const uint8_t* src, const uint32_t* inv, uint8_t* dst, uint
     return (int)cudaGetLastError();
 }
 
-template <int LOG2M>
-static int far_bytes() { return 8 * FarGeo<LOG2M>::WARP_BYTES; }
+template <int LOG2M, bool FAR>
+constexpr int far_bytes() { return FAR ? 8 * FarGeo<LOG2M>::WARP_BYTES : 0; }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against the driver library)
@@ -1471,14 +1473,24 @@ int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* 
 #undef CALL
 }
 
+template <int LOG2M, bool FAR>
+static int tile_launch(const UnionArgs& a, int grid, cudaStream_t s) {
+    constexpr int smem = far_bytes<LOG2M, FAR>();
+    if constexpr (smem > 48 * 1024) {
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            k_union_window<LOG2M, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (attr != cudaSuccess) return (int)attr;
+    }
+    ++t_launches;
+    k_union_window<LOG2M, FAR><<<grid, 256, smem, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
 template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
-    static const cudaError_t attr = cudaFuncSetAttribute(
-        k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize, far_bytes<LOG2M>());
-    if (attr != cudaSuccess) return (int)attr;
-    ++t_launches;
-    k_union_window<LOG2M><<<grid, 256, far_bytes<LOG2M>(), s>>>(a);
-    return (int)cudaGetLastError();
+    if constexpr (FarGeo<LOG2M>::ON)
+        if (a.far_tma) return tile_launch<LOG2M, true>(a, grid, s);
+    return tile_launch<LOG2M, false>(a, grid, s);
 }
 
 template <int LOG2M>
@@ -1494,10 +1506,7 @@ static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
 template <int LOG2M>
 static int tile_grid_impl(int device) {
     int per_sm = 1;
-    cudaFuncSetAttribute(k_union_window<LOG2M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         far_bytes<LOG2M>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M>, 256,
-                                                  far_bytes<LOG2M>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false>, 256, 0);
     return std::max(1, per_sm) * num_sms(device);
 }
 

@@ -48,7 +48,7 @@ HB_SUM_OF_DISTANCES = 1 << 0
 HB_SUM_OF_INVERSE_DISTANCES = 1 << 1
 HB_TRANSPOSE_ON_DEVICE = 1 << 2
 HB_NO_I32_SHIFT_QUIRK = 1 << 3
-HB_NO_TMA_GATHER = 1 << 4
+HB_TMA_GATHER = 1 << 4
 
 HB_CURRENT_STATE = 0
 HB_NEXT_STATE = 1
@@ -480,7 +480,7 @@ class HyperBallBuilder:
         self._small = None
         self._medium = None
         self._quirk = True
-        self._tma = True
+        self._tma = False
         self._far_rows = None
 
     @staticmethod
@@ -562,10 +562,10 @@ class HyperBallBuilder:
         self._quirk = bool(flag)
         return self
 
-    def tma_gather(self, flag, far_rows=None):
+    def tma_gather(self, flag=True, far_rows=None):
         """Far successors (more than far_rows ids from their node, default
-        8192) by TMA gathers (default) or by plain loads; the results are the
-        same."""
+        8192) by TMA gathers instead of plain loads (the default); the
+        results are the same."""
         self._tma = bool(flag)
         self._far_rows = far_rows
         return self
@@ -595,8 +595,8 @@ class HyperBall:
             flags |= HB_TRANSPOSE_ON_DEVICE
         if not b._quirk:
             flags |= HB_NO_I32_SHIFT_QUIRK
-        if not b._tma:
-            flags |= HB_NO_TMA_GATHER
+        if b._tma:
+            flags |= HB_TMA_GATHER
         if b._far_rows is not None:
             o.far_rows = int(b._far_rows)
         o.flags = flags
