@@ -238,6 +238,38 @@ __device__ __forceinline__ bool is_far(uint32_t s, uint32_t v, uint32_t far_rows
     return s - v + far_rows > 2 * far_rows;
 }
 
+template <int LOG2M, int FK>
+__device__ __forceinline__ void filtered_gather(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
+                                                uint64_t e1, uint32_t stride,
+                                                uint32_t (&acc)[Geo<LOG2M>::NW], int skip) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    for (uint64_t e = e0; e < e1; e += (uint64_t)FK * stride) {
+        uint32_t ids[FK];
+#pragma unroll
+        for (int k = 0; k < FK; k++) {
+            const uint64_t ek = e + (uint64_t)k * stride;
+            ids[k] = ek < e1 ? __ldg(a.succ + ek) : v;
+        }
+        uint32_t want = 0;
+#pragma unroll
+        for (int k = 0; k < FK; k++)
+            want |= (uint32_t)(ids[k] != v && test_bit(a.curr_mod, ids[k])) << k;
+        if (!want) continue;
+#pragma unroll
+        for (int k = 0; k < FK; k++) {
+            if (!((want >> k) & 1u)) continue;
+            if (skip > 0 && is_far(ids[k], v, a.far_rows)) {
+                skip--;
+                continue;
+            }
+            uint32_t y[NW];
+            load_chunk<LOG2M>(a.curr, ids[k], c, y);
+            merge_chunk<REGS>(acc, y);
+        }
+    }
+}
+
 // Merges into acc (chunk c) the counters of the successors e0, e0+stride, ...
 // (< e1) of node v: all of them, or (filter) only the non-loop ones modified
 // in the previous iteration; the first `skip` far ones that qualify are left
@@ -256,6 +288,17 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
         }
         return w;
     };
+    if (filter) {
+        // Filtered: the ids and modified bits of FK arcs load together, so
+        // their latencies overlap; then the counters of the modified ones, in
+        // arc order. Systolic iterations (few successors modified) take 16
+        // arcs at a time, filtered standard iterations (many modified) 4.
+        if (a.systolic)
+            filtered_gather<LOG2M, 16>(a, v, c, e0, e1, stride, acc, skip);
+        else
+            filtered_gather<LOG2M, 4>(a, v, c, e0, e1, stride, acc, skip);
+        return;
+    }
     if constexpr (PIPE == 1) {
         // one counter in flight: the next successor id loads while the current
         // counter is merged
