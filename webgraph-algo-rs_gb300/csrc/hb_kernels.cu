@@ -1102,16 +1102,24 @@ __global__ void __launch_bounds__(256) k_mark_preds(const uint32_t* __restrict__
     const uint64_t nwords = (n + 31) >> 5;
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t wi = gw; wi < nwords; wi += nw) {
-        uint32_t bits = __ldg(next_mod + wi);
-        while (bits) {
-            const int b = __ffs(bits) - 1;
-            bits &= bits - 1u;
-            const uint64_t v = (wi << 5) + (uint64_t)b;
-            const uint64_t e0 = __ldg(toff + v), e1 = __ldg(toff + v + 1);
-            for (uint64_t e = e0 + lane; e < e1; e += 32) {
-                const uint32_t p = __ldg(tsucc + e);
-                atomicOr(next_mbc + (p >> 5), 1u << (p & 31));
+    // a warp reads 32 bitmap words at once (one per lane), then walks the
+    // in-arcs of each modified node with all lanes
+    for (uint64_t base = gw * 32; base < nwords; base += nw * 32) {
+        const uint64_t wi = base + lane;
+        const uint32_t bits = wi < nwords ? __ldg(next_mod + wi) : 0u;
+        uint32_t busy = __ballot_sync(0xffffffffu, bits != 0u);
+        while (busy) {
+            const int src = __ffs(busy) - 1;
+            busy &= busy - 1u;
+            uint32_t b = __shfl_sync(0xffffffffu, bits, src);
+            while (b) {
+                const uint64_t v = ((base + (uint64_t)src) << 5) + (uint64_t)(__ffs(b) - 1);
+                b &= b - 1u;
+                const uint64_t e0 = __ldg(toff + v), e1 = __ldg(toff + v + 1);
+                for (uint64_t e = e0 + lane; e < e1; e += 32) {
+                    const uint32_t p = __ldg(tsucc + e);
+                    atomicOr(next_mbc + (p >> 5), 1u << (p & 31));
+                }
             }
         }
     }
