@@ -101,6 +101,9 @@ struct hb_handle {
     // configuration
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the heavy-node kernel runs here, beside the window kernel
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint64_t n = 0, m = 0;
     int log2m = 4;
     uint64_t counter_bytes = 0;   // the reference's packed counter size, 2^log2m * 5 / 8
@@ -245,6 +248,9 @@ void release(hb_handle* h) {
     h->bufs.clear();
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->fork) cudaEventDestroy(h->fork);
+    if (h->join) cudaEventDestroy(h->join);
+    if (h->side) cudaStreamDestroy(h->side);
 }
 
 // Static work order of the union kernels (the graph does not change), and the
@@ -663,12 +669,21 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         a.list_counts = h->d_word_off + words;
     }
     HB_CUDA(h, cudaEventRecord(h->ev[1], s));
-    if (h->n_tiles) HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, h->grid_tile, s));
     if (h->n_heavy) {
-        a.list = h->d_heavy;
-        a.list_len = h->n_heavy;
-        HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, a, h->grid_heavy, s));
+        // The heavy nodes (one CTA each) start first on the side stream; the
+        // window kernel's blocks take the SMs as they free up, so the long
+        // heavy nodes overlap the window work instead of forming a tail.
+        // They touch disjoint nodes; shared totals are atomics.
+        hbk::UnionArgs ah = a;
+        ah.list = h->d_heavy;
+        ah.list_len = h->n_heavy;
+        HB_CUDA(h, cudaEventRecord(h->fork, s));
+        HB_CUDA(h, cudaStreamWaitEvent(h->side, h->fork, 0));
+        HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, ah, h->grid_heavy, h->side));
+        HB_CUDA(h, cudaEventRecord(h->join, h->side));
     }
+    if (h->n_tiles) HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, h->grid_tile, s));
+    if (h->n_heavy) HB_CUDA(h, cudaStreamWaitEvent(s, h->join, 0));
     HB_CUDA(h, cudaEventRecord(h->ev[2], s));
     if (h->systolic)
         HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
@@ -1309,6 +1324,12 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
             release(hp);
             return r;
         }
+    if ((r = cuda_err(hp, cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming), "cudaEventCreate")) ||
+        (r = cuda_err(hp, cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming), "cudaEventCreate")) ||
+        (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking), "cudaStreamCreate"))) {
+        release(hp);
+        return r;
+    }
 
     auto fail = [&](int code) {
         g_global_err = hp->err;
