@@ -86,6 +86,9 @@ typedef struct hb_options {
     void* stream;             /* cudaStream_t to launch on; NULL = legacy default stream */
     uint32_t small_max_degree;  /* tuning: nodes up to this out-degree run one lane-group each; HB_AUTO = tuned default */
     uint32_t medium_max_degree; /* tuning: nodes up to this out-degree run one warp each, above: one CTA; HB_AUTO = tuned default */
+    uint32_t union_variant;     /* tuning: HB_AUTO = the autotuner picks the union-kernel variant per graph
+                                   (see hb_union_variant_count); else the index of a fixed variant.
+                                   Every variant gives bit-identical results. */
 } hb_options;
 
 /* Per-iteration statistics (reference: the progress-logger lines of
@@ -97,7 +100,8 @@ typedef struct hb_iter_stats {
     uint64_t scanned_nodes;      /* nodes whose successors were enumerated */
     double neighborhood_function;/* value appended to the neighbourhood function */
     double relative_increment;   /* HB:929-941 */
-    int32_t systolic, local, pre_local, reserved;
+    int32_t systolic, local, pre_local;
+    int32_t union_variant;       /* variant of the union kernels this iteration ran */
     double union_ms;             /* device time of the union kernels of this iteration */
     double iteration_ms;         /* device time of the whole iteration */
     uint64_t scanned_arcs;       /* arcs of the scanned nodes (successor ids read) */
@@ -178,6 +182,21 @@ int hb_reachable_nodes_from(const hb_handle* h, uint64_t node, double* out);
  * bytes [i*B, (i+1)*B), B = 2^log2m * 5 / 8, 5-bit registers packed LSB-first
  * in little-endian words). `bytes` must be num_nodes * B. */
 int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes);
+
+/* Variants of the union kernels. They differ in how successor counters are
+ * requested (plain loads, or software prefetch into L1 or L2 ahead of the
+ * loads) and in the registers per thread (3 or 4 resident blocks per SM);
+ * they give bit-identical results. With union_variant = HB_AUTO the library
+ * times them on the handle's own standard iterations (one iteration each,
+ * per kind of iteration: merging every successor or only modified ones) and
+ * keeps the fastest; the choice is remembered for later handles of a graph
+ * with the same nodes, arcs and log2m in the process. No reference
+ * counterpart: the reference has one code path (HB:960-1152). */
+int hb_union_variant_count(void);
+/* The variant chosen for each kind of iteration (0: standard iterations
+ * merging every successor, 1: standard iterations merging modified
+ * successors, 2: systolic); -1 while still being timed. */
+int hb_union_variant_chosen(const hb_handle* h, int32_t chosen[3]);
 
 /* Counter size in bytes and register width (HLL:301-303). */
 int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* register_size);

@@ -53,6 +53,49 @@ def test_tma_far_gathers_rmat(hb, oracle):
     lockstep(hb, oracle, g, 6, transpose_on_device=True, tma=True)
 
 
+@pytest.mark.parametrize("log2m", [4, 6, 8])
+@pytest.mark.parametrize("variant", range(5))
+def test_union_variants(hb, oracle, log2m, variant):
+    """Every union-kernel variant (prefetch into L1 or L2, 3 or 4 blocks per
+    SM) gives the oracle's counters, in every kind of iteration."""
+    assert hb.union_variant_count() == 5
+    g = hb.Graph.weblike(20_000, cap=3000, window=256, seed=variant)
+    lockstep(hb, oracle, g, log2m, transpose_on_device=True, variant=variant)
+
+
+def test_autotuner_identical_results(hb):
+    """The autotuner switches variants between iterations; the run equals a run
+    on one fixed variant, bit for bit."""
+    g = hb.Graph.weblike(1 << 19, seed=9)
+    assert g.num_arcs >= 1 << 22  # large enough to be tuned
+    logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(6).build()
+
+    def run(variant, runs):
+        h = (hb.HyperBallBuilder.new(g, logic).transpose_on_device(True)
+             .sum_of_distances(True).sum_of_inverse_distances(True).union_variant(variant).build())
+        used = set()
+        for _ in range(runs):
+            h.run_until_done()
+            used |= {s["union_variant"] for s in h.iteration_stats()}
+        out = (h.registers(0), h.neighborhood_function(), h.sum_of_distances(),
+               h.harmonic_centralities(), [s["modified_counters"] for s in h.iteration_stats()],
+               h.union_variants_chosen())
+        h.close()
+        return out, used
+
+    fixed, used0 = run(0, 1)
+    assert used0 == {0}
+    tuned, used = run(None, 2)
+    assert len(used) > 1, used
+    chosen = tuned[5]
+    assert chosen[0] >= 0 and chosen[2] >= 0, chosen
+    np.testing.assert_array_equal(tuned[0], fixed[0])
+    np.testing.assert_array_equal(tuned[1], fixed[1])
+    assert tuned[4] == fixed[4]
+    np.testing.assert_array_equal(tuned[2], fixed[2])
+    np.testing.assert_array_equal(tuned[3], fixed[3])
+
+
 def test_transpose_on_device(hb, oracle):
     g = hb.Graph.rmat(12, 8, seed=5)
     lockstep(hb, oracle, g, 6, transpose_on_device=True)
@@ -157,6 +200,8 @@ def test_errors(hb):
     bad = hb.Graph.from_csr(np.array([0, 1], dtype=np.uint64), np.array([5], dtype=np.uint32))
     with pytest.raises(hb.InvalidArgumentError):
         hb.HyperBallBuilder.new(bad, logic).build()
+    with pytest.raises(hb.InvalidArgumentError):
+        hb.HyperBallBuilder.new(g, logic).union_variant(hb.union_variant_count()).build()
 
 
 @pytest.mark.skipif(cnr_basename() is None, reason="cnr-2000 fixture not present")

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -27,6 +28,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "hb_internal.h"
@@ -96,6 +98,47 @@ cudaError_t pool_alloc(int device, void** p, size_t bytes, cudaStream_t s) {
 struct hb_graph {
     Csr g;
 };
+
+// ---------------------------------------------------------------------------
+// Autotuner of the union kernels. The variants differ only in how successor
+// counters are requested (software prefetch into L1 or L2 ahead of the plain
+// loads) and in the registers per thread (3 or 4 resident blocks per SM); they
+// give the same counters, sums and statistics, so the engine may switch
+// between them at any iteration. Per kind of iteration (standard merging every
+// successor, standard merging modified successors) each variant is timed on
+// one iteration that scans at least an eighth of the arcs and merges at least
+// half of what it scans, as union time per scanned-plus-merged arc; the
+// fastest is kept for the rest of the handle's life and remembered for later
+// handles of a graph with the same shape. Systolic iterations vary too much
+// from one to the next to be compared; they take the choice of the filtered
+// standard iterations (or of the others, or the first variant).
+// ---------------------------------------------------------------------------
+struct UnionVariant {
+    uint32_t pf, pd, occ;
+};
+constexpr UnionVariant kVariants[] = {{0, 0, 0}, {2, 2, 0}, {0, 0, 1}, {2, 2, 1}, {1, 4, 0}};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+constexpr int kTunedClasses = 2;  // gather-all standard, filtered standard
+constexpr uint64_t kTuneMinArcs = 1ull << 22;  // smaller graphs keep the first variant
+
+struct Tuner {
+    int fixed = -1;                            // a variant forced by the options
+    int chosen[kTunedClasses] = {-1, -1};
+    double best[kTunedClasses][kNumVariants] = {};
+    bool timed[kTunedClasses][kNumVariants] = {};
+    int last = 0;                              // the variant of the iteration in flight
+    int last_class = -1;                       // its class when it is a sample, else -1
+};
+
+struct TuneKey {
+    int device, log2m;
+    uint64_t n, m;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(device, log2m, n, m) < std::tie(o.device, o.log2m, o.n, o.m);
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, std::array<int, kTunedClasses>> g_tune_cache;
 
 struct hb_handle {
     // configuration
@@ -177,6 +220,8 @@ struct hb_handle {
     int* d_any31 = nullptr;
     bool any31 = false;
     int grid_tile = 1, grid_heavy = 1, grid_mark = 1;
+    int grid_tile_occ = 1;           // the window kernel's grid in its 4-blocks-per-SM variant
+    Tuner tuner;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // reference state (IterationContext + HyperBall fields)
@@ -551,6 +596,9 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.partials = h->d_partials;
     a.far_tma = h->far_ok ? 1 : 0;
     a.far_rows = h->far_rows;
+    a.pf = 0;
+    a.pd = 0;
+    a.occ = 0;
     if (h->far_ok) a.far_map = h->far_map[h->cur];
     return a;
 }
@@ -562,6 +610,45 @@ struct LaunchTally {
     explicit LaunchTally(hb_handle* hh) : h(hh), c0(hbk::launch_count()) {}
     ~LaunchTally() { h->launches += hbk::launch_count() - c0; }
 };
+
+// The union-kernel variant of the next iteration. `cls`: 0 standard merging
+// every successor, 1 standard merging modified successors, -1 systolic;
+// `sample`: the iteration is large and typical enough to time a variant on.
+int choose_variant(hb_handle* h, int cls, bool sample) {
+    Tuner& t = h->tuner;
+    t.last_class = -1;
+    if (t.fixed >= 0) return t.last = t.fixed;
+    if (cls < 0) return t.last = t.chosen[1] >= 0 ? t.chosen[1] : t.chosen[0] >= 0 ? t.chosen[0] : 0;
+    if (t.chosen[cls] >= 0) return t.last = t.chosen[cls];
+    if (sample)
+        for (int v = 0; v < kNumVariants; v++)
+            if (!t.timed[cls][v]) {
+                t.last_class = cls;
+                return t.last = v;
+            }
+    return t.last = 0;
+}
+
+// Records the union time per scanned-plus-merged arc of a sampled iteration;
+// once every variant of the class has a time, keeps the fastest.
+void record_variant(hb_handle* h, double union_ms, uint64_t arcs) {
+    Tuner& t = h->tuner;
+    const int cls = t.last_class;
+    if (cls < 0 || arcs == 0) return;
+    t.best[cls][t.last] = union_ms / (double)arcs;
+    t.timed[cls][t.last] = true;
+    int best = 0;
+    for (int v = 0; v < kNumVariants; v++) {
+        if (!t.timed[cls][v]) return;
+        if (t.best[cls][v] < t.best[cls][best]) best = v;
+    }
+    t.chosen[cls] = best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto& e = g_tune_cache.try_emplace(TuneKey{h->device, h->log2m, h->n, h->m},
+                                       std::array<int, kTunedClasses>{-1, -1})
+                  .first->second;
+    e[cls] = best;
+}
 
 int do_init(hb_handle* h) {
     const uint64_t n = h->n;
@@ -658,6 +745,14 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     // nearly every counter changed in the previous iteration: merge all
     // successors without waiting for their modified bits
     a.gather_all = !h->systolic && prev_mod >= n - n / 8;
+    // the union-kernel variant (identical results; see Tuner)
+    const uint64_t merged = a.gather_all ? m - h->self_loops : h->pending_visited;
+    const int cls = h->systolic ? -1 : a.gather_all ? 0 : 1;
+    const bool sample = h->iteration > 0 && m >= kTuneMinArcs && 2 * merged >= m;
+    const int variant = choose_variant(h, cls, sample);
+    a.pf = kVariants[variant].pf;
+    a.pd = kVariants[variant].pd;
+    a.occ = kVariants[variant].occ;
     if (h->systolic && h->n_tiles) {
         // the chunks of the windows holding a node to check or to copy
         HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_medium_bits, h->d_light_bits, n,
@@ -682,7 +777,8 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, ah, h->grid_heavy, h->side));
         HB_CUDA(h, cudaEventRecord(h->join, h->side));
     }
-    if (h->n_tiles) HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, h->grid_tile, s));
+    if (h->n_tiles)
+        HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, a.occ ? h->grid_tile_occ : h->grid_tile, s));
     if (h->n_heavy) HB_CUDA(h, cudaStreamWaitEvent(s, h->join, 0));
     HB_CUDA(h, cudaEventRecord(h->ev[2], s));
     if (h->systolic)
@@ -755,6 +851,8 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     st.union_ms = ms_union;
     st.iteration_ms = ms_all;
     st.scanned_arcs = host.st[3];
+    st.union_variant = h->tuner.last;
+    record_variant(h, ms_union, host.st[3] + merged);
     st.kernel_launches = hbk::launch_count() - launches0;
     h->stats.push_back(st);
     if (out) *out = st;
@@ -842,6 +940,7 @@ void hb_options_default(hb_options* o) {
     o->hash_kind = HB_HASH_SIP13;
     o->small_max_degree = HB_AUTO;
     o->medium_max_degree = HB_AUTO;
+    o->union_variant = HB_AUTO;
 }
 
 // ---- batches ------------------------------------------------------------------
@@ -1445,11 +1544,23 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
             return fail(r);
     }
     trace.mark("state arrays");
-    h->grid_tile = hbk::tile_grid(h->log2m, h->device);
+    h->grid_tile = hbk::tile_grid(h->log2m, h->device, 0);
+    h->grid_tile_occ = hbk::tile_grid(h->log2m, h->device, 1);
     {
         // one warp per chunk, 8 warps per block
         const uint64_t need = (h->n_chunks + 7) / 8 + 1;
         if ((uint64_t)h->grid_tile > need) h->grid_tile = (int)need;
+        if ((uint64_t)h->grid_tile_occ > need) h->grid_tile_occ = (int)need;
+    }
+    if (o.union_variant != HB_AUTO) {
+        if (o.union_variant >= (uint32_t)kNumVariants)
+            return fail(set_err(hp, HB_ERR_INVALID, "union_variant out of range"));
+        h->tuner.fixed = (int)o.union_variant;
+    } else {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(TuneKey{h->device, h->log2m, h->n, h->m});
+        if (it != g_tune_cache.end())
+            for (int c = 0; c < kTunedClasses; c++) h->tuner.chosen[c] = it->second[c];
     }
     h->grid_heavy = hbk::heavy_grid(h->log2m, h->device);
     if ((uint64_t)h->grid_heavy > h->n_heavy + 1) h->grid_heavy = (int)(h->n_heavy + 1);
@@ -1639,6 +1750,16 @@ int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes) {
         return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "which must be HB_CURRENT_STATE or HB_NEXT_STATE");
     // the device keeps a byte per register; pack into the reference's layout
     return copy_registers_range(h, which, dst, 0, h->n);
+}
+
+int hb_union_variant_count(void) { return kNumVariants; }
+
+int hb_union_variant_chosen(const hb_handle* h, int32_t chosen[3]) {
+    if (!h || !chosen) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "null argument");
+    const Tuner& t = h->tuner;
+    for (int c = 0; c < kTunedClasses; c++) chosen[c] = t.fixed >= 0 ? t.fixed : t.chosen[c];
+    chosen[2] = t.fixed >= 0 ? t.fixed : t.chosen[1] >= 0 ? t.chosen[1] : t.chosen[0] >= 0 ? t.chosen[0] : 0;
+    return HB_OK;
 }
 
 int hb_counter_layout(const hb_handle* h, uint64_t* counter_bytes, int* reg_size) {

@@ -90,6 +90,10 @@ struct UnionArgs {
     uint64_t heavy_item_base; // index of the first heavy node's part
     uint64_t n_chunks;
     unsigned long long* cursor; // next chunk to take (zero at launch)
+    // variant of the union kernels (same results; chosen by the autotuner)
+    uint32_t pf;              // successor counters prefetched: 0 no, 1 into L2, 2 into L1
+    uint32_t pd;              // prefetch distance in arcs
+    uint32_t occ;             // window kernel sized for 4 resident blocks per SM instead of 3
     uint32_t tile_max_degree; // nodes above this out-degree are listed as heavy
     uint32_t acc_slot;        // partial slot accumulating the union kernels' integer totals
     TilePartial* partials;    // one per finalize block, then acc_slot
@@ -145,7 +149,7 @@ int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream);
 // kernel's far gathers read it; nonzero when the TMA path is not available
 // for this size (log2m > 8, n >= 2^31) or the driver cannot encode it.
 int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* out);
-int tile_grid(int log2m, int device);
+int tile_grid(int log2m, int device, int occ);
 // nodes and staged arcs one tile holds at this log2m
 int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);
 // heavy nodes, one CTA each

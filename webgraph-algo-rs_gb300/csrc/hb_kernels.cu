@@ -256,6 +256,14 @@ __device__ __forceinline__ void filtered_gather(const UnionArgs& a, uint32_t v, 
         for (int k = 0; k < FK; k++)
             want |= (uint32_t)(ids[k] != v && test_bit(a.curr_mod, ids[k])) << k;
         if (!want) continue;
+        if (a.pf) {
+            // every wanted counter but the first is requested now, so the
+            // loads below find them on chip
+            const int first = __ffs(want) - 1;
+#pragma unroll
+            for (int k = 0; k < FK; k++)
+                if (k != first && ((want >> k) & 1u)) prefetch_chunk<LOG2M>(a.curr, ids[k], c, a.pf);
+        }
 #pragma unroll
         for (int k = 0; k < FK; k++) {
             if (!((want >> k) & 1u)) continue;
@@ -305,12 +313,17 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
         if (e0 >= e1) return;
         const uint32_t* sp = a.succ + e0;
         const uint32_t cnt = (uint32_t)((e1 - e0 + stride - 1) / stride);
+        const uint32_t pd = a.pf ? a.pd : 0u;
+        for (uint32_t k = 1; k <= pd && k < cnt; k++)
+            prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)k * stride), c, a.pf);
         uint32_t s = __ldg(sp);
         bool have = wanted(s);
         uint32_t y[NW];
         if (have) load_chunk<LOG2M>(a.curr, s, c, y);
         for (uint32_t i = 1; i < cnt; i++) {
             const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
+            if (pd && i + pd < cnt)
+                prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)(i + pd) * stride), c, a.pf);
             const bool nh = wanted(ns);
             if (have) merge_chunk<REGS>(acc, y);
             if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
@@ -645,8 +658,10 @@ __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
 
 // FAR: far successors by TMA gathers (an option: measured slower than plain
 // loads on the web-like and R-MAT workloads)
-template <int LOG2M, bool FAR>
-__global__ void __launch_bounds__(256, 3) k_union_window(const __grid_constant__ UnionArgs a) {
+// MINB: resident blocks per SM the registers are sized for (3: 80 registers
+// a thread, 4: 64; the autotuner picks one per graph)
+template <int LOG2M, bool FAR, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
     constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
@@ -1524,24 +1539,25 @@ int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* 
 #undef CALL
 }
 
-template <int LOG2M, bool FAR>
+template <int LOG2M, bool FAR, int MINB>
 static int tile_launch(const UnionArgs& a, int grid, cudaStream_t s) {
     constexpr int smem = far_bytes<LOG2M, FAR>();
     if constexpr (smem > 48 * 1024) {
         static const cudaError_t attr = cudaFuncSetAttribute(
-            k_union_window<LOG2M, FAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            k_union_window<LOG2M, FAR, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (attr != cudaSuccess) return (int)attr;
     }
     ++t_launches;
-    k_union_window<LOG2M, FAR><<<grid, 256, smem, s>>>(a);
+    k_union_window<LOG2M, FAR, MINB><<<grid, 256, smem, s>>>(a);
     return (int)cudaGetLastError();
 }
 
 template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     if constexpr (FarGeo<LOG2M>::ON)
-        if (a.far_tma) return tile_launch<LOG2M, true>(a, grid, s);
-    return tile_launch<LOG2M, false>(a, grid, s);
+        if (a.far_tma) return tile_launch<LOG2M, true, 3>(a, grid, s);
+    if (a.occ) return tile_launch<LOG2M, false, 4>(a, grid, s);
+    return tile_launch<LOG2M, false, 3>(a, grid, s);
 }
 
 template <int LOG2M>
@@ -1555,9 +1571,12 @@ static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
 
 
 template <int LOG2M>
-static int tile_grid_impl(int device) {
+static int tile_grid_impl(int device, int occ) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false>, 256, 0);
+    if (occ)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false, 4>, 256, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false, 3>, 256, 0);
     return std::max(1, per_sm) * num_sms(device);
 }
 
@@ -1675,8 +1694,8 @@ int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream) {
 #undef CALL
 }
 
-int tile_grid(int log2m, int device) {
-#define CALL(L) tile_grid_impl<L>(device)
+int tile_grid(int log2m, int device, int occ) {
+#define CALL(L) tile_grid_impl<L>(device, occ)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
 }

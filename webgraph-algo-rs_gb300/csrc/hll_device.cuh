@@ -199,6 +199,22 @@ __device__ __forceinline__ void load_chunk(const uint8_t* __restrict__ base, uin
     }
 }
 
+// Requests chunk c of counter `node` into L2 (level 1) or L1 (level 2)
+// without waiting for it: the sectors of a later load_chunk are then on chip.
+template <int LOG2M>
+__device__ __forceinline__ void prefetch_chunk(const uint8_t* __restrict__ base, uint64_t node, int c,
+                                               uint32_t level) {
+    using G = Geo<LOG2M>;
+    const uint8_t* p = base + node * (uint64_t)G::COUNTER_BYTES + (uint64_t)c * G::CHUNK_BYTES;
+    if (level == 2) {
+#pragma unroll
+        for (int i = 0; i < G::CHUNK_BYTES; i += 32) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + i));
+    } else {
+#pragma unroll
+        for (int i = 0; i < G::CHUNK_BYTES; i += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + i));
+    }
+}
+
 template <int LOG2M>
 __device__ __forceinline__ void store_chunk(uint8_t* __restrict__ base, uint64_t node, int c,
                                             const uint32_t (&w)[Geo<LOG2M>::NW]) {

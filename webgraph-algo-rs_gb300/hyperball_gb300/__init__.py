@@ -116,6 +116,7 @@ class Options(ctypes.Structure):
         ("stream", ctypes.c_void_p),
         ("small_max_degree", ctypes.c_uint32),
         ("medium_max_degree", ctypes.c_uint32),
+        ("union_variant", ctypes.c_uint32),
     ]
 
 
@@ -157,7 +158,7 @@ class IterStats(ctypes.Structure):
         ("systolic", ctypes.c_int32),
         ("local", ctypes.c_int32),
         ("pre_local", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("union_variant", ctypes.c_int32),
         ("union_ms", ctypes.c_double),
         ("iteration_ms", ctypes.c_double),
         ("scanned_arcs", ctypes.c_uint64),
@@ -165,7 +166,7 @@ class IterStats(ctypes.Structure):
     ]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 DISCOUNT_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p)
@@ -198,6 +199,8 @@ EXPORTS = [
     ("hb_reachable_nodes_from", ctypes.c_int, [_H, ctypes.c_uint64, _P(ctypes.c_double)]),
     ("hb_get_registers", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
     ("hb_counter_layout", ctypes.c_int, [_H, _P(ctypes.c_uint64), _P(ctypes.c_int)]),
+    ("hb_union_variant_count", ctypes.c_int, []),
+    ("hb_union_variant_chosen", ctypes.c_int, [_H, _P(ctypes.c_int32)]),
     ("hb_last_error", ctypes.c_char_p, [_H]),
     ("hb_global_last_error", ctypes.c_char_p, []),
     ("hb_graph_load_bvgraph", ctypes.c_int, [ctypes.c_char_p, _P(_H)]),
@@ -254,6 +257,11 @@ EXPORTS = [
 ]
 
 _lib = None
+
+
+def union_variant_count():
+    """Variants of the union kernels the autotuner chooses from."""
+    return int(load_library().hb_union_variant_count())
 
 
 def load_library(path=None):
@@ -482,6 +490,7 @@ class HyperBallBuilder:
         self._quirk = True
         self._tma = False
         self._far_rows = None
+        self._variant = None
 
     @staticmethod
     def new(graph, logic):
@@ -570,6 +579,13 @@ class HyperBallBuilder:
         self._far_rows = far_rows
         return self
 
+    def union_variant(self, index):
+        """A fixed variant of the union kernels (0 .. union_variant_count() - 1)
+        instead of the autotuner's choice (None); every variant gives the same
+        results."""
+        self._variant = None if index is None else int(index)
+        return self
+
     def build(self):
         return HyperBall(self)
 
@@ -607,6 +623,8 @@ class HyperBall:
             o.small_max_degree = b._small
         if b._medium is not None:
             o.medium_max_degree = b._medium
+        if b._variant is not None:
+            o.union_variant = b._variant
         if b._weights is not None:
             o.weights = b._weights.ctypes.data_as(_P(ctypes.c_uint64))
             o.weight_seed = b._weight_seed
@@ -722,6 +740,14 @@ class HyperBall:
     def kernel_launches(self):
         """CUDA kernels the library launched for this instance so far."""
         return int(self._lib.hb_kernel_launches(self._h))
+
+    def union_variants_chosen(self):
+        """The union-kernel variant kept for standard iterations merging every
+        successor, standard iterations merging modified successors, and
+        systolic iterations (-1: still being timed)."""
+        c = (ctypes.c_int32 * 3)()
+        _check(self._lib.hb_union_variant_chosen(self._h, c), self._h)
+        return list(c)
 
     def registers(self, which=HB_CURRENT_STATE):
         """Raw counter bytes (num_nodes x counter_bytes), reference layout."""
