@@ -47,6 +47,7 @@ extern "C" {
 #define HB_TRANSPOSE_ON_DEVICE (1u << 2)      /* build the transpose on the GPU (enables systolic iterations) */
 #define HB_NO_I32_SHIFT_QUIRK (1u << 3)       /* count() with +2^-31 for register value 31 instead of Rust's i32 wrap (HLL:178) */
 #define HB_TMA_GATHER (1u << 4)               /* far successors by TMA gathers instead of plain loads (tuning; same results) */
+#define HB_NO_GRAPHS (1u << 5)                /* launch every iteration directly instead of replaying CUDA graphs of repeated iteration shapes (same results) */
 
 /* "choose automatically" value of the tuning fields of hb_options */
 #define HB_AUTO 0xffffffffu
@@ -106,6 +107,8 @@ typedef struct hb_iter_stats {
     double iteration_ms;         /* device time of the whole iteration */
     uint64_t scanned_arcs;       /* arcs of the scanned nodes (successor ids read) */
     uint64_t kernel_launches;    /* CUDA kernels this library launched for the iteration */
+    int32_t from_graph;          /* 1: the iteration ran as a replay of a captured CUDA graph */
+    int32_t reserved;
 } hb_iter_stats;
 
 /* Discount function: weight of distance d >= 1 (reference: the closures of

@@ -30,7 +30,7 @@ def assert_close(a, b, rtol, what):
 
 def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True, harm=True,
              transpose_on_device=False, buckets=None, max_iters=10_000, check_next=True,
-             discounts=(), tma=False, far_rows=None, variant=None):
+             discounts=(), tma=False, far_rows=None, variant=None, graphs=True):
     """Runs GPU and oracle side by side; returns (gpu, oracle, stats list)."""
     hasher = hb.JenkinsHasher(seed) if hash_kind == 1 else hb.DefaultHasher()
     logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(log2m).build_hasher(hasher).build()
@@ -43,7 +43,7 @@ def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True
         b = b.discount_function(f)
     if buckets:
         b = b.degree_buckets(*buckets)
-    b = b.tma_gather(tma, far_rows).union_variant(variant)
+    b = b.tma_gather(tma, far_rows).union_variant(variant).cuda_graphs(graphs)
     gpu = b.build()
     has_t = transpose is not None or transpose_on_device
     t = transpose

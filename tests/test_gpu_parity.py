@@ -96,6 +96,23 @@ def test_autotuner_identical_results(hb):
     np.testing.assert_array_equal(tuned[3], fixed[3])
 
 
+@pytest.mark.parametrize("graphs", [False, True])
+def test_cuda_graph_iterations(hb, oracle, graphs):
+    """Iterations replayed from captured CUDA graphs (standard, first systolic
+    and systolic shapes; discount factors and 1/d from device memory) match
+    the oracle exactly as directly launched ones do."""
+    g = hb.Graph.weblike(30_000, cap=2000, window=256, seed=4)
+    gpu, orc, stats = lockstep(hb, oracle, g, 6, transpose_on_device=True, graphs=graphs,
+                               discounts=(lambda d: 1.0 / d, lambda d: 0.5 ** d))
+    replays = [sg["from_graph"] for sg, _ in stats]
+    if graphs:
+        assert any(replays), replays
+        assert any(sg["systolic"] and sg["from_graph"] for sg, _ in stats)
+        assert all(sg["kernel_launches"] > 0 for sg, _ in stats)
+    else:
+        assert not any(replays)
+
+
 def test_transpose_on_device(hb, oracle):
     g = hb.Graph.rmat(12, 8, seed=5)
     lockstep(hb, oracle, g, 6, transpose_on_device=True)

@@ -140,6 +140,25 @@ struct TuneKey {
 static std::mutex g_tune_mu;
 static std::map<TuneKey, std::array<int, kTunedClasses>> g_tune_cache;
 
+// The shape of an iteration: everything that fixes the arguments of its
+// launches (state parities, mode, union-kernel variant).
+struct GraphKey {
+    int cur, mbc_cur;
+    bool systolic, first_systolic, gather_all;
+    int variant;
+    bool operator==(const GraphKey& o) const {
+        return cur == o.cur && mbc_cur == o.mbc_cur && systolic == o.systolic &&
+               first_systolic == o.first_systolic && gather_all == o.gather_all && variant == o.variant;
+    }
+};
+
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+    uint64_t launches;  // kernels one launch of it runs
+};
+constexpr size_t kMaxGraphs = 32;
+
 struct hb_handle {
     // configuration
     int device = 0;
@@ -222,6 +241,16 @@ struct hb_handle {
     int grid_tile = 1, grid_heavy = 1, grid_mark = 1;
     int grid_tile_occ = 1;           // the window kernel's grid in its 4-blocks-per-SM variant
     Tuner tuner;
+    // iterations as CUDA graphs: captured on `cap`, launched on `stream`
+    bool use_graphs = true;
+    cudaStream_t cap = nullptr;
+    std::vector<GraphEntry> graphs;
+    std::vector<GraphKey> shapes_seen;
+    hbk::IterConsts* d_ic = nullptr;           // this iteration's constants (device)
+    hbk::IterConsts* h_ic = nullptr;           // ... staged in page-locked host memory
+    hbk::TilePartial* h_tot = nullptr;         // the iteration's totals (page-locked)
+    unsigned long long* h_inst_mod = nullptr;  // batches: per instance (page-locked)
+    double* h_inst_sum = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // reference state (IterationContext + HyperBall fields)
@@ -296,6 +325,11 @@ void release(hb_handle* h) {
     if (h->fork) cudaEventDestroy(h->fork);
     if (h->join) cudaEventDestroy(h->join);
     if (h->side) cudaStreamDestroy(h->side);
+    for (GraphEntry& g : h->graphs) cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
+    if (h->cap) cudaStreamDestroy(h->cap);
+    for (void* p : {(void*)h->h_ic, (void*)h->h_tot, (void*)h->h_inst_mod, (void*)h->h_inst_sum})
+        if (p) cudaFreeHost(p);
 }
 
 // Static work order of the union kernels (the graph does not change), and the
@@ -559,14 +593,11 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.sod = h->d_sod;
     a.harm = h->d_harm;
     a.ndisc = (int)h->d_disc.size();
-    for (int k = 0; k < a.ndisc; k++) {
-        a.disc[k] = h->d_disc[k];
-        a.disc_factor[k] = h->disc_fn[k](h->iteration + 1, h->disc_ctx[k]);
-    }
+    for (int k = 0; k < a.ndisc; k++) a.disc[k] = h->d_disc[k];
+    a.ic = h->d_ic;
     a.systolic = h->systolic ? 1 : 0;
     a.quirk = h->quirk ? 1 : 0;
     a.any31 = h->any31 ? 1 : 0;
-    a.iter = (uint32_t)h->iteration;
     a.n = h->n;
     a.alpha_m_m = h->alpha_m_m;
     a.a_scaled = h->alpha_m_m * 2147483648.0;  // exact: power-of-two scaling
@@ -576,8 +607,6 @@ hbk::UnionArgs union_args(hb_handle* h) {
         std::memcpy(&bits, &small, sizeof bits);
         a.small_bits = bits;
     }
-    a.d1 = (double)(h->iteration + 1);
-    a.rd1 = 1.0 / a.d1;
     a.ln_table = h->d_lnt;
     a.tiles = h->d_tiles;
     a.n_tiles = (uint32_t)h->n_tiles;
@@ -712,24 +741,23 @@ int do_init(hb_handle* h) {
     return HB_OK;
 }
 
-int do_iterate(hb_handle* h, hb_iter_stats* out) {
-    const uint64_t n = h->n, m = h->m;
-    const uint64_t prev_mod = h->modified_counters;
-    const bool prev_was_systolic = h->systolic;
-    // HB:795-810
-    h->systolic = h->has_transpose && h->iteration > 0 && prev_mod < n / 4;
-    double current_nf = h->systolic ? h->last : 0.0;
-    h->local = h->pre_local;
-    h->pre_local = h->systolic && m > 0 && prev_mod < (n * n) / (m * 10);
-
+// Every asynchronous operation of one iteration, in order, on stream s (the
+// heavy-node kernel on h->side, forked from s and joined back). `external`:
+// the timing events are recorded as graph nodes (stream capture). The host
+// reads the totals from h->h_tot (and, for batches, h->h_inst_*) once s is
+// synchronised; the per-iteration constants come from h->h_ic.
+int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaStream_t s,
+                      bool external) {
+    const uint64_t n = h->n;
     const uint64_t words = (n + 31) / 32;
-    const uint64_t launches0 = hbk::launch_count();
-    cudaStream_t s = h->stream;
-    HB_CUDA(h, cudaEventRecord(h->ev[0], s));
+    auto rec = [&](cudaEvent_t e) {
+        return external ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+    };
+    HB_CUDA(h, rec(h->ev[0]));
     HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mod_cur ^ 1], 0, words * 4, s));
     if (h->systolic) {
         HB_CUDA(h, cudaMemsetAsync(h->d_bits[h->mbc_cur ^ 1], 0, words * 4, s));
-        if (!prev_was_systolic) {
+        if (first_systolic) {
             // The reference scans every node in the first systolic iteration
             // (HB:853-857); scanning the predecessors of the nodes modified in
             // the previous iteration gives the same counters.
@@ -741,20 +769,9 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     HB_CUDA(h, cudaMemsetAsync(h->d_partials, 0, h->n_partials * sizeof(hbk::TilePartial), s));
     HB_CUDA(h, cudaMemsetAsync(h->d_nf_items, 0, (h->n_chunks + h->n_heavy) * sizeof(double), s));
     HB_CUDA(h, cudaMemsetAsync(h->d_cursor, 0, sizeof(unsigned long long), s));
-    hbk::UnionArgs a = union_args(h);
-    // nearly every counter changed in the previous iteration: merge all
-    // successors without waiting for their modified bits
-    a.gather_all = !h->systolic && prev_mod >= n - n / 8;
-    // the union-kernel variant (identical results; see Tuner)
-    const uint64_t merged = a.gather_all ? m - h->self_loops : h->pending_visited;
-    const int cls = h->systolic ? -1 : a.gather_all ? 0 : 1;
-    const bool sample = h->iteration > 0 && m >= kTuneMinArcs && 2 * merged >= m;
-    const int variant = choose_variant(h, cls, sample);
-    a.pf = kVariants[variant].pf;
-    a.pd = kVariants[variant].pd;
-    a.occ = kVariants[variant].occ;
+    HB_CUDA(h, cudaMemcpyAsync(h->d_ic, h->h_ic, sizeof(hbk::IterConsts), cudaMemcpyHostToDevice, s));
     if (h->systolic && h->n_tiles) {
-        // the chunks of the windows holding a node to check or to copy
+        // the light and medium nodes to check or to copy
         HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_medium_bits, h->d_light_bits, n,
                                             h->d_word_cnt, h->d_word_off, h->d_list_scratch,
                                             h->list_scratch_len, h->d_light_list,
@@ -763,7 +780,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         a.medium_list = h->d_medium_list;
         a.list_counts = h->d_word_off + words;
     }
-    HB_CUDA(h, cudaEventRecord(h->ev[1], s));
+    HB_CUDA(h, rec(h->ev[1]));
     if (h->n_heavy) {
         // The heavy nodes (one CTA each) start first on the side stream; the
         // window kernel's blocks take the SMs as they free up, so the long
@@ -780,7 +797,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     if (h->n_tiles)
         HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, a.occ ? h->grid_tile_occ : h->grid_tile, s));
     if (h->n_heavy) HB_CUDA(h, cudaStreamWaitEvent(s, h->join, 0));
-    HB_CUDA(h, cudaEventRecord(h->ev[2], s));
+    HB_CUDA(h, rec(h->ev[2]));
     if (h->systolic)
         HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
                                             h->d_bits[h->mbc_cur ^ 1], n, h->grid_mark, s));
@@ -791,17 +808,112 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     if (n_inst) {
         HB_LAUNCH(h, hbk::launch_inst_stats(h->d_bits[h->mod_cur ^ 1], h->d_est, h->d_inst_start,
                                             (uint32_t)n_inst, h->d_inst_mod, h->d_inst_nf, s));
-        h->inst_mod.resize(n_inst);
-        h->inst_sum.resize(n_inst);
-        HB_CUDA(h, cudaMemcpyAsync(h->inst_mod.data(), h->d_inst_mod, n_inst * 8, cudaMemcpyDeviceToHost, s));
-        HB_CUDA(h, cudaMemcpyAsync(h->inst_sum.data(), h->d_inst_nf, n_inst * 8, cudaMemcpyDeviceToHost, s));
+        HB_CUDA(h, cudaMemcpyAsync(h->h_inst_mod, h->d_inst_mod, n_inst * 8, cudaMemcpyDeviceToHost, s));
+        HB_CUDA(h, cudaMemcpyAsync(h->h_inst_sum, h->d_inst_nf, n_inst * 8, cudaMemcpyDeviceToHost, s));
     }
-    hbk::TilePartial tot{};
-    HB_CUDA(h, cudaMemcpyAsync(&tot, h->d_partials, sizeof(tot), cudaMemcpyDeviceToHost, s));
-    HB_CUDA(h, cudaEventRecord(h->ev[3], s));
+    HB_CUDA(h, cudaMemcpyAsync(h->h_tot, h->d_partials, sizeof(hbk::TilePartial), cudaMemcpyDeviceToHost, s));
+    HB_CUDA(h, rec(h->ev[3]));
+    return HB_OK;
+}
+
+// The executable graph of an iteration of this shape, captured the second time
+// the shape comes up (a shape seen once is launched directly: a run whose
+// shapes never repeat pays no capture), or null. Kernel arguments are fixed
+// by the shape: the state parities, the mode, the union-kernel variant; the
+// values that change every iteration reach the kernels through h->d_ic.
+cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::UnionArgs& a,
+                                bool first_systolic, int* err) {
+    *err = HB_OK;
+    if (!h->use_graphs) return nullptr;
+    for (const GraphEntry& g : h->graphs)
+        if (g.key == key) {
+            hbk::count_launches((int64_t)g.launches);
+            return g.exec;
+        }
+    if (h->graphs.size() >= kMaxGraphs) return nullptr;
+    auto seen = std::find(h->shapes_seen.begin(), h->shapes_seen.end(), key);
+    if (seen == h->shapes_seen.end()) {
+        h->shapes_seen.push_back(key);
+        return nullptr;
+    }
+    const uint64_t c0 = hbk::launch_count();
+    cudaError_t e = cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        *err = cuda_err(h, e, "cudaStreamBeginCapture");
+        return nullptr;
+    }
+    const int r = enqueue_iteration(h, a, first_systolic, h->cap, true);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(h->cap, &graph);
+    const uint64_t launches = hbk::launch_count() - c0;
+    hbk::count_launches(-(int64_t)launches);  // captured, not launched
+    if (r != HB_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        *err = r != HB_OK ? r : cuda_err(h, e, "cudaStreamEndCapture");
+        return nullptr;
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        *err = cuda_err(h, e, "cudaGraphInstantiate");
+        return nullptr;
+    }
+    h->graphs.push_back(GraphEntry{key, exec, launches});
+    hbk::count_launches((int64_t)launches);
+    return exec;
+}
+
+int do_iterate(hb_handle* h, hb_iter_stats* out) {
+    const uint64_t n = h->n, m = h->m;
+    const uint64_t prev_mod = h->modified_counters;
+    const bool prev_was_systolic = h->systolic;
+    // HB:795-810
+    h->systolic = h->has_transpose && h->iteration > 0 && prev_mod < n / 4;
+    double current_nf = h->systolic ? h->last : 0.0;
+    h->local = h->pre_local;
+    h->pre_local = h->systolic && m > 0 && prev_mod < (n * n) / (m * 10);
+
+    const uint64_t launches0 = hbk::launch_count();
+    cudaStream_t s = h->stream;
+    hbk::UnionArgs a = union_args(h);
+    // nearly every counter changed in the previous iteration: merge all
+    // successors without waiting for their modified bits
+    a.gather_all = !h->systolic && prev_mod >= n - n / 8;
+    // the union-kernel variant (identical results; see Tuner)
+    const uint64_t merged = a.gather_all ? m - h->self_loops : h->pending_visited;
+    const int cls = h->systolic ? -1 : a.gather_all ? 0 : 1;
+    const bool sample = h->iteration > 0 && m >= kTuneMinArcs && 2 * merged >= m;
+    const int variant = choose_variant(h, cls, sample);
+    a.pf = kVariants[variant].pf;
+    a.pd = kVariants[variant].pd;
+    a.occ = kVariants[variant].occ;
+    // the values that change from one iteration to the next
+    h->h_ic->d1 = (double)(h->iteration + 1);
+    h->h_ic->rd1 = 1.0 / h->h_ic->d1;
+    for (size_t k = 0; k < h->d_disc.size(); k++)
+        h->h_ic->disc_factor[k] = h->disc_fn[k](h->iteration + 1, h->disc_ctx[k]);
+    const bool first_systolic = h->systolic && !prev_was_systolic;
+    const GraphKey key{h->cur, h->mbc_cur, h->systolic, first_systolic, (bool)a.gather_all, variant};
+    int gerr = HB_OK;
+    cudaGraphExec_t exec = iteration_graph(h, key, a, first_systolic, &gerr);
+    if (gerr != HB_OK) return gerr;
+    if (exec) {
+        HB_CUDA(h, cudaGraphLaunch(exec, s));
+    } else {
+        int r = enqueue_iteration(h, a, first_systolic, s, false);
+        if (r != HB_OK) return r;
+    }
     HB_CUDA(h, cudaStreamSynchronize(s));
+    const hbk::TilePartial tot = *h->h_tot;
     if (tot.timeouts)
         return set_err(h, HB_ERR_TIMEOUT, "a TMA gather did not complete within its bounded wait");
+    const size_t n_inst = h->inst_start.empty() ? 0 : h->inst_start.size() - 1;
+    if (n_inst) {
+        h->inst_mod.assign(h->h_inst_mod, h->h_inst_mod + n_inst);
+        h->inst_sum.assign(h->h_inst_sum, h->h_inst_sum + n_inst);
+    }
     struct {
         unsigned long long st[4];
         double nf;
@@ -852,6 +964,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     st.iteration_ms = ms_all;
     st.scanned_arcs = host.st[3];
     st.union_variant = h->tuner.last;
+    st.from_graph = exec != nullptr;
     record_variant(h, ms_union, host.st[3] + merged);
     st.kernel_launches = hbk::launch_count() - launches0;
     h->stats.push_back(st);
@@ -1425,10 +1538,24 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         }
     if ((r = cuda_err(hp, cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming), "cudaEventCreate")) ||
         (r = cuda_err(hp, cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming), "cudaEventCreate")) ||
-        (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking), "cudaStreamCreate"))) {
+        (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking), "cudaStreamCreate")) ||
+        (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "cudaStreamCreate")) ||
+        (r = cuda_err(hp, cudaMallocHost((void**)&h->h_ic, sizeof(hbk::IterConsts)), "cudaMallocHost")) ||
+        (r = cuda_err(hp, cudaMallocHost((void**)&h->h_tot, sizeof(hbk::TilePartial)), "cudaMallocHost"))) {
         release(hp);
         return r;
     }
+    std::memset(h->h_ic, 0, sizeof(hbk::IterConsts));
+    std::memset(h->h_tot, 0, sizeof(hbk::TilePartial));
+    if (!h->inst_start.empty()) {
+        const size_t ni = h->inst_start.size() - 1;
+        if ((r = cuda_err(hp, cudaMallocHost((void**)&h->h_inst_mod, std::max<size_t>(ni, 1) * 8), "cudaMallocHost")) ||
+            (r = cuda_err(hp, cudaMallocHost((void**)&h->h_inst_sum, std::max<size_t>(ni, 1) * 8), "cudaMallocHost"))) {
+            release(hp);
+            return r;
+        }
+    }
+    h->use_graphs = !(o.flags & HB_NO_GRAPHS);
 
     auto fail = [&](int code) {
         g_global_err = hp->err;
@@ -1572,6 +1699,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     if ((r = dalloc(hp, &h->d_nf_items, h->n_chunks + h->n_heavy + 1))) return fail(r);
     if ((r = dalloc(hp, &h->d_nf_scratch, 256))) return fail(r);
     if ((r = dalloc(hp, &h->d_any31, 1))) return fail(r);
+    if ((r = dalloc(hp, &h->d_ic, 1))) return fail(r);
     if ((r = dalloc(hp, &h->d_cursor, 1))) return fail(r);
     if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     trace.mark("launch setup");

@@ -45,6 +45,14 @@ struct TilePartial {
     unsigned long long timeouts;  // bounded mbarrier waits that gave up (an error)
 };
 
+// The values of one iteration t that the kernels read from device memory, so
+// that the launches of an iteration (and a graph captured from them) do not
+// change from one iteration to the next.
+struct IterConsts {
+    double d1, rd1;                      // t + 1 and RN(1 / (t + 1))
+    double disc_factor[MAX_DISCOUNT];    // discount function k at distance t + 1
+};
+
 // Everything the union kernels read or write in one iteration.
 struct UnionArgs {
     CUtensorMap far_map;      // the current counters as rows of 2^log2m bytes (TMA gathers)
@@ -61,17 +69,15 @@ struct UnionArgs {
     double* sod;              // sum of distances or null
     double* harm;             // sum of inverse distances or null
     double* disc[MAX_DISCOUNT];
-    double disc_factor[MAX_DISCOUNT];
     int ndisc;
+    const IterConsts* ic;     // this iteration's d = t + 1, 1/d and discount factors (device)
     int systolic;             // 1: scan only must-be-checked nodes
     int quirk;                // Rust i32-shift count semantics
     int any31;                // some register may hold 31 (only then count looks for it)
-    uint32_t iter;            // 0-based iteration number
     uint64_t n;
     double alpha_m_m;
     double a_scaled;          // alpha_m_m * 2^31
     long long small_bits;     // bit pattern of 2.5 * m
-    double d1, rd1;           // iteration + 1 and RN(1 / (iteration + 1))
     const double* ln_table;   // m * ln(m / z), z = 0..m
     const uint32_t* list;     // heavy node list
     uint64_t list_len;
@@ -207,7 +213,9 @@ int launch_validate(const uint64_t* off, const uint32_t* succ, uint64_t n, uint6
                     void* stream);
 
 int num_sms(int device);
-// kernels launched so far by the calling host thread
+// kernels launched so far by the calling host thread (a graph launch adds the
+// kernels it runs)
 uint64_t launch_count();
+void count_launches(int64_t delta);
 
 }  // namespace hbk

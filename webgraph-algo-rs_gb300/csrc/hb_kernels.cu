@@ -41,6 +41,7 @@ namespace hbk {
 // kernels launched by this host thread (diagnostics: launches per iteration)
 static thread_local uint64_t t_launches = 0;
 uint64_t launch_count() { return t_launches; }
+void count_launches(int64_t delta) { t_launches += (uint64_t)delta; }
 
 // ---------------------------------------------------------------------------
 // block-level publish of per-thread statistics into one partial slot
@@ -162,10 +163,11 @@ __device__ __forceinline__ void finish_node(const UnionArgs& a, uint32_t v, int 
             // delta > 0.0 as an integer test: positive, not NaN
             const long long db = __double_as_longlong(delta);
             if (db > 0 && db <= 0x7ff0000000000000ll) {
-                if (a.sod) a.sod[v] = __dadd_rn(ns.sod, __dmul_rn(delta, a.d1));
-                if (a.harm) a.harm[v] = __dadd_rn(ns.harm, div_by_small_int(delta, a.d1, a.rd1));
+                const double d1 = __ldg(&a.ic->d1);
+                if (a.sod) a.sod[v] = __dadd_rn(ns.sod, __dmul_rn(delta, d1));
+                if (a.harm) a.harm[v] = __dadd_rn(ns.harm, div_by_small_int(delta, d1, __ldg(&a.ic->rd1)));
                 for (int k = 0; k < a.ndisc; k++)
-                    a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, a.disc_factor[k]));
+                    a.disc[k][v] = __dadd_rn(a.disc[k][v], __dmul_rn(delta, __ldg(&a.ic->disc_factor[k])));
             }
             vis += ns.indeg;
         }

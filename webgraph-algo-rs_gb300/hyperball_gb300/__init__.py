@@ -49,6 +49,7 @@ HB_SUM_OF_INVERSE_DISTANCES = 1 << 1
 HB_TRANSPOSE_ON_DEVICE = 1 << 2
 HB_NO_I32_SHIFT_QUIRK = 1 << 3
 HB_TMA_GATHER = 1 << 4
+HB_NO_GRAPHS = 1 << 5
 
 HB_CURRENT_STATE = 0
 HB_NEXT_STATE = 1
@@ -163,10 +164,12 @@ class IterStats(ctypes.Structure):
         ("iteration_ms", ctypes.c_double),
         ("scanned_arcs", ctypes.c_uint64),
         ("kernel_launches", ctypes.c_uint64),
+        ("from_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
 DISCOUNT_FN = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p)
@@ -491,6 +494,7 @@ class HyperBallBuilder:
         self._tma = False
         self._far_rows = None
         self._variant = None
+        self._graphs = True
 
     @staticmethod
     def new(graph, logic):
@@ -579,6 +583,12 @@ class HyperBallBuilder:
         self._far_rows = far_rows
         return self
 
+    def cuda_graphs(self, flag=True):
+        """Replay repeated iteration shapes as CUDA graphs (the default) or
+        launch every iteration directly; the results are the same."""
+        self._graphs = bool(flag)
+        return self
+
     def union_variant(self, index):
         """A fixed variant of the union kernels (0 .. union_variant_count() - 1)
         instead of the autotuner's choice (None); every variant gives the same
@@ -613,6 +623,8 @@ class HyperBall:
             flags |= HB_NO_I32_SHIFT_QUIRK
         if b._tma:
             flags |= HB_TMA_GATHER
+        if not b._graphs:
+            flags |= HB_NO_GRAPHS
         if b._far_rows is not None:
             o.far_rows = int(b._far_rows)
         o.flags = flags
