@@ -361,6 +361,8 @@ def run_gb300(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
+    variants = h.union_variants_chosen()
+    replayed = sum(s["from_graph"] for s in st)
     barrier()
     clk = clocks.stop()
     launches = h.kernel_launches() - launches0
@@ -449,7 +451,9 @@ def run_gb300(args):
             "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": dict(workload(args), arcs=m, iterations=len(ref_stats),
-                           parallelism=f"replicas x{world}"),
+                           parallelism=f"replicas x{world}",
+                           union_variants=variants,
+                           graph_replayed_iterations=f"{replayed} of {len(st)}"),
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
             "clocks": clk, "gpu_launches": launches,
         }

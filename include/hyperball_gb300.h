@@ -47,7 +47,7 @@ extern "C" {
 #define HB_TRANSPOSE_ON_DEVICE (1u << 2)      /* build the transpose on the GPU (enables systolic iterations) */
 #define HB_NO_I32_SHIFT_QUIRK (1u << 3)       /* count() with +2^-31 for register value 31 instead of Rust's i32 wrap (HLL:178) */
 #define HB_TMA_GATHER (1u << 4)               /* far successors by TMA gathers instead of plain loads (tuning; same results) */
-#define HB_NO_GRAPHS (1u << 5)                /* launch every iteration directly instead of replaying CUDA graphs of repeated iteration shapes (same results) */
+#define HB_NO_GRAPHS (1u << 5)                /* launch every iteration directly instead of replaying CUDA graphs of the iteration shapes an earlier run of the handle showed (same results) */
 
 /* "choose automatically" value of the tuning fields of hb_options */
 #define HB_AUTO 0xffffffffu
@@ -192,8 +192,9 @@ int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes);
  * they give bit-identical results. With union_variant = HB_AUTO the library
  * times them on the handle's own standard iterations (one iteration each,
  * per kind of iteration: merging every successor or only modified ones) and
- * keeps the fastest; the choice is remembered for later handles of a graph
- * with the same nodes, arcs and log2m in the process. No reference
+ * keeps the fastest if it beats the first variant by 3%; systolic iterations
+ * run the first variant. The choice is remembered for later handles of a
+ * graph with the same nodes, arcs and log2m in the process. No reference
  * counterpart: the reference has one code path (HB:960-1152). */
 int hb_union_variant_count(void);
 /* The variant chosen for each kind of iteration (0: standard iterations

@@ -30,7 +30,7 @@ def assert_close(a, b, rtol, what):
 
 def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True, harm=True,
              transpose_on_device=False, buckets=None, max_iters=10_000, check_next=True,
-             discounts=(), tma=False, far_rows=None, variant=None, graphs=True):
+             discounts=(), tma=False, far_rows=None, variant=None, graphs=True, warm_runs=0):
     """Runs GPU and oracle side by side; returns (gpu, oracle, stats list)."""
     hasher = hb.JenkinsHasher(seed) if hash_kind == 1 else hb.DefaultHasher()
     logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(log2m).build_hasher(hasher).build()
@@ -53,6 +53,8 @@ def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True
         g.offsets, g.successors, log2m, hash_kind=hash_kind, seed=seed,
         t_offsets=t.offsets if has_t else None, t_successors=t.successors if has_t else None,
         sod=sod, harm=harm, threads=1, discounts=discounts)
+    for _ in range(warm_runs):
+        gpu.run_until_done()  # the shapes of a finished run are replayed as CUDA graphs
     gpu.init()
     orc.init()
     np.testing.assert_array_equal(gpu.registers(0), orc.registers(0), "init current state")

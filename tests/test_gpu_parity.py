@@ -98,16 +98,17 @@ def test_autotuner_identical_results(hb):
 
 @pytest.mark.parametrize("graphs", [False, True])
 def test_cuda_graph_iterations(hb, oracle, graphs):
-    """Iterations replayed from captured CUDA graphs (standard, first systolic
-    and systolic shapes; discount factors and 1/d from device memory) match
-    the oracle exactly as directly launched ones do."""
+    """After a first run, the iterations of the next run are replayed from
+    captured CUDA graphs (standard, first systolic and systolic shapes;
+    discount factors and 1/d from device memory) and match the oracle exactly
+    as directly launched ones do."""
     g = hb.Graph.weblike(30_000, cap=2000, window=256, seed=4)
     gpu, orc, stats = lockstep(hb, oracle, g, 6, transpose_on_device=True, graphs=graphs,
-                               discounts=(lambda d: 1.0 / d, lambda d: 0.5 ** d))
+                               discounts=(lambda d: 1.0 / d, lambda d: 0.5 ** d), warm_runs=1)
     replays = [sg["from_graph"] for sg, _ in stats]
     if graphs:
-        assert any(replays), replays
-        assert any(sg["systolic"] and sg["from_graph"] for sg, _ in stats)
+        assert all(replays), replays
+        assert any(sg["systolic"] for sg, _ in stats)
         assert all(sg["kernel_launches"] > 0 for sg, _ in stats)
     else:
         assert not any(replays)

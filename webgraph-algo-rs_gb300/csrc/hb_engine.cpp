@@ -109,9 +109,10 @@ struct hb_graph {
 // one iteration that scans at least an eighth of the arcs and merges at least
 // half of what it scans, as union time per scanned-plus-merged arc; the
 // fastest is kept for the rest of the handle's life and remembered for later
-// handles of a graph with the same shape. Systolic iterations vary too much
-// from one to the next to be compared; they take the choice of the filtered
-// standard iterations (or of the others, or the first variant).
+// handles of a graph with the same shape. A variant other than the first
+// must be at least 3% faster to be kept (one sample each). Systolic
+// iterations vary too much from one to the next to be compared, and
+// prefetching measured slower there: they run the first variant.
 // ---------------------------------------------------------------------------
 struct UnionVariant {
     uint32_t pf, pd, occ;
@@ -120,6 +121,7 @@ constexpr UnionVariant kVariants[] = {{0, 0, 0}, {2, 2, 0}, {0, 0, 1}, {2, 2, 1}
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 constexpr int kTunedClasses = 2;  // gather-all standard, filtered standard
 constexpr uint64_t kTuneMinArcs = 1ull << 22;  // smaller graphs keep the first variant
+constexpr double kTuneMargin = 0.97;
 
 struct Tuner {
     int fixed = -1;                            // a variant forced by the options
@@ -245,7 +247,8 @@ struct hb_handle {
     bool use_graphs = true;
     cudaStream_t cap = nullptr;
     std::vector<GraphEntry> graphs;
-    std::vector<GraphKey> shapes_seen;
+    std::vector<GraphKey> shapes_run;   // iteration shapes of the current run
+    std::vector<GraphKey> shapes_seen;  // ... of the earlier runs of this handle
     hbk::IterConsts* d_ic = nullptr;           // this iteration's constants (device)
     hbk::IterConsts* h_ic = nullptr;           // ... staged in page-locked host memory
     hbk::TilePartial* h_tot = nullptr;         // the iteration's totals (page-locked)
@@ -647,7 +650,7 @@ int choose_variant(hb_handle* h, int cls, bool sample) {
     Tuner& t = h->tuner;
     t.last_class = -1;
     if (t.fixed >= 0) return t.last = t.fixed;
-    if (cls < 0) return t.last = t.chosen[1] >= 0 ? t.chosen[1] : t.chosen[0] >= 0 ? t.chosen[0] : 0;
+    if (cls < 0) return t.last = 0;
     if (t.chosen[cls] >= 0) return t.last = t.chosen[cls];
     if (sample)
         for (int v = 0; v < kNumVariants; v++)
@@ -671,6 +674,8 @@ void record_variant(hb_handle* h, double union_ms, uint64_t arcs) {
         if (!t.timed[cls][v]) return;
         if (t.best[cls][v] < t.best[cls][best]) best = v;
     }
+    // one sample each: another variant must beat the first by a clear margin
+    if (t.best[cls][best] > kTuneMargin * t.best[cls][0]) best = 0;
     t.chosen[cls] = best;
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto& e = g_tune_cache.try_emplace(TuneKey{h->device, h->log2m, h->n, h->m},
@@ -737,6 +742,11 @@ int do_init(hb_handle* h) {
         // run() caps the iterations at the number of nodes (HB:541)
         h->inst_done[i] = ni_nodes == 0;
     }
+    // a new run: the shapes of the last one may now be captured
+    for (const GraphKey& k : h->shapes_run)
+        if (std::find(h->shapes_seen.begin(), h->shapes_seen.end(), k) == h->shapes_seen.end())
+            h->shapes_seen.push_back(k);
+    h->shapes_run.clear();
     h->initialised = true;
     return HB_OK;
 }
@@ -816,11 +826,12 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
     return HB_OK;
 }
 
-// The executable graph of an iteration of this shape, captured the second time
-// the shape comes up (a shape seen once is launched directly: a run whose
-// shapes never repeat pays no capture), or null. Kernel arguments are fixed
-// by the shape: the state parities, the mode, the union-kernel variant; the
-// values that change every iteration reach the kernels through h->d_ic.
+// The executable graph of an iteration of this shape, or null. A shape is
+// captured once an earlier run of the handle has shown it (the first run of a
+// handle launches directly, so a handle that runs once pays no capture); the
+// later runs replay it. Kernel arguments are fixed by the shape: the state
+// parities, the mode, the union-kernel variant; the values that change every
+// iteration reach the kernels through h->d_ic.
 cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::UnionArgs& a,
                                 bool first_systolic, int* err) {
     *err = HB_OK;
@@ -831,9 +842,9 @@ cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::Un
             return g.exec;
         }
     if (h->graphs.size() >= kMaxGraphs) return nullptr;
-    auto seen = std::find(h->shapes_seen.begin(), h->shapes_seen.end(), key);
-    if (seen == h->shapes_seen.end()) {
-        h->shapes_seen.push_back(key);
+    if (std::find(h->shapes_seen.begin(), h->shapes_seen.end(), key) == h->shapes_seen.end()) {
+        if (std::find(h->shapes_run.begin(), h->shapes_run.end(), key) == h->shapes_run.end())
+            h->shapes_run.push_back(key);
         return nullptr;
     }
     const uint64_t c0 = hbk::launch_count();
@@ -1886,7 +1897,7 @@ int hb_union_variant_chosen(const hb_handle* h, int32_t chosen[3]) {
     if (!h || !chosen) return set_err(const_cast<hb_handle*>(h), HB_ERR_INVALID, "null argument");
     const Tuner& t = h->tuner;
     for (int c = 0; c < kTunedClasses; c++) chosen[c] = t.fixed >= 0 ? t.fixed : t.chosen[c];
-    chosen[2] = t.fixed >= 0 ? t.fixed : t.chosen[1] >= 0 ? t.chosen[1] : t.chosen[0] >= 0 ? t.chosen[0] : 0;
+    chosen[2] = t.fixed >= 0 ? t.fixed : 0;
     return HB_OK;
 }
 

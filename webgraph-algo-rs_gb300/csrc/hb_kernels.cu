@@ -315,21 +315,32 @@ __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, i
         if (e0 >= e1) return;
         const uint32_t* sp = a.succ + e0;
         const uint32_t cnt = (uint32_t)((e1 - e0 + stride - 1) / stride);
-        const uint32_t pd = a.pf ? a.pd : 0u;
-        for (uint32_t k = 1; k <= pd && k < cnt; k++)
-            prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)k * stride), c, a.pf);
         uint32_t s = __ldg(sp);
         bool have = wanted(s);
         uint32_t y[NW];
         if (have) load_chunk<LOG2M>(a.curr, s, c, y);
-        for (uint32_t i = 1; i < cnt; i++) {
-            const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
-            if (pd && i + pd < cnt)
-                prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)(i + pd) * stride), c, a.pf);
-            const bool nh = wanted(ns);
-            if (have) merge_chunk<REGS>(acc, y);
-            if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
-            have = nh;
+        if (a.pf) {
+            // the same with the counter `pd` arcs ahead requested early
+            const uint32_t pd = a.pd;
+            for (uint32_t k = 1; k <= pd && k < cnt; k++)
+                prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)k * stride), c, a.pf);
+            for (uint32_t i = 1; i < cnt; i++) {
+                const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
+                if (i + pd < cnt)
+                    prefetch_chunk<LOG2M>(a.curr, __ldg(sp + (uint64_t)(i + pd) * stride), c, a.pf);
+                const bool nh = wanted(ns);
+                if (have) merge_chunk<REGS>(acc, y);
+                if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
+                have = nh;
+            }
+        } else {
+            for (uint32_t i = 1; i < cnt; i++) {
+                const uint32_t ns = __ldg(sp + (uint64_t)i * stride);
+                const bool nh = wanted(ns);
+                if (have) merge_chunk<REGS>(acc, y);
+                if (nh) load_chunk<LOG2M>(a.curr, ns, c, y);
+                have = nh;
+            }
         }
         if (have) merge_chunk<REGS>(acc, y);
     } else {
