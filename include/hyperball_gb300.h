@@ -85,8 +85,8 @@ typedef struct hb_options {
     const uint64_t* weights;  /* optional node weights, host array of num_nodes (HB:286-290); NULL = all 1 */
     uint64_t weight_seed;     /* seeds the values added for weights (the reference uses a non-reproducible RNG, HB:1167-1174) */
     void* stream;             /* cudaStream_t to launch on; NULL = legacy default stream */
-    uint32_t small_max_degree;  /* tuning: nodes up to this out-degree run one lane-group each; HB_AUTO = tuned default */
-    uint32_t medium_max_degree; /* tuning: nodes up to this out-degree run one warp each, above: one CTA; HB_AUTO = tuned default */
+    uint32_t small_max_degree;  /* tuning: nodes up to this out-degree run one lane-group each; HB_AUTO = 64 (see hb_tune_degree_buckets) */
+    uint32_t medium_max_degree; /* tuning: nodes up to this out-degree run one 8-lane team each, above: one CTA; HB_AUTO = 4096 */
     uint32_t union_variant;     /* tuning: HB_AUTO = the autotuner picks the union-kernel variant per graph
                                    (see hb_union_variant_count); else the index of a fixed variant.
                                    Every variant gives bit-identical results. */
@@ -148,6 +148,18 @@ int hb_run_until_stable(hb_handle* h, uint64_t upper_bound);
 
 /* HyperBall::run_until_done() (HB:614-621). */
 int hb_run_until_done(hb_handle* h);
+
+/* Autotuner of the degree buckets: which nodes run one lane group each
+ * (out-degree up to small_max), one 8-lane team each (up to medium_max) or one
+ * CTA each (above). Builds a handle per candidate pair (small_max in
+ * {16, 32, 64, 128, 256}, medium_max in {1024, 4096, 16384, 65536}) from `opts`, times
+ * the union kernels over `iterations` standard iterations (at least 2; the
+ * first is not counted) and returns the fastest pair and its union time.
+ * Pass the pair as hb_options.small_max_degree / medium_max_degree; every
+ * pair gives identical results. No reference counterpart: the reference
+ * splits work by arc granularity only (HB:280-283, HB:1012). */
+int hb_tune_degree_buckets(const hb_graph_view* graph, const hb_options* opts, uint32_t iterations,
+                           uint32_t* small_max, uint32_t* medium_max, double* union_ms);
 
 /* Step-wise driving, as the reference's in-crate test does with init() and
  * iterate() (HB:1155-1213, HB:775-949). `out` may be NULL. */

@@ -114,6 +114,30 @@ def test_cuda_graph_iterations(hb, oracle, graphs):
         assert not any(replays)
 
 
+def test_degree_bucket_tuner(hb):
+    """The bucket autotuner returns one of its candidate pairs, and a handle
+    built with it gives the same registers and sums as the default buckets."""
+    g = hb.Graph.weblike(1 << 16, cap=20_000, window=512, seed=3)
+    logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(6).build()
+    small, medium, ms = hb.tune_degree_buckets(g, logic, iterations=3)
+    assert small in (16, 32, 64, 128, 256) and medium in (1024, 4096, 16384, 65536) and ms > 0
+
+    def run(buckets):
+        b = hb.HyperBallBuilder.new(g, logic).transpose_on_device(True).sum_of_distances(True)
+        if buckets:
+            b = b.degree_buckets(*buckets)
+        h = b.build()
+        h.run_until_done()
+        out = (h.registers(0), h.sum_of_distances(), h.neighborhood_function())
+        h.close()
+        return out
+
+    tuned, default = run((small, medium)), run(None)
+    np.testing.assert_array_equal(tuned[0], default[0])
+    assert_close(tuned[1], default[1], 1e-12, "sum of distances")
+    assert_close(tuned[2], default[2], 1e-12, "neighbourhood function")
+
+
 def test_transpose_on_device(hb, oracle):
     g = hb.Graph.rmat(12, 8, seed=5)
     lockstep(hb, oracle, g, 6, transpose_on_device=True)

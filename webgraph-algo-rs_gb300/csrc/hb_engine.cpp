@@ -1575,7 +1575,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     };
     // Work partition and renumbering (host), then the CSR (and the transpose
     // when given) uploaded, validated and renumbered on the device.
-    h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 32;
+    h->small_max = o.small_max_degree != HB_AUTO ? o.small_max_degree : 64;
     h->medium_max = o.medium_max_degree != HB_AUTO ? o.medium_max_degree : 4096;
     if (h->medium_max < h->small_max) h->medium_max = h->small_max;
     const bool device_transpose = !transpose && (o.flags & HB_TRANSPOSE_ON_DEVICE);
@@ -1776,6 +1776,57 @@ int hb_run(hb_handle* h, uint64_t upper_bound, double threshold) {
 
 int hb_run_until_stable(hb_handle* h, uint64_t upper_bound) { return hb_run(h, upper_bound, NAN); }
 int hb_run_until_done(hb_handle* h) { return hb_run(h, UINT64_MAX, NAN); }
+
+int hb_tune_degree_buckets(const hb_graph_view* graph, const hb_options* opts, uint32_t iterations,
+                           uint32_t* small_max, uint32_t* medium_max, double* union_ms) {
+    if (!graph || !opts || !small_max || !medium_max)
+        return set_err(nullptr, HB_ERR_INVALID, "NULL argument");
+    if (opts->struct_size != sizeof(hb_options))
+        return set_err(nullptr, HB_ERR_INVALID, "hb_options.struct_size mismatch");
+    iterations = std::max<uint32_t>(iterations, 2);
+    // lane-group nodes up to 16..256 successors; warp teams up to 1024..65536
+    static const uint32_t kSmall[] = {16, 32, 64, 128, 256};
+    static const uint32_t kMedium[] = {1024, 4096, 16384, 65536};
+    double best = INFINITY;
+    uint32_t bs = 32, bm = 4096;
+    for (uint32_t sm : kSmall)
+        for (uint32_t mm : kMedium) {
+            hb_options o = *opts;
+            o.small_max_degree = sm;
+            o.medium_max_degree = mm;
+            // standard iterations only (they carry the union work), on one
+            // fixed kernel variant so that only the buckets differ
+            o.flags &= ~HB_TRANSPOSE_ON_DEVICE;
+            o.flags |= HB_NO_GRAPHS;
+            if (o.union_variant == HB_AUTO) o.union_variant = 0;
+            hb_handle* h = nullptr;
+            int r = hb_create(graph, nullptr, &o, &h);
+            if (r) return r;
+            r = hb_init(h);
+            double t = 0.0;
+            for (uint32_t i = 0; r == HB_OK && i < iterations; i++) {
+                hb_iter_stats st{};
+                r = hb_iterate(h, &st);
+                if (r == HB_OK && i > 0) t += st.union_ms;  // the first iteration warms up
+                if (r == HB_OK && st.modified_counters == 0) break;
+            }
+            if (r) {
+                g_global_err = h->err;
+                hb_destroy(h);
+                return r;
+            }
+            hb_destroy(h);
+            if (t < best) {
+                best = t;
+                bs = sm;
+                bm = mm;
+            }
+        }
+    *small_max = bs;
+    *medium_max = bm;
+    if (union_ms) *union_ms = best;
+    return HB_OK;
+}
 
 uint64_t hb_num_iterations(const hb_handle* h) { return h ? h->iteration : 0; }
 

@@ -203,6 +203,9 @@ EXPORTS = [
     ("hb_get_registers", ctypes.c_int, [_H, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]),
     ("hb_counter_layout", ctypes.c_int, [_H, _P(ctypes.c_uint64), _P(ctypes.c_int)]),
     ("hb_union_variant_count", ctypes.c_int, []),
+    ("hb_tune_degree_buckets", ctypes.c_int,
+     [ctypes.POINTER(GraphView), ctypes.POINTER(Options), ctypes.c_uint32, _P(ctypes.c_uint32),
+      _P(ctypes.c_uint32), _P(ctypes.c_double)]),
     ("hb_union_variant_chosen", ctypes.c_int, [_H, _P(ctypes.c_int32)]),
     ("hb_last_error", ctypes.c_char_p, [_H]),
     ("hb_global_last_error", ctypes.c_char_p, []),
@@ -260,6 +263,27 @@ EXPORTS = [
 ]
 
 _lib = None
+
+
+def tune_degree_buckets(graph, logic, iterations=3, device=0, stream=None):
+    """hb_tune_degree_buckets: the (small_max, medium_max) degree-bucket pair
+    whose union kernels ran the given standard iterations fastest on this
+    graph, and that time in ms. Pass the pair to
+    HyperBallBuilder.degree_buckets(); every pair gives identical results."""
+    lib = load_library()
+    o = Options()
+    lib.hb_options_default(ctypes.byref(o))
+    o.log2m = logic.log2m
+    o.hash_kind = logic.hasher.kind
+    o.hash_seed = logic.hasher.seed
+    o.num_elements = logic.num_elements
+    o.device = int(device)
+    o.stream = stream
+    gv = graph.view()
+    sm, mm, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+    _check(lib.hb_tune_degree_buckets(ctypes.byref(gv), ctypes.byref(o), int(iterations),
+                                      ctypes.byref(sm), ctypes.byref(mm), ctypes.byref(ms)))
+    return int(sm.value), int(mm.value), float(ms.value)
 
 
 def union_variant_count():
