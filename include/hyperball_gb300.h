@@ -152,7 +152,7 @@ int hb_run_until_done(hb_handle* h);
 /* Autotuner of the degree buckets: which nodes run one lane group each
  * (out-degree up to small_max), one 8-lane team each (up to medium_max) or one
  * CTA each (above). Builds a handle per candidate pair (small_max in
- * {16, 32, 64, 128, 256}, medium_max in {1024, 4096, 16384, 65536}) from `opts`, times
+ * {32, 64, 128, 256, 512, 1024}, medium_max in {4096, 16384, 65536}) from `opts`, times
  * the union kernels over `iterations` standard iterations (at least 2; the
  * first is not counted) and returns the fastest pair and its union time.
  * Pass the pair as hb_options.small_max_degree / medium_max_degree; every

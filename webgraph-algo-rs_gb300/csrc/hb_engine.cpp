@@ -1784,9 +1784,9 @@ int hb_tune_degree_buckets(const hb_graph_view* graph, const hb_options* opts, u
     if (opts->struct_size != sizeof(hb_options))
         return set_err(nullptr, HB_ERR_INVALID, "hb_options.struct_size mismatch");
     iterations = std::max<uint32_t>(iterations, 2);
-    // lane-group nodes up to 16..256 successors; warp teams up to 1024..65536
-    static const uint32_t kSmall[] = {16, 32, 64, 128, 256};
-    static const uint32_t kMedium[] = {1024, 4096, 16384, 65536};
+    // lane-group nodes up to 32..1024 successors; 8-lane teams up to 4096..65536
+    static const uint32_t kSmall[] = {32, 64, 128, 256, 512, 1024};
+    static const uint32_t kMedium[] = {4096, 16384, 65536};
     double best = INFINITY;
     uint32_t bs = 32, bm = 4096;
     for (uint32_t sm : kSmall)
