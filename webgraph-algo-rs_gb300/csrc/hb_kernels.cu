@@ -220,6 +220,12 @@ __device__ __forceinline__ double warp_sum_f64(double x) {
 // self-loops), which finish_node accumulates for the next iteration.
 // ---------------------------------------------------------------------------
 constexpr int WINDOW = 1024;
+// lanes of the team that runs one medium node: 8 arc lanes of G chunk lanes
+// (measured at 2^26 web-like: 4 arc lanes 8% slower, 16 the same)
+template <int LOG2M>
+__host__ __device__ constexpr int team_lanes() {
+    return 8 * Geo<LOG2M>::CHUNKS < 32 ? 8 * Geo<LOG2M>::CHUNKS : 32;
+}
 // counter loads in flight per lane: 64 bytes, within the register budget of
 // three 256-thread blocks per SM (measured: more resident warps beat deeper
 // per-lane pipelines)
@@ -677,7 +683,7 @@ template <int LOG2M, bool FAR, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
-    constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
+    constexpr int TB_MED = team_lanes<LOG2M>();
     const int lane = threadIdx.x & 31;
     // per warp: the mbarrier of its far-successor TMA copies
     FarState fs{0u};
@@ -1728,7 +1734,7 @@ int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs) {
 template <int L>
 static int chunk_nodes_impl(uint32_t* light, uint32_t* medium) {
     constexpr int G = Geo<L>::CHUNKS;
-    constexpr int TB_MED = 8 * G < 32 ? 8 * G : 32;
+    constexpr int TB_MED = team_lanes<L>();
     *light = 32 / G;
     *medium = 32 / TB_MED;
     return 0;
