@@ -277,6 +277,10 @@ int hb_batch_get_registers(const hb_batch* b, uint32_t graph, void* dst, size_t 
  * iteration, device time of the iterations (summed over groups). */
 int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_arcs,
                    uint64_t* register_updates, double* device_ms);
+/* Union iterations of the batch's groups that ran as replays of a captured
+ * CUDA graph, and all of them (a batch captures an iteration shape the second
+ * time it comes). No reference counterpart. */
+int hb_batch_graph_replays(const hb_batch* b, uint64_t* replayed, uint64_t* iterations);
 void hb_batch_destroy(hb_batch* b);
 
 /* ---- served jobs: continuous admission against a device-memory budget --------- */

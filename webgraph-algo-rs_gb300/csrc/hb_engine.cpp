@@ -245,6 +245,7 @@ struct hb_handle {
     Tuner tuner;
     // iterations as CUDA graphs: captured on `cap`, launched on `stream`
     bool use_graphs = true;
+    bool capture_in_run = false;        // batches: capture a shape the second time it comes
     cudaStream_t cap = nullptr;
     std::vector<GraphEntry> graphs;
     std::vector<GraphKey> shapes_run;   // iteration shapes of the current run
@@ -829,7 +830,8 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
 // The executable graph of an iteration of this shape, or null. A shape is
 // captured once an earlier run of the handle has shown it (the first run of a
 // handle launches directly, so a handle that runs once pays no capture); the
-// later runs replay it. Kernel arguments are fixed by the shape: the state
+// later runs replay it. A batch, which usually runs once, captures a shape the
+// second time it comes in the run (shapes alternate with the state parities). Kernel arguments are fixed by the shape: the state
 // parities, the mode, the union-kernel variant; the values that change every
 // iteration reach the kernels through h->d_ic.
 cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::UnionArgs& a,
@@ -843,9 +845,9 @@ cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::Un
         }
     if (h->graphs.size() >= kMaxGraphs) return nullptr;
     if (std::find(h->shapes_seen.begin(), h->shapes_seen.end(), key) == h->shapes_seen.end()) {
-        if (std::find(h->shapes_run.begin(), h->shapes_run.end(), key) == h->shapes_run.end())
-            h->shapes_run.push_back(key);
-        return nullptr;
+        const bool in_run = std::find(h->shapes_run.begin(), h->shapes_run.end(), key) != h->shapes_run.end();
+        if (!in_run) h->shapes_run.push_back(key);
+        if (!(in_run && h->capture_in_run)) return nullptr;
     }
     const uint64_t c0 = hbk::launch_count();
     cudaError_t e = cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal);
@@ -1313,6 +1315,19 @@ int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_ar
     return HB_OK;
 }
 
+int hb_batch_graph_replays(const hb_batch* b, uint64_t* replayed, uint64_t* iterations) {
+    if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
+    uint64_t r = 0, it = 0;
+    for (const auto& g : b->groups)
+        for (const auto& s : g.h->stats) {
+            r += s.from_graph ? 1 : 0;
+            it += 1;
+        }
+    if (replayed) *replayed = r;
+    if (iterations) *iterations = it;
+    return HB_OK;
+}
+
 // ---- device CSR utilities ----------------------------------------------------
 namespace {
 // Checks a device CSR before any kernel indexes with it: offsets[0] == 0,
@@ -1567,6 +1582,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         }
     }
     h->use_graphs = !(o.flags & HB_NO_GRAPHS);
+    h->capture_in_run = !h->inst_start.empty();
 
     auto fail = [&](int code) {
         g_global_err = hp->err;

@@ -237,6 +237,7 @@ EXPORTS = [
     ("hb_batch_get_registers", ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t]),
     ("hb_batch_stats", ctypes.c_int,
      [_H, _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_uint64), _P(ctypes.c_double)]),
+    ("hb_batch_graph_replays", ctypes.c_int, [_H, _P(ctypes.c_uint64), _P(ctypes.c_uint64)]),
     ("hb_batch_destroy", None, [_H]),
     ("hb_server_options_default", None, [_P(ServerOptions)]),
     ("hb_server_create", ctypes.c_int, [_P(ServerOptions), _P(_H)]),
@@ -877,8 +878,10 @@ class HyperBallBatch:
         it, vis, upd, ms = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
         _check(self._lib.hb_batch_stats(self._h, ctypes.byref(it), ctypes.byref(vis),
                                         ctypes.byref(upd), ctypes.byref(ms)))
+        rep, total = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self._lib.hb_batch_graph_replays(self._h, ctypes.byref(rep), ctypes.byref(total)))
         return {"iterations": it.value, "visited_arcs": vis.value, "register_updates": upd.value,
-                "device_ms": ms.value}
+                "device_ms": ms.value, "graph_replays": rep.value, "group_iterations": total.value}
 
 
 # ---------------------------------------------------------------------------
