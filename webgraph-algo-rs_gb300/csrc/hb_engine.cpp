@@ -93,6 +93,39 @@ cudaError_t pool_alloc(int device, void** p, size_t bytes, cudaStream_t s) {
     return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
+// Page-locked host blocks for the per-iteration totals and constants of a
+// handle. Freed blocks are kept for the next handle instead of going back
+// through cudaFreeHost, which may synchronise the device under the other
+// handles' work (the job server destroys handles while others run).
+std::mutex g_pinned_mu;
+std::multimap<size_t, void*> g_pinned_free;
+
+size_t pinned_class(size_t bytes) {
+    size_t c = 256;
+    while (c < bytes) c <<= 1;
+    return c;
+}
+
+cudaError_t pinned_alloc(void** p, size_t bytes) {
+    const size_t c = pinned_class(bytes);
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        auto it = g_pinned_free.find(c);
+        if (it != g_pinned_free.end()) {
+            *p = it->second;
+            g_pinned_free.erase(it);
+            return cudaSuccess;
+        }
+    }
+    return cudaMallocHost(p, c);
+}
+
+void pinned_free(void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned_free.emplace(pinned_class(bytes), p);
+}
+
 }  // namespace
 
 struct hb_graph {
@@ -332,8 +365,15 @@ void release(hb_handle* h) {
     for (GraphEntry& g : h->graphs) cudaGraphExecDestroy(g.exec);
     h->graphs.clear();
     if (h->cap) cudaStreamDestroy(h->cap);
-    for (void* p : {(void*)h->h_ic, (void*)h->h_tot, (void*)h->h_inst_mod, (void*)h->h_inst_sum})
-        if (p) cudaFreeHost(p);
+    const size_t ni = h->inst_start.empty() ? 1 : std::max<size_t>(h->inst_start.size() - 1, 1);
+    pinned_free(h->h_ic, sizeof(hbk::IterConsts));
+    pinned_free(h->h_tot, sizeof(hbk::TilePartial));
+    pinned_free(h->h_inst_mod, ni * 8);
+    pinned_free(h->h_inst_sum, ni * 8);
+    h->h_ic = nullptr;
+    h->h_tot = nullptr;
+    h->h_inst_mod = nullptr;
+    h->h_inst_sum = nullptr;
 }
 
 // Static work order of the union kernels (the graph does not change), and the
@@ -1566,8 +1606,8 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         (r = cuda_err(hp, cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming), "cudaEventCreate")) ||
         (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking), "cudaStreamCreate")) ||
         (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "cudaStreamCreate")) ||
-        (r = cuda_err(hp, cudaMallocHost((void**)&h->h_ic, sizeof(hbk::IterConsts)), "cudaMallocHost")) ||
-        (r = cuda_err(hp, cudaMallocHost((void**)&h->h_tot, sizeof(hbk::TilePartial)), "cudaMallocHost"))) {
+        (r = cuda_err(hp, pinned_alloc((void**)&h->h_ic, sizeof(hbk::IterConsts)), "cudaMallocHost")) ||
+        (r = cuda_err(hp, pinned_alloc((void**)&h->h_tot, sizeof(hbk::TilePartial)), "cudaMallocHost"))) {
         release(hp);
         return r;
     }
@@ -1575,8 +1615,8 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     std::memset(h->h_tot, 0, sizeof(hbk::TilePartial));
     if (!h->inst_start.empty()) {
         const size_t ni = h->inst_start.size() - 1;
-        if ((r = cuda_err(hp, cudaMallocHost((void**)&h->h_inst_mod, std::max<size_t>(ni, 1) * 8), "cudaMallocHost")) ||
-            (r = cuda_err(hp, cudaMallocHost((void**)&h->h_inst_sum, std::max<size_t>(ni, 1) * 8), "cudaMallocHost"))) {
+        if ((r = cuda_err(hp, pinned_alloc((void**)&h->h_inst_mod, std::max<size_t>(ni, 1) * 8), "cudaMallocHost")) ||
+            (r = cuda_err(hp, pinned_alloc((void**)&h->h_inst_sum, std::max<size_t>(ni, 1) * 8), "cudaMallocHost"))) {
             release(hp);
             return r;
         }
