@@ -326,6 +326,11 @@ int hb_server_create(const hb_server_options* opts, hb_server** out);
  * when the job alone exceeds the budget. */
 int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options* opts,
                      uint64_t* job);
+/* The same without the copy: the graph's arrays must stay valid and unchanged
+ * until hb_server_wait has returned for the job. Submitting then costs no
+ * host time, so a stream of large jobs arrives on schedule. */
+int hb_server_submit_borrowed(hb_server* s, const hb_graph_view* graph, const hb_options* opts,
+                              uint64_t* job);
 /* Waits until the job finished (timeout_s < 0: no limit); HB_ERR_TIMEOUT when
  * the limit passed first, the job's own status when it failed. */
 int hb_server_wait(hb_server* s, uint64_t job, double timeout_s);

@@ -34,11 +34,12 @@ def _alone(g, log2m):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("max_active", [1, 3, 16])
-def test_served_jobs_equal_jobs_alone(max_active):
+@pytest.mark.parametrize("max_active,borrow", [(1, False), (3, False), (16, False), (16, True)])
+def test_served_jobs_equal_jobs_alone(max_active, borrow):
     jobs = _jobs()
     s = hb.HyperBallServer(max_active=max_active, keep_registers=True)
-    ids = [s.submit(g, l2m, sum_of_distances=True, sum_of_inverse_distances=True) for g, l2m in jobs]
+    ids = [s.submit(g, l2m, sum_of_distances=True, sum_of_inverse_distances=True, borrow=borrow)
+           for g, l2m in jobs]
     for j in ids:
         s.wait(j, timeout=600)
     for j, (g, l2m) in zip(ids, jobs):

@@ -33,7 +33,9 @@ using Clock = std::chrono::steady_clock;
 
 struct Job {
     uint64_t id = 0;
-    Csr graph;
+    Csr graph;                // the copied graph (hb_server_submit)
+    hb_graph_view borrowed{}; // the caller's graph (hb_server_submit_borrowed), else empty
+    bool is_borrowed = false;
     hb_options opts{};
     uint64_t footprint = 0;
     int state = HB_JOB_QUEUED;
@@ -101,8 +103,10 @@ static void run_job(hb_server* s, std::shared_ptr<Job> job) {
     if (!r) {
         hb_options o = job->opts;
         o.stream = stream;
-        hb_graph_view v{job->graph.n, job->graph.m, job->graph.offsets.data(),
-                        job->graph.successors.data()};
+        hb_graph_view v = job->is_borrowed ? job->borrowed
+                                           : hb_graph_view{job->graph.n, job->graph.m,
+                                                           job->graph.offsets.data(),
+                                                           job->graph.successors.data()};
         r = hb_create(&v, nullptr, &o, &h);
         if (r) msg = hb_global_last_error();
     }
@@ -207,7 +211,8 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
     return HB_OK;
 }
 
-int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options* opts, uint64_t* job) {
+static int submit_impl(hb_server* s, const hb_graph_view* graph, const hb_options* opts, bool borrow,
+                       uint64_t* job) {
     if (!s || !graph || !opts || !job) return server_err(HB_ERR_INVALID, "NULL argument");
     if (opts->struct_size != sizeof(hb_options))
         return server_err(HB_ERR_INVALID, "hb_options.struct_size mismatch");
@@ -222,8 +227,13 @@ int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options*
                                               " device bytes, more than the budget");
     j->graph.n = graph->num_nodes;
     j->graph.m = graph->num_arcs;
-    j->graph.offsets.assign(graph->offsets, graph->offsets + graph->num_nodes + 1);
-    j->graph.successors.assign(graph->successors, graph->successors + graph->num_arcs);
+    if (borrow) {
+        j->borrowed = *graph;
+        j->is_borrowed = true;
+    } else {
+        j->graph.offsets.assign(graph->offsets, graph->offsets + graph->num_nodes + 1);
+        j->graph.successors.assign(graph->successors, graph->successors + graph->num_arcs);
+    }
     j->opts = *opts;
     j->opts.device = s->opts.device;
     j->opts.stream = nullptr;
@@ -238,6 +248,15 @@ int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options*
     }
     s->cv.notify_all();
     return HB_OK;
+}
+
+int hb_server_submit(hb_server* s, const hb_graph_view* graph, const hb_options* opts, uint64_t* job) {
+    return submit_impl(s, graph, opts, false, job);
+}
+
+int hb_server_submit_borrowed(hb_server* s, const hb_graph_view* graph, const hb_options* opts,
+                              uint64_t* job) {
+    return submit_impl(s, graph, opts, true, job);
 }
 
 static std::shared_ptr<Job> find_job(hb_server* s, uint64_t id) {

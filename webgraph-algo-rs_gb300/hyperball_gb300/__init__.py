@@ -242,6 +242,7 @@ EXPORTS = [
     ("hb_server_options_default", None, [_P(ServerOptions)]),
     ("hb_server_create", ctypes.c_int, [_P(ServerOptions), _P(_H)]),
     ("hb_server_submit", ctypes.c_int, [_H, _P(GraphView), _P(Options), _P(ctypes.c_uint64)]),
+    ("hb_server_submit_borrowed", ctypes.c_int, [_H, _P(GraphView), _P(Options), _P(ctypes.c_uint64)]),
     ("hb_server_wait", ctypes.c_int, [_H, ctypes.c_uint64, ctypes.c_double]),
     ("hb_server_job_info", ctypes.c_int, [_H, ctypes.c_uint64, _P(JobInfo)]),
     ("hb_server_get_neighborhood_function", ctypes.c_int,
@@ -913,9 +914,12 @@ class HyperBallServer:
         _scheck(lib.hb_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h
         self._nodes = {}
+        self._borrowed = {}
 
     def submit(self, graph, log2m, hasher=None, sum_of_distances=False,
-               sum_of_inverse_distances=False, transpose_on_device=True):
+               sum_of_inverse_distances=False, transpose_on_device=True, borrow=False):
+        """Queues a job. borrow=True skips the copy of the graph: the graph
+        object is then kept alive by the server until the job is released."""
         hasher = hasher or DefaultHasher()
         o = Options()
         self._lib.hb_options_default(ctypes.byref(o))
@@ -928,8 +932,11 @@ class HyperBallServer:
                    | (HB_TRANSPOSE_ON_DEVICE if transpose_on_device else 0))
         v = graph.view()
         job = ctypes.c_uint64()
-        _scheck(self._lib.hb_server_submit(self._h, ctypes.byref(v), ctypes.byref(o), ctypes.byref(job)))
+        submit = self._lib.hb_server_submit_borrowed if borrow else self._lib.hb_server_submit
+        _scheck(submit(self._h, ctypes.byref(v), ctypes.byref(o), ctypes.byref(job)))
         self._nodes[job.value] = (graph.num_nodes, (1 << int(log2m)) * 5 // 8)
+        if borrow:
+            self._borrowed[job.value] = graph
         return job.value
 
     def wait(self, job, timeout=None):
@@ -968,11 +975,13 @@ class HyperBallServer:
     def release(self, job):
         _scheck(self._lib.hb_server_release(self._h, job))
         self._nodes.pop(job, None)
+        self._borrowed.pop(job, None)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.hb_server_destroy(self._h)
             self._h = None
+        self._borrowed = {}
 
     def __del__(self):
         self.close()
