@@ -875,8 +875,7 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
 // parities, the mode, the union-kernel variant; the values that change every
 // iteration reach the kernels through h->d_ic.
 cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::UnionArgs& a,
-                                bool first_systolic, int* err) {
-    *err = HB_OK;
+                                bool first_systolic) {
     if (!h->use_graphs) return nullptr;
     for (const GraphEntry& g : h->graphs)
         if (g.key == key) {
@@ -889,12 +888,17 @@ cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::Un
         if (!in_run) h->shapes_run.push_back(key);
         if (!(in_run && h->capture_in_run)) return nullptr;
     }
+    // A capture that fails turns graphs off for the handle; the iteration
+    // then launches directly (graphs change no result).
+    auto give_up = [&]() -> cudaGraphExec_t {
+        cudaGetLastError();
+        h->use_graphs = false;
+        h->err.clear();
+        return nullptr;
+    };
     const uint64_t c0 = hbk::launch_count();
     cudaError_t e = cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) {
-        *err = cuda_err(h, e, "cudaStreamBeginCapture");
-        return nullptr;
-    }
+    if (e != cudaSuccess) return give_up();
     const int r = enqueue_iteration(h, a, first_systolic, h->cap, true);
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(h->cap, &graph);
@@ -902,17 +906,12 @@ cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::Un
     hbk::count_launches(-(int64_t)launches);  // captured, not launched
     if (r != HB_OK || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
-        cudaGetLastError();
-        *err = r != HB_OK ? r : cuda_err(h, e, "cudaStreamEndCapture");
-        return nullptr;
+        return give_up();
     }
     cudaGraphExec_t exec = nullptr;
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
-        *err = cuda_err(h, e, "cudaGraphInstantiate");
-        return nullptr;
-    }
+    if (e != cudaSuccess) return give_up();
     h->graphs.push_back(GraphEntry{key, exec, launches});
     hbk::count_launches((int64_t)launches);
     return exec;
@@ -949,9 +948,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
         h->h_ic->disc_factor[k] = h->disc_fn[k](h->iteration + 1, h->disc_ctx[k]);
     const bool first_systolic = h->systolic && !prev_was_systolic;
     const GraphKey key{h->cur, h->mbc_cur, h->systolic, first_systolic, (bool)a.gather_all, variant};
-    int gerr = HB_OK;
-    cudaGraphExec_t exec = iteration_graph(h, key, a, first_systolic, &gerr);
-    if (gerr != HB_OK) return gerr;
+    cudaGraphExec_t exec = iteration_graph(h, key, a, first_systolic);
     if (exec) {
         HB_CUDA(h, cudaGraphLaunch(exec, s));
     } else {
