@@ -691,6 +691,7 @@ int choose_variant(hb_handle* h, int cls, bool sample) {
     Tuner& t = h->tuner;
     t.last_class = -1;
     if (t.fixed >= 0) return t.last = t.fixed;
+    if (h->far_ok) return t.last = 0;  // the TMA-gather kernel is its own opt-in variant
     if (cls < 0) return t.last = 0;
     if (t.chosen[cls] >= 0) return t.last = t.chosen[cls];
     if (sample)
