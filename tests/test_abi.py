@@ -122,3 +122,22 @@ def test_transpose(hb):
         for s in t.successors_of(v):
             tp.add((int(s), int(v)))
     assert pairs == tp
+
+
+def test_tuning_entry_points_on_the_host(hb):
+    """The variant count is host-only; the bucket tuner needs a device and
+    fails loudly without one; bad arguments are rejected first."""
+    import ctypes.util
+
+    assert hb.union_variant_count() == 5
+    lib = hb.load_library()
+    sm, mm = ctypes.c_uint32(), ctypes.c_uint32()
+    assert lib.hb_tune_degree_buckets(None, None, 3, ctypes.byref(sm), ctypes.byref(mm), None) == hb.HB_ERR_INVALID
+    assert lib.hb_batch_graph_replays(None, None, None) == hb.HB_ERR_INVALID
+    assert lib.hb_union_variant_chosen(None, None) == hb.HB_ERR_INVALID
+    if ctypes.util.find_library("cuda") is not None and os.path.exists("/dev/nvidia0"):
+        return
+    g = hb.Graph.erdos_renyi(100, 3, 0)
+    logic = hb.HyperLogLogBuilder(100).log_2_num_reg(6).build()
+    with pytest.raises(hb.HyperBallError):
+        hb.tune_degree_buckets(g, logic)
