@@ -932,8 +932,10 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     cudaStream_t s = h->stream;
     hbk::UnionArgs a = union_args(h);
     // nearly every counter changed in the previous iteration: merge all
-    // successors without waiting for their modified bits
-    a.gather_all = !h->systolic && prev_mod >= n - n / 8;
+    // successors without waiting for their modified bits (init marks every
+    // counter modified, HB:1208, so the first iteration merges them all)
+    const uint64_t changed_before = h->iteration == 0 ? n : prev_mod;
+    a.gather_all = !h->systolic && changed_before >= n - n / 8;
     // the union-kernel variant (identical results; see Tuner)
     const uint64_t merged = a.gather_all ? m - h->self_loops : h->pending_visited;
     const int cls = h->systolic ? -1 : a.gather_all ? 0 : 1;
