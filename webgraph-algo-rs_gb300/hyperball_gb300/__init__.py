@@ -594,6 +594,10 @@ class HyperBallBuilder:
         return self
 
     def degree_buckets(self, small_max, medium_max):
+        """Nodes of out-degree up to small_max run one lane group each, up to
+        medium_max one 8-lane team each, above one CTA each (defaults 64 and
+        4096; tune_degree_buckets picks them per graph). The results do not
+        depend on them."""
         self._small, self._medium = int(small_max), int(medium_max)
         return self
 
