@@ -395,7 +395,8 @@ uint64_t hb_kernel_launches(const hb_handle* h);
  * keeps per device; memory a destroyed handle gave back stays reserved there
  * for the next one, so creating and destroying handles in a loop maps no new
  * memory. This returns the reserved, unused memory of `device` to the device
- * (memory in use is untouched). No reference counterpart. */
+ * (memory in use is untouched), and frees the small page-locked host blocks
+ * that destroyed handles left for reuse. No reference counterpart. */
 int hb_release_cached_memory(int device);
 
 #ifdef __cplusplus

@@ -1489,6 +1489,14 @@ int hb_release_cached_memory(int device) {
         cudaGetLastError();
         return set_err(nullptr, HB_ERR_CUDA, std::string("cudaMemPoolTrimTo: ") + cudaGetErrorString(e));
     }
+    // the page-locked blocks no handle holds
+    std::multimap<size_t, void*> blocks;
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        blocks.swap(g_pinned_free);
+    }
+    for (auto& b : blocks) cudaFreeHost(b.second);
+    cudaGetLastError();
     return HB_OK;
 }
 const char* hb_global_last_error(void) { return g_global_err.c_str(); }
