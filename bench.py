@@ -19,8 +19,11 @@ distances and harmonic centralities are read back).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 `--impl reference` times the CPU restatement of the reference algorithm (the
-oracle's threaded engine, one thread per host core) on the same workload; each
-step is one standard iteration of the same run.
+oracle's threaded engine, one thread per host core) on the same workload and
+the same work per step: one complete run (init plus every iteration to
+stabilisation). Its graph comes from the generators compiled into the
+oracle's library, so that process never loads the product library. The GPU
+line's `cpu_baseline` is the same measurement.
 """
 import argparse
 import json
@@ -40,7 +43,9 @@ METRIC = "HyperBall arc-register updates/s"
 UNIT = "arc-register updates/s"
 LOG2M = 6
 COUNTER_BYTES = (1 << LOG2M) * 5 // 8
-PROFILE = os.path.join(ROOT, "profiles", "union_weblike.md")
+PROFILES = {"weblike": os.path.join(ROOT, "profiles", "union_weblike.md"),
+            "rmat": os.path.join(ROOT, "profiles", "union_rmat.md")}
+DIGESTS = os.path.join(ROOT, "tests", "golden", "scale_digests.json")
 
 
 def parse_args():
@@ -88,7 +93,25 @@ def make_graph(args):
     return hb.Graph.weblike(1 << args.log2n)
 
 
-def workload(args):
+def make_oracle_graph(args):
+    """The same graph from the generators compiled into the oracle's library
+    (same source file as the product's)."""
+    from oracle import hbo
+    if args.workload == "rmat":
+        return hbo.OracleGraph.rmat(args.log2n, 16, 0.57, 0.19, 0.19, seed=1)
+    return hbo.OracleGraph.weblike(1 << args.log2n)
+
+
+def digest_key(args):
+    """Name of the committed oracle digest of this workload, if there is one."""
+    if args.workload == "rmat" and args.log2n == 24:
+        return "rmat24"
+    if args.workload == "weblike" and args.log2n == 26:
+        return "weblike26"
+    return None
+
+
+def workload(args, arcs=None, iterations=None):
     if args.workload == "rmat":
         name = f"rmat-2^{args.log2n} HyperBall to stabilisation"
         graph = "R-MAT (0.57, 0.19, 0.19, 0.05), 16 arcs drawn per node, seed 1, duplicates and self-loops removed"
@@ -105,6 +128,9 @@ def workload(args):
         "mode": "systolic, transpose built on device",
         "outputs": "neighbourhood function, sum of distances, harmonic centrality",
         "l2": f"inputs larger than L2 (two 2^n x {COUNTER_BYTES} B counter arrays, CSR 4 B/arc)",
+        "arcs": arcs,
+        "iterations": iterations,
+        "parallelism": "replicas x" + os.environ.get("WORLD_SIZE", "1"),
     }
 
 
@@ -213,38 +239,44 @@ class ClockSampler:
 N_SUMS = 2  # sum of distances and harmonic centrality are requested
 
 
-def union_model_bytes(stats, n):
-    """Compulsory HBM bytes of the union kernels of each iteration:
-    8 B offsets per scanned node, 4 B per successor id read, one counter read
-    per distinct modified successor (bounded by min(previously modified,
-    visited arcs)), prev read + next write of every scanned node, the
-    modified / must-be-checked bitmaps, and for every changed counter the
-    estimate cache and each requested per-node sum read and written once.
-    Counters count at the reference's size (2^log2m * 5 / 8 bytes)."""
+def union_model_bytes(stats, n, with_sums=False):
+    """Compulsory HBM bytes of the union kernels of each iteration (the
+    per-iteration model B_t of the hot-path measurement plan):
+        8 (S_t + 1)   offsets of the scanned nodes
+      + 4 A_t         successor ids of the scanned nodes
+      + W U_t         one read per distinct modified successor counter
+                      (U_t bounded by min(previously modified, visited arcs))
+      + 2 W S_t       previous read and next write of the scanned nodes
+      + n / 4         the four bitmaps
+    with W the reference's counter size (2^log2m * 5 / 8 bytes). with_sums
+    adds, per changed counter, the requested per-node sums and the estimate
+    cache read and written once (16 + 16 * N_SUMS bytes)."""
     out = []
     prev_mod = n  # init marks every counter modified
     for s in stats:
         S, A, V, M = s["scanned_nodes"], s["scanned_arcs"], s["visited_arcs"], s["modified_counters"]
         U = min(prev_mod, V)
-        out.append(8 * S + 4 * A + COUNTER_BYTES * U + 2 * COUNTER_BYTES * S + n // 4
-                   + (16 + 16 * N_SUMS) * M)
+        b = 8 * (S + 1) + 4 * A + COUNTER_BYTES * U + 2 * COUNTER_BYTES * S + n // 4
+        if with_sums:
+            b += (16 + 16 * N_SUMS) * M
+        out.append(b)
         prev_mod = M
     return out
 
 
-def profiled_traffic_ratio():
-    """DRAM bytes per model byte of the union kernel, from the committed ncu
-    summary (None when there is none)."""
+def profiled_traffic_ratio(workload_name):
+    """DRAM bytes per model byte of one union launch, from the committed ncu
+    summary of this workload (None when there is none)."""
     try:
-        text = open(PROFILE).read()
-    except OSError:
+        text = open(PROFILES[workload_name]).read()
+    except (OSError, KeyError):
         return None
     m = re.search(r"dram_bytes_per_model_byte:\s*([0-9.]+)", text)
     return float(m.group(1)) if m else None
 
 
 # ---------------------------------------------------------------------------
-# CPU restatement (oracle) sample: standard iterations of the same workload
+# CPU restatement (oracle): one complete run of the same workload
 # ---------------------------------------------------------------------------
 def host_cores():
     try:
@@ -253,62 +285,100 @@ def host_cores():
         return os.cpu_count() or 1
 
 
-class CpuSample:
-    """The oracle's threaded engine (one thread per host core) on the same graph;
-    each sample is one iteration of the run (the first ones are standard
-    iterations over every arc)."""
+def cpu_full_run(offsets, successors, t_offsets, t_successors, warm_iterations):
+    """The oracle's threaded engine (one thread per host core) on the graph:
+    `warm_iterations` iterations of a first run (untimed), then one complete
+    run timed, init plus every iteration until no counter changes, which is
+    the work of one GPU step. Returns units, seconds, iterations, cores."""
+    from oracle import hbo
+    cores = host_cores()
+    o = hbo.OracleHyperBall(offsets, successors, LOG2M, 0, 0, t_offsets=t_offsets,
+                            t_successors=t_successors, sod=True, harm=True, threads=cores)
+    o.init()
+    for _ in range(warm_iterations):
+        if o.iterate()["modified"] == 0:
+            break
+    t = time.perf_counter()
+    o.init()
+    visited, iters = 0, 0
+    while True:
+        st = o.iterate()
+        visited += st["visited_arcs"]
+        iters += 1
+        if st["modified"] == 0:
+            break
+    secs = time.perf_counter() - t
+    return {"units": visited << LOG2M, "seconds": secs, "iterations": iters, "cores": cores}
 
-    def __init__(self, graph):
-        import numpy as np
-        from oracle import hbo
-        self.cores = host_cores()
-        self.off = np.array(graph.offsets)
-        self.suc = np.array(graph.successors)
-        self.o = hbo.OracleHyperBall(self.off, self.suc, LOG2M, 0, 0, sod=True, harm=True,
-                                     threads=self.cores)
-        t = time.perf_counter()
-        self.o.init()
-        self.init_s = time.perf_counter() - t
 
-    def step(self):
-        t = time.perf_counter()
-        s = self.o.iterate()
-        dt = time.perf_counter() - t
-        return s["visited_arcs"] << LOG2M, dt, s["iteration"]
+def cpu_baseline_object(r, warm_iterations):
+    return {
+        "value": r["units"] / r["seconds"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+        "sample": (f"C++ restatement of the reference algorithm (oracle), threaded engine, "
+                   f"{r['cores']} threads: one complete run of the same graph (init + "
+                   f"{r['iterations']} iterations to stabilisation, the GPU step's work) in "
+                   f"{r['seconds']:.1f} s, after {warm_iterations} warm-up iterations"),
+    }
 
 
 # ---------------------------------------------------------------------------
 def run_reference(args):
+    """The CPU arm: only oracle/ libraries are loaded in this process."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    import hyperball_gb300 as hb
-    g = make_graph(args)
-    cpu = CpuSample(g)
-    for _ in range(args.warmup):
-        cpu.step()
-    units, secs, its = 0, 0.0, []
-    for _ in range(args.steps):
-        u, dt, it = cpu.step()
-        units += u
-        secs += dt
-        its.append(it)
-    value = units / secs
-    sample = (f"iterations {its[0]}-{its[-1]} of the run (after {args.warmup} warm-up "
-              f"iterations), {units >> LOG2M} visited arcs, {secs:.1f} s")
+    g = make_oracle_graph(args)
+    t = g.transpose()
+    r = cpu_full_run(g.offsets, g.successors, t.offsets, t.successors, args.warmup)
+    value = r["units"] / r["seconds"]
+    cb = cpu_baseline_object(r, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "n_gpus": args.gpus, "steps": 1, "warmup": args.warmup,
+        "ms_per_step": 1e3 * r["seconds"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": workload(args),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cpu.cores, "kind": "port",
-                         "sample": "C++ restatement of the reference algorithm (oracle), "
-                                   "threaded engine; " + sample},
+        "config": workload(args, g.num_arcs, r["iterations"]),
+        "cpu_baseline": cb,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("one step = one complete run (minutes on the host cores), so one step is timed; "
+                 "the warm-up is the first iterations of an earlier run"),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def check_digest(h, args, buf_holder):
+    """Compares the last run of handle h with the committed oracle digest of
+    this workload: per-iteration modified counters and visited arcs, the
+    SHA-256 of the final registers and the neighbourhood function (1e-12).
+    Raises on a mismatch; returns a summary (None without a digest)."""
+    import hashlib
+    import numpy as np
+    key = digest_key(args)
+    if key is None or not os.path.exists(DIGESTS):
+        return None
+    d = json.load(open(DIGESTS))["cases"].get(key)
+    if d is None:
+        return None
+    st = h.iteration_stats()
+    got = [(s["modified_counters"], s["visited_arcs"]) for s in st]
+    want = [(it["modified"], it["visited_arcs"]) for it in d["iterations"]]
+    if got != want:
+        raise RuntimeError(f"oracle digest {key}: per-iteration counts differ")
+    buf = h.registers(0)
+    sha = hashlib.sha256(buf).hexdigest()
+    del buf
+    if sha != d["iterations"][-1]["registers_sha256"]:
+        raise RuntimeError(f"oracle digest {key}: final registers differ")
+    nf = h.neighborhood_function()
+    ref = np.array(d["neighborhood_function"])
+    err = float(np.max(np.abs(nf - ref) / np.maximum(np.abs(ref), 1e-300)))
+    if len(nf) != len(ref) or err > 1e-12:
+        raise RuntimeError(f"oracle digest {key}: neighbourhood function differs ({err:.2e})")
+    return {"oracle_digest": key, "result": "match",
+            "checked": "per-iteration modified counters and visited arcs, SHA-256 of the final "
+                       "registers (bit-exact), neighbourhood function within 1e-12",
+            "nf_max_rel_err": err}
 
 
 def run_gb300(args):
@@ -343,6 +413,8 @@ def run_gb300(args):
         h.run_until_done()
     ref_stats = [dict(s) for s in h.iteration_stats()]
     units_per_step = sum(s["visited_arcs"] for s in ref_stats) << LOG2M
+    # the run just finished against the oracle's digest of this workload
+    parity = check_digest(h, args, None)
 
     # --- device-resident timed region -------------------------------------
     props = torch.cuda.get_device_properties(local)
@@ -356,7 +428,7 @@ def run_gb300(args):
     # the timed region is the profiled range (ncu --profile-from-start off)
     torch.cuda.profiler.start()
     ev0.record(stream)
-    union_ms, model_bytes, iters = 0.0, 0, 0
+    union_ms, model_bytes, model_sums, iters = 0.0, 0, 0, 0
     for _ in range(args.steps):
         h.run_until_done()
         st = h.iteration_stats()
@@ -364,6 +436,7 @@ def run_gb300(args):
             raise RuntimeError("visited arcs differ between runs")
         union_ms += sum(s["union_ms"] for s in st)
         model_bytes += sum(union_model_bytes(st, n))
+        model_sums += sum(union_model_bytes(st, n, with_sums=True))
         iters += len(st)
     ev1.record(stream)
     torch.cuda.synchronize()
@@ -383,14 +456,23 @@ def run_gb300(args):
         peak_src = "measured"
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
-    ratio = profiled_traffic_ratio()
+    ratio = profiled_traffic_ratio(args.workload)
     per_launch_model = model_bytes / iters
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_src,
         "traffic": ratio * per_launch_model if ratio else None,
+        "traffic_source": (f"DRAM bytes per model byte of the committed ncu capture of this "
+                           f"workload ({os.path.relpath(PROFILES[args.workload], ROOT)}) times "
+                           f"the model bytes of the average launch") if ratio else
+                          "no ncu capture of this workload",
         "kernel": "union (k_union_window + k_union_heavy), one launch each per iteration",
+        "model": "compulsory bytes: 8(S+1) + 4A + W U + 2 W S + n/4 per iteration",
         "model_bytes_per_launch": per_launch_model,
+        "with_sums": {"achieved": model_sums / (union_ms / 1e3) / 1e9,
+                      "frac": model_sums / (union_ms / 1e3) / 1e9 / peak,
+                      "note": "the same model plus the per-node sums and estimate cache of "
+                              "each changed counter (48 B)"},
         "union_ms_per_step": union_ms / args.steps,
     }
 
@@ -442,14 +524,13 @@ def run_gb300(args):
 
     cpu_baseline = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = CpuSample(g)
-        u, dt, it = cpu.step()
-        cpu_baseline = {
-            "value": u / dt, "unit": UNIT, "cores": cpu.cores, "kind": "port",
-            "sample": f"C++ restatement of the reference algorithm (oracle), threaded engine: "
-                      f"iteration {it} of the same run (standard, {u >> LOG2M} visited arcs) "
-                      f"in {dt:.1f} s",
-        }
+        from oracle import hbo
+        t = hbo.OracleGraph.transpose_of(g.offsets, g.successors)
+        r = cpu_full_run(g.offsets, g.successors, t.offsets, t.successors, 1)
+        del t
+        if r["units"] != units_per_step:
+            raise RuntimeError("the oracle's run visited other arcs than the GPU's")
+        cpu_baseline = cpu_baseline_object(r, 1)
 
     if rank == 0:
         line = {
@@ -457,14 +538,13 @@ def run_gb300(args):
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": dict(workload(args), arcs=m, iterations=len(ref_stats),
-                           parallelism=f"replicas x{world}",
-                           degree_buckets=[small, medium],
-                           bucket_tuning_s=round(t_tune, 2),
-                           union_variants=variants,
-                           graph_replayed_iterations=f"{replayed} of {len(st)}"),
+            "config": workload(args, m, len(ref_stats)),
+            "tuning": {"degree_buckets": [small, medium], "bucket_tuning_s": round(t_tune, 2),
+                       "union_variants": variants,
+                       "graph_replayed_iterations": f"{replayed} of {len(st)}"},
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
-            "clocks": clk, "gpu_launches": launches,
+            "parity": parity, "clocks": clk, "gpu_launches": launches,
+            "iteration_union_ms": [round(s["union_ms"], 3) for s in st],
         }
         print(json.dumps(line), flush=True)
     ranks.close()

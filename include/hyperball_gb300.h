@@ -368,20 +368,33 @@ int hb_device_transpose(const uint64_t* d_offsets, const uint32_t* d_successors,
                         void* stream);
 
 /* hb_device_transpose without any device allocation, for callers that cannot
- * allocate: code that must not call the CUDA allocator while it runs (inside a
- * stream-capture region, or a serving loop whose device memory is fixed up
- * front) or a process whose memory pool is exhausted. No reference
+ * allocate: a serving loop whose device memory is reserved up front and must
+ * not grow while it runs, a host program that hands all device memory to its
+ * own allocator, or a process whose memory pool is exhausted. No reference
  * counterpart. Its scratch is one fixed array in the library's device memory
- * (a little over 8 MiB per device), so num_nodes is at most 1,048,576;
- * larger graphs get HB_ERR_INVALID. That array is shared by every call on a
- * device: calls that overlap in time (other streams or threads) race on it and
- * must be serialized by the caller. The first call on each device looks up the
- * array's address (cudaGetSymbolAddress) once; make that first call before
- * any stream capture. No claim is made about capturing the call in a CUDA
+ * (a little over 8 MiB per device, held until the process exits), so
+ * num_nodes is at most 1,048,576; larger graphs get HB_ERR_INVALID. That
+ * array is shared by every call on a device: calls that overlap in time
+ * (other streams or threads) race on it and must be serialized by the caller.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) once; make that first call before any stream
+ * capture. `stream` must belong to the current device (HB_ERR_INVALID
+ * otherwise). The call checks the graph and waits for its stream like
+ * hb_device_transpose. No claim is made about capturing the call in a CUDA
  * graph. Same arguments, checks and results as hb_device_transpose. */
 int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_successors,
                                 uint64_t num_nodes, uint64_t num_arcs, uint64_t* d_t_offsets,
                                 uint32_t* d_t_successors, void* stream);
+
+/* Test hook of the TMA far-gather variant (HB_TMA_GATHER): every bounded
+ * mbarrier wait of the handle's union kernel gives up after `polls` polls
+ * (0: the default limit), and `extra_tx_bytes` (at most 2^20) are added to
+ * every expected transaction count, so that no wait can complete and the
+ * timeout path runs: the kernel releases the extra bytes, waits (bounded)
+ * for its copies in flight, issues no more TMA copies, and the iteration
+ * returns HB_ERR_TIMEOUT. hb_init then starts a clean run. Pass (0, 0) to
+ * restore the defaults. No reference counterpart. */
+int hb_debug_far_wait(hb_handle* h, uint32_t polls, uint32_t extra_tx_bytes);
 
 /* ---- introspection ---------------------------------------------------------- */
 /* Library build string, e.g. "hyperball_gb300 sm_103a". */

@@ -3,6 +3,9 @@
 Compiles oracle/hyperball_oracle.cpp into oracle/_build/libhb_oracle.so with
 g++. The reference crate itself is Rust and cannot be built in this image (no
 cargo/rustc), so there is no oracle/_ref: the oracle is this C++ restatement.
+The seeded graph generators (webgraph-algo-rs_gb300/csrc/graph_gen.cpp, plain
+C++) are compiled in too, so a process that only runs the oracle can build the
+benchmark graphs without loading the product library.
 
 -ffp-contract=off keeps every f64 multiply and add separately rounded, as Rust
 computes them; without it gcc on aarch64 fuses a*b+c into fmadd and the
@@ -14,8 +17,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhb_oracle.so")
-SOURCES = [os.path.join(HERE, "hyperball_oracle.cpp")]
-HEADERS = [os.path.join(HERE, "hll_oracle.hpp")]
+GEN_DIR = os.path.join(os.path.dirname(HERE), "webgraph-algo-rs_gb300", "csrc")
+SOURCES = [os.path.join(HERE, "hyperball_oracle.cpp"), os.path.join(GEN_DIR, "graph_gen.cpp")]
+HEADERS = [os.path.join(HERE, "hll_oracle.hpp"), os.path.join(GEN_DIR, "graph_gen.h")]
 
 
 def _stale():
@@ -28,7 +32,7 @@ def _stale():
 def command():
     return [
         "g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-pthread",
-        "-ffp-contract=off", "-Wall", "-Wno-unused-function",
+        "-ffp-contract=off", "-Wall", "-Wno-unused-function", "-I" + GEN_DIR,
         "-o", LIB, *SOURCES,
     ]
 

@@ -86,6 +86,18 @@ def lib():
             "hbo_hll_count_hashes": (ctypes.c_double, [ctypes.c_int, ctypes.c_uint64,
                                                        _P(ctypes.c_uint64), ctypes.c_uint64,
                                                        _P(ctypes.c_uint64), ctypes.c_uint64]),
+            "hbo_gen_er": (V, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64]),
+            "hbo_gen_rmat": (V, [ctypes.c_int, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_uint64]),
+            "hbo_gen_weblike": (V, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double,
+                                    ctypes.c_uint64, ctypes.c_uint64]),
+            "hbo_graph_transpose": (V, [V]),
+            "hbo_transpose_csr": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32)]),
+            "hbo_graph_nodes": (ctypes.c_uint64, [V]),
+            "hbo_graph_arcs": (ctypes.c_uint64, [V]),
+            "hbo_graph_offsets": (V, [V]),
+            "hbo_graph_successors": (V, [V]),
+            "hbo_graph_free": (None, [V]),
         }
         for k, (r, a) in sig.items():
             f = getattr(L, k)
@@ -93,6 +105,56 @@ def lib():
             f.argtypes = a
         _lib = L
     return _lib
+
+
+class OracleGraph:
+    """A CSR graph made by the seeded generators compiled into the oracle's
+    library (the same source as the product's): `offsets` (u64, n+1) and
+    `successors` (u32, m) are views of memory this object owns."""
+
+    def __init__(self, handle):
+        if not handle:
+            raise MemoryError("graph generation failed")
+        self._h = ctypes.c_void_p(handle)
+        L = lib()
+        self.num_nodes = int(L.hbo_graph_nodes(self._h))
+        self.num_arcs = int(L.hbo_graph_arcs(self._h))
+        self.offsets = self._view(L.hbo_graph_offsets(self._h), self.num_nodes + 1, ctypes.c_uint64)
+        self.successors = self._view(L.hbo_graph_successors(self._h), self.num_arcs, ctypes.c_uint32)
+
+    @staticmethod
+    def _view(ptr, count, ctype):
+        if count == 0 or not ptr:
+            return np.zeros(count, dtype=np.dtype(ctype))
+        return np.ctypeslib.as_array(ctypes.cast(ptr, _P(ctype)), shape=(count,))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hbo_graph_free(self._h)
+            self._h = None
+
+    @staticmethod
+    def erdos_renyi(n, d, seed):
+        return OracleGraph(lib().hbo_gen_er(n, d, seed))
+
+    @staticmethod
+    def rmat(scale, edges_per_node, a=0.57, b=0.19, c=0.19, seed=1):
+        return OracleGraph(lib().hbo_gen_rmat(scale, edges_per_node, a, b, c, seed))
+
+    @staticmethod
+    def weblike(n, cap=100_000, shift=1.266, window=1024, seed=2):
+        return OracleGraph(lib().hbo_gen_weblike(n, cap, shift, window, seed))
+
+    def transpose(self):
+        return OracleGraph(lib().hbo_graph_transpose(self._h))
+
+    @staticmethod
+    def transpose_of(offsets, successors):
+        """The transpose of a CSR held in numpy arrays (rows sorted)."""
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        suc = np.ascontiguousarray(successors, dtype=np.uint32)
+        return OracleGraph(lib().hbo_transpose_csr(len(off) - 1, off.ctypes.data_as(_P(ctypes.c_uint64)),
+                                                   suc.ctypes.data_as(_P(ctypes.c_uint32))))
 
 
 def word_bits_for(log2m):

@@ -23,6 +23,7 @@
 // (Rust never fuses), which keeps per-node sums bit-identical to the
 // reference's arithmetic.
 #include "hll_oracle.hpp"
+#include "graph_gen.h"
 
 #include <atomic>
 #include <cstdio>
@@ -738,6 +739,47 @@ uint64_t hbo_check_div_small_int(uint64_t d_max, uint64_t samples, uint64_t seed
     }
     return bad;
 }
+
+// ---- input graphs ------------------------------------------------------------
+// The seeded generators are webgraph-algo-rs_gb300/csrc/graph_gen.cpp compiled
+// into this library (the product library compiles the same file), so the CPU
+// baseline builds the GPU path's input graphs without loading the product.
+void* hbo_gen_er(uint64_t n, uint32_t d, uint64_t seed) {
+    Csr* g = new Csr();
+    hbg::gen_er(n, d, seed, *g);
+    return g;
+}
+void* hbo_gen_rmat(int scale, uint64_t edges_per_node, double a, double b, double c,
+                   uint64_t seed) {
+    Csr* g = new Csr();
+    hbg::gen_rmat(scale, edges_per_node, a, b, c, seed, *g);
+    return g;
+}
+void* hbo_gen_weblike(uint64_t n, uint64_t cap, double shift, uint64_t window, uint64_t seed) {
+    Csr* g = new Csr();
+    hbg::gen_weblike(n, cap, shift, window, seed, *g);
+    return g;
+}
+void* hbo_graph_transpose(const void* g) {
+    Csr* t = new Csr();
+    hbg::transpose(*(const Csr*)g, *t);
+    return t;
+}
+void* hbo_transpose_csr(uint64_t n, const uint64_t* off, const uint32_t* succ) {
+    Csr g;
+    g.n = n;
+    g.m = off[n];
+    g.offsets.assign(off, off + n + 1);
+    g.successors.assign(succ, succ + g.m);
+    Csr* t = new Csr();
+    hbg::transpose(g, *t);
+    return t;
+}
+uint64_t hbo_graph_nodes(const void* g) { return ((const Csr*)g)->n; }
+uint64_t hbo_graph_arcs(const void* g) { return ((const Csr*)g)->m; }
+const uint64_t* hbo_graph_offsets(const void* g) { return ((const Csr*)g)->offsets.data(); }
+const uint32_t* hbo_graph_successors(const void* g) { return ((const Csr*)g)->successors.data(); }
+void hbo_graph_free(void* g) { delete (Csr*)g; }
 
 // Per-counter parameters for the tests.
 void hbo_hll_params(int log2m, uint64_t n, double* alpha_m_m, uint64_t* words16) {

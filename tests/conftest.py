@@ -11,9 +11,13 @@ for p in (REPO, PKG):
 
 GOLDEN = os.path.join(REPO, "tests", "golden")
 # cnr-2000 BVGraph copies made by tests/golden/make_fixtures.py (git-ignored,
-# shipped with the working tree); the reference checkout is used when present.
-CNR_DIRS = [os.path.join(GOLDEN, "_data"), "/root/reference/tests/graphs"]
-CNR_RESULTS_DIRS = [os.path.join(GOLDEN, "_data"), "/root/reference/tests/hyperball_results"]
+# shipped with the working tree); a reference checkout named by the
+# HB_REFERENCE environment variable is searched after them.
+_REF = os.environ.get("HB_REFERENCE")
+CNR_DIRS = [os.path.join(GOLDEN, "_data")] + (
+    [os.path.join(_REF, "tests", "graphs")] if _REF else [])
+CNR_RESULTS_DIRS = [os.path.join(GOLDEN, "_data")] + (
+    [os.path.join(_REF, "tests", "hyperball_results")] if _REF else [])
 
 
 def pytest_configure(config):

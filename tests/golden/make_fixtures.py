@@ -1,7 +1,7 @@
 """Makes the test fixtures derived from the reference checkout.
 
-Run in a container where the reference is mounted (default
-/root/reference). It
+Run with the environment variable HB_REFERENCE set to a checkout of the
+reference crate. It
   1. copies the cnr-2000 BVGraph files and the five Java-produced HyperBall
      results into tests/golden/_data/ (git-ignored: used by the GPU tests on
      machines without the reference checkout);
@@ -26,7 +26,9 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 sys.path.insert(0, os.path.join(REPO, "webgraph-algo-rs_gb300"))
 
-REF = os.environ.get("HB_REFERENCE", "/root/reference")
+REF = os.environ.get("HB_REFERENCE")
+if __name__ == "__main__" and not REF:
+    raise SystemExit("set HB_REFERENCE to the reference checkout")
 NAMES = ["sum_of_distances", "harmonic_centrality", "lin_centrality",
          "closeness_centrality", "nieminen_centrality"]
 

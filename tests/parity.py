@@ -30,7 +30,8 @@ def assert_close(a, b, rtol, what):
 
 def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True, harm=True,
              transpose_on_device=False, buckets=None, max_iters=10_000, check_next=True,
-             discounts=(), tma=False, far_rows=None, variant=None, graphs=True, warm_runs=0):
+             discounts=(), tma=False, far_rows=None, variant=None, graphs=True, warm_runs=0,
+             weights=None, weight_seed=0):
     """Runs GPU and oracle side by side; returns (gpu, oracle, stats list)."""
     hasher = hb.JenkinsHasher(seed) if hash_kind == 1 else hb.DefaultHasher()
     logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(log2m).build_hasher(hasher).build()
@@ -39,6 +40,8 @@ def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True
     else:
         b = hb.HyperBallBuilder.new(g, logic).transpose_on_device(transpose_on_device)
     b = b.sum_of_distances(sod).sum_of_inverse_distances(harm)
+    if weights is not None:
+        b = b.weights(weights, weight_seed)
     for f in discounts:
         b = b.discount_function(f)
     if buckets:
@@ -52,7 +55,8 @@ def lockstep(hb, oracle, g, log2m, hash_kind=0, seed=0, transpose=None, sod=True
     orc = oracle.OracleHyperBall(
         g.offsets, g.successors, log2m, hash_kind=hash_kind, seed=seed,
         t_offsets=t.offsets if has_t else None, t_successors=t.successors if has_t else None,
-        sod=sod, harm=harm, threads=1, discounts=discounts)
+        sod=sod, harm=harm, threads=1, discounts=discounts, weights=weights,
+        weight_seed=weight_seed)
     for _ in range(warm_runs):
         gpu.run_until_done()  # the shapes of a finished run are replayed as CUDA graphs
     gpu.init()

@@ -56,8 +56,10 @@ def test_union_model_bytes():
     ]
     w, f = bench.COUNTER_BYTES, 16 + 16 * bench.N_SUMS
     got = bench.union_model_bytes(stats, n)
-    assert got[0] == 8 * 1000 + 4 * 8000 + w * min(n, 7900) + 2 * w * 1000 + n // 4 + f * 900
-    assert got[1] == 8 * 300 + 4 * 2000 + w * min(900, 500) + 2 * w * 300 + n // 4 + f * 0
+    assert got[0] == 8 * 1001 + 4 * 8000 + w * min(n, 7900) + 2 * w * 1000 + n // 4
+    assert got[1] == 8 * 301 + 4 * 2000 + w * min(900, 500) + 2 * w * 300 + n // 4
+    ext = bench.union_model_bytes(stats, n, with_sums=True)
+    assert ext[0] == got[0] + f * 900 and ext[1] == got[1]
 
 
 def test_clock_summary():
@@ -83,6 +85,25 @@ def test_reference_arm_line():
     assert line["value"] > 0 and line["unit"] == bench.UNIT
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    # the same config keys as the GPU arm's line, filled from the CPU run
+    assert set(line["config"]) == {"workload", "nodes", "graph", "log2m", "hash", "mode",
+                                   "outputs", "l2", "arcs", "iterations", "parallelism"}
+    assert line["config"]["arcs"] > 0 and line["config"]["iterations"] > 0
+
+
+def test_reference_arm_loads_only_oracle_libraries():
+    """The CPU arm builds its graph with the generators compiled into the
+    oracle's library: no library of the product is mapped in that process."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--log2n', '11', "
+            "'--steps', '1', '--warmup', '1']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\n"
+            "except SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('MAPS', 'libhyperball_gb300' in maps, 'libhb_oracle' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    assert "MAPS False True" in r.stdout
 
 
 def test_reference_arm_other_ranks_exit_quietly():

@@ -53,6 +53,31 @@ def test_tma_far_gathers_rmat(hb, oracle):
     lockstep(hb, oracle, g, 6, transpose_on_device=True, tma=True)
 
 
+def test_tma_wait_timeout_reports_and_recovers(hb, oracle):
+    """The far-gather mbarrier wait is bounded. With bytes added to every
+    expected count the wait cannot complete: the iteration must return
+    HB_ERR_TIMEOUT (after the kernel drained its copies), and the same handle
+    must then run a clean, oracle-exact run after hb_init."""
+    g = hb.Graph.weblike(6000, cap=200, window=512, seed=3)
+    logic = hb.HyperLogLogBuilder(g.num_nodes).log_2_num_reg(6).build()
+    gpu = (hb.HyperBallBuilder.new(g, logic).transpose_on_device(True).sum_of_distances(True)
+           .tma_gather(True, 1).cuda_graphs(False).build())
+    gpu.debug_far_wait(polls=64, extra_tx_bytes=16)
+    gpu.init()
+    with pytest.raises(hb.HyperBallError) as ei:
+        gpu.iterate()
+    assert ei.value.code == hb.HB_ERR_TIMEOUT
+    gpu.debug_far_wait(0, 0)
+    gpu.run_until_done()
+    orc = oracle.OracleHyperBall(g.offsets, g.successors, 6, sod=True,
+                                 t_offsets=g.transpose().offsets,
+                                 t_successors=g.transpose().successors)
+    orc.run_until_done()
+    assert gpu.iteration == orc.iteration
+    np.testing.assert_array_equal(gpu.registers(0), orc.registers(0))
+    assert_close(gpu.sum_of_distances(), orc.sum_of_distances(), 1e-12, "sum of distances")
+
+
 @pytest.mark.parametrize("log2m", [4, 6, 8])
 @pytest.mark.parametrize("variant", range(5))
 def test_union_variants(hb, oracle, log2m, variant):
@@ -171,6 +196,23 @@ def test_discount_functions(hb, oracle):
     g = hb.Graph.erdos_renyi(2000, 4, 9)
     lockstep(hb, oracle, g, 6, transpose=g.transpose(),
              discounts=(lambda d: 1.0 / (d * d), lambda d: 0.5 ** d))
+
+
+@pytest.mark.parametrize("log2m,hash_kind", [(4, 0), (6, 0), (8, 1)])
+def test_node_weights(hb, oracle, log2m, hash_kind):
+    """Node weights (HB:1165-1174): node v starts with w[v] added values
+    instead of its own id. The reference draws them from a thread RNG (not
+    reproducible); here value k of node v is SplitMix64 step k from
+    weight_seed ^ v * golden, on the GPU (k_init) and in the oracle alike.
+    Weights of 0 leave a counter empty; large ones fill many registers."""
+    g = hb.Graph.erdos_renyi(3000, 5, 21 + log2m)
+    rng = np.random.default_rng(log2m)
+    w = rng.integers(0, 6, size=g.num_nodes).astype(np.uint64)
+    w[::97] = 0
+    w[5] = 3000
+    for seed in (0, 12345):
+        lockstep(hb, oracle, g, log2m, hash_kind=hash_kind, seed=42 * hash_kind,
+                 transpose=g.transpose(), weights=w, weight_seed=seed)
 
 
 def test_edge_cases(hb, oracle):

@@ -84,6 +84,58 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     assert b"at most 1048576" in lib.hb_global_last_error()
 
 
+class _CurrentPool:
+    """The current memory pool of device 0 through the driver API (the pool
+    cudaMallocAsync draws from): its used-memory high watermark can be reset
+    and read, so a call that allocated from it, even briefly, shows."""
+    USED_MEM_CURRENT, USED_MEM_HIGH = 7, 8  # CUmemPool_attribute
+
+    def __init__(self):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        dev = ctypes.c_int()
+        assert self.cu.cuDeviceGet(ctypes.byref(dev), 0) == 0
+        self.pool = ctypes.c_void_p()
+        assert self.cu.cuDeviceGetMemPool(ctypes.byref(self.pool), dev) == 0
+
+    def _get(self, attr):
+        v = ctypes.c_uint64()
+        assert self.cu.cuMemPoolGetAttribute(self.pool, attr, ctypes.byref(v)) == 0
+        return v.value
+
+    def reset_high(self):
+        zero = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, self.USED_MEM_HIGH, ctypes.byref(zero)) == 0
+
+    def used_high(self):
+        return self._get(self.USED_MEM_HIGH)
+
+
+def test_noalloc_allocates_no_device_memory():
+    lib = hb.load_library()
+    g = hb.Graph.weblike(1 << 18, seed=9)
+    n, m = g.num_nodes, g.num_arcs
+    d_off, d_succ = _device_csr(g)
+    t_off = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    t_succ = torch.empty(m, dtype=torch.int32, device="cuda")
+    args = (d_off.data_ptr(), d_succ.data_ptr(), n, m, t_off.data_ptr(), t_succ.data_ptr(), None)
+    pool = _CurrentPool()
+    # the allocating transpose shows up in the pool's watermark ...
+    torch.cuda.synchronize()
+    pool.reset_high()
+    assert lib.hb_device_transpose(*args) == hb.HB_OK
+    assert pool.used_high() > 0
+    # ... the fixed-scratch one does not, and the free device memory stays put
+    lib.hb_device_transpose_noalloc(*args)  # first call on the device: address lookup
+    torch.cuda.synchronize()
+    pool.reset_high()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(2):
+        assert lib.hb_device_transpose_noalloc(*args) == hb.HB_OK
+    torch.cuda.synchronize()
+    assert pool.used_high() == 0
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
 def test_noalloc_rejects_invalid_graphs_and_handles_empty_ones():
     lib = hb.load_library()
     # successor out of range: refused before any kernel indexes with it

@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HEADERS = [
     os.path.join(CSRC, "hb_internal.h"),
     os.path.join(CSRC, "hll_device.cuh"),
+    os.path.join(CSRC, "graph_gen.h"),
     os.path.join(REPO, "include", "hyperball_gb300.h"),
 ]
 
@@ -44,7 +45,7 @@ def _units():
         cmd = [os.path.join(cuda, "bin", "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17",
                "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj]
         units.append((src, obj, cmd))
-    for name in ("hb_engine.cpp", "graph_host.cpp", "hb_server.cpp"):
+    for name in ("hb_engine.cpp", "graph_host.cpp", "graph_gen.cpp", "hb_server.cpp"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OBJ, name + ".o")
         cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall",

@@ -238,6 +238,8 @@ struct hb_handle {
     CUtensorMap far_map[2];
     bool far_ok = false;
     uint32_t far_rows = 8192;
+    uint32_t far_polls = 0;       // hb_debug_far_wait: poll limit (0: default)
+    uint32_t far_extra_tx = 0;    // hb_debug_far_wait: bytes that never arrive
     uint64_t n_tiles = 0;         // number of windows
     uint2* d_chunks = nullptr;      // work units of the union kernel, in node order
     uint32_t* d_indeg = nullptr;    // in-degree without self-loops
@@ -669,6 +671,8 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.partials = h->d_partials;
     a.far_tma = h->far_ok ? 1 : 0;
     a.far_rows = h->far_rows;
+    a.mbar_polls = h->far_polls;
+    a.test_extra_tx = h->far_extra_tx;
     a.pf = 0;
     a.pd = 0;
     a.occ = 0;
@@ -1455,6 +1459,23 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
                            cudaGetErrorString((cudaError_t)r));
     }
     cudaStream_t s = (cudaStream_t)stream;
+    // the scratch address is the current device's; a stream of another
+    // device would run the kernels on that device's copy of nothing
+    if (s != nullptr) {
+        int cur = -1, sdev = -1;
+        cudaError_t de = cudaGetDevice(&cur);
+        if (de == cudaSuccess) de = cudaStreamGetDevice(s, &sdev);
+        if (de != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(nullptr, HB_ERR_CUDA,
+                           std::string("hb_device_transpose_noalloc: ") + cudaGetErrorString(de));
+        }
+        if (sdev != cur)
+            return set_err(nullptr, HB_ERR_INVALID,
+                           "hb_device_transpose_noalloc: the stream belongs to device " +
+                               std::to_string(sdev) + ", the current device is " +
+                               std::to_string(cur) + "; make the stream's device current");
+    }
     const uint64_t n = num_nodes, sl = hbk::scan_scratch_len(n + 1);
     if (n + 1 + sl + 1 > words)
         return set_err(nullptr, HB_ERR_INVALID, "hb_device_transpose_noalloc: scratch too small");
@@ -1468,6 +1489,19 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
         cudaGetLastError();
         return set_err(nullptr, HB_ERR_CUDA, std::string("hb_device_transpose_noalloc: ") + cudaGetErrorString(e));
     }
+    return HB_OK;
+}
+
+int hb_debug_far_wait(hb_handle* h, uint32_t polls, uint32_t extra_tx_bytes) {
+    if (!h) return set_err(nullptr, HB_ERR_INVALID, "null handle");
+    if (extra_tx_bytes > (1u << 20))
+        return set_err(h, HB_ERR_INVALID, "extra_tx_bytes must be at most 2^20");
+    h->far_polls = polls;
+    h->far_extra_tx = extra_tx_bytes;
+    // captured iterations hold the old values: capture again
+    cudaStreamSynchronize(h->stream);
+    for (GraphEntry& g : h->graphs) cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
     return HB_OK;
 }
 

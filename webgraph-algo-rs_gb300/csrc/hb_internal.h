@@ -10,20 +10,9 @@
 #include <vector_types.h>
 
 #include "../../include/hyperball_gb300.h"
-
-// Host CSR graph: offsets[n+1] (u64), successors[m] (u32), rows sorted.
-struct Csr {
-    uint64_t n = 0, m = 0;
-    std::vector<uint64_t> offsets;
-    std::vector<uint32_t> successors;
-};
+#include "graph_gen.h"
 
 namespace hbg {
-void transpose(const Csr& g, Csr& t);
-void gen_er(uint64_t n, uint32_t d, uint64_t seed, Csr& g);
-void gen_rmat(int scale, uint64_t edges_per_node, double a, double b, double c, uint64_t seed,
-              Csr& g);
-void gen_weblike(uint64_t n, uint64_t cap, double shift, uint64_t window, uint64_t seed, Csr& g);
 int load_bvgraph(const std::string& basename, Csr& g, std::string& err, uint64_t* bits_checked);
 }  // namespace hbg
 
@@ -58,6 +47,8 @@ struct UnionArgs {
     CUtensorMap far_map;      // the current counters as rows of 2^log2m bytes (TMA gathers)
     int far_tma;              // 1: far successors by TMA gathers (far_map valid)
     uint32_t far_rows;        // a successor is far when more than this many ids from its node
+    uint32_t mbar_polls;      // polls of a bounded far-gather wait (0: the default limit)
+    uint32_t test_extra_tx;   // tests only: bytes added to every expected count (the wait cannot complete)
     const uint64_t* off;      // CSR offsets, n+1
     const uint32_t* succ;     // CSR successors, m
     const uint8_t* curr;      // current counters, n * 2^log2m bytes (byte per register)

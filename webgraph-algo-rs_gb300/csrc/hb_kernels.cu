@@ -407,15 +407,21 @@ __device__ __forceinline__ void mbar_arrive_expect(uint32_t bar, uint32_t bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint32_t polls) {
+    const uint32_t limit = polls ? polls : (uint32_t)MBAR_POLLS;
     uint32_t done = 0;
-    for (int i = 0; i < MBAR_POLLS && !done; i++)
+    for (uint32_t i = 0; i < limit && !done; i++)
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
             : "=r"(done)
             : "r"(bar), "r"(phase)
             : "memory");
     return done != 0;
+}
+// counts `bytes` in as if a copy had delivered them (releases the bytes a
+// test added to the expected count)
+__device__ __forceinline__ void mbar_complete_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 // orders this thread's earlier shared-memory reads before later TMA writes
 __device__ __forceinline__ void fence_proxy_async() {
@@ -469,7 +475,7 @@ __device__ __forceinline__ void merge_far(uint32_t region, int c, int nf,
 
 // A warp's far-gather slots and mbarrier (dynamic and static shared memory of
 // the union kernel), and its state: bit 0 the barrier's phase, bit 1 set when
-// a wait gave up.
+// a wait gave up (the warp then issues no more TMA copies).
 extern __shared__ __align__(128) uint8_t far_smem[];
 __shared__ __align__(8) unsigned long long far_bar[8];
 template <int LOG2M>
@@ -543,9 +549,9 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
         // far successors: one TMA gather per lane group, in flight during the
         // plain loads below
         int nfar = 0;
-        bool far_used = false;
+        bool far_used = false, gave_up = false;
         if constexpr (FAR && FarGeo<LOG2M>::ON) {
-            {
+            if (!(fs.bits & 2u)) {
                 uint32_t f[FAR_SLOTS];
                 if (scan) nfar = collect_far(a, v, s0 + p, s1, PB, filter, f);
                 const bool issue = nfar > 0 && c == 0;
@@ -554,7 +560,8 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
                     far_used = true;
                     if (lane == 0)
                         mbar_arrive_expect(far_barrier(),
-                                           (uint32_t)__popc(im) * FAR_SLOTS * FarGeo<LOG2M>::ROW);
+                                           (uint32_t)__popc(im) * FAR_SLOTS * FarGeo<LOG2M>::ROW +
+                                               a.test_extra_tx);
                     __syncwarp();
                     if (issue)
                         tma_gather4(far_region<LOG2M>(lane), &a.far_map, f[0], f[1], f[2], f[3],
@@ -573,11 +580,11 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
             }
             gather_rolling<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc, nfar);
             if (nfar > 0) {
-                if (mbar_wait(far_barrier(), fs.bits & 1u)) {
+                if (mbar_wait(far_barrier(), fs.bits & 1u, a.mbar_polls)) {
                     merge_far<LOG2M>(far_region<LOG2M>(lane), c, nfar, acc);
                     fence_proxy_async();
                 } else {
-                    fs.bits |= 2u;
+                    gave_up = true;
                 }
             }
             if constexpr (PB > 1) {
@@ -616,6 +623,18 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
             uint32_t w[NW];
             load_chunk<LOG2M>(a.curr, v, c, w);
             store_chunk<LOG2M>(a.next, v, c, w);
+        }
+        if constexpr (FAR && FarGeo<LOG2M>::ON) {
+            if (__any_sync(0xffffffffu, gave_up)) {
+                // A wait gave up: the iteration fails (HB_ERR_TIMEOUT). Drain
+                // this warp's copies before going on without the far path:
+                // release any bytes a test added to the expected count, then
+                // wait once more, again bounded, for the phase to complete.
+                if (lane == 0 && a.test_extra_tx) mbar_complete_tx(far_barrier(), a.test_extra_tx);
+                __syncwarp();
+                mbar_wait(far_barrier(), fs.bits & 1u, a.mbar_polls);
+                fs.bits |= 2u;
+            }
         }
         if (far_used) fs.bits ^= 1u;
         // modified bits, aggregated over the lanes that hit the same word

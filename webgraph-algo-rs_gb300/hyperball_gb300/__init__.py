@@ -262,6 +262,7 @@ EXPORTS = [
     ("hb_device_transpose_noalloc", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
+    ("hb_debug_far_wait", ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),
 ]
 
 _lib = None
@@ -716,6 +717,12 @@ class HyperBall:
     def init(self):
         _check(self._lib.hb_init(self._h), self._h)
 
+    def debug_far_wait(self, polls=0, extra_tx_bytes=0):
+        """Test hook (hb_debug_far_wait): bounds the TMA far-gather waits to
+        `polls` polls and adds bytes that never arrive to every expected
+        count, so the timeout path runs. (0, 0) restores the defaults."""
+        _check(self._lib.hb_debug_far_wait(self._h, int(polls), int(extra_tx_bytes)), self._h)
+
     def iterate(self):
         s = IterStats()
         _check(self._lib.hb_iterate(self._h, ctypes.byref(s)), self._h)
@@ -791,9 +798,14 @@ class HyperBall:
         _check(self._lib.hb_union_variant_chosen(self._h, c), self._h)
         return list(c)
 
-    def registers(self, which=HB_CURRENT_STATE):
-        """Raw counter bytes (num_nodes x counter_bytes), reference layout."""
-        out = np.zeros((self.num_nodes, self.counter_bytes), dtype=np.uint8)
+    def registers(self, which=HB_CURRENT_STATE, out=None):
+        """Raw counter bytes (num_nodes x counter_bytes), reference layout;
+        `out` is an optional C-contiguous uint8 array of that shape to fill."""
+        shape = (self.num_nodes, self.counter_bytes)
+        if out is None:
+            out = np.zeros(shape, dtype=np.uint8)
+        elif out.dtype != np.uint8 or out.shape != shape or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous uint8 array of num_nodes x counter_bytes")
         _check(self._lib.hb_get_registers(self._h, which, out.ctypes.data, out.nbytes), self._h)
         return out
 
