@@ -78,14 +78,38 @@ def test_tma_wait_timeout_reports_and_recovers(hb, oracle):
     assert_close(gpu.sum_of_distances(), orc.sum_of_distances(), 1e-12, "sum of distances")
 
 
+N_VARIANTS = 9
+STAGED = (5, 6, 7, 8)
+
+
 @pytest.mark.parametrize("log2m", [4, 6, 8])
-@pytest.mark.parametrize("variant", range(5))
+@pytest.mark.parametrize("variant", range(N_VARIANTS))
 def test_union_variants(hb, oracle, log2m, variant):
     """Every union-kernel variant (prefetch into L1 or L2, 3 or 4 blocks per
-    SM) gives the oracle's counters, in every kind of iteration."""
-    assert hb.union_variant_count() == 5
+    SM, the staged kernel with one or two loads in flight) gives the oracle's
+    counters, in every kind of iteration."""
+    assert hb.union_variant_count() == N_VARIANTS
     g = hb.Graph.weblike(20_000, cap=3000, window=256, seed=variant)
     lockstep(hb, oracle, g, log2m, transpose_on_device=True, variant=variant)
+
+
+@pytest.mark.parametrize("log2m", [5, 7, 9, 10])
+@pytest.mark.parametrize("variant", STAGED)
+def test_staged_kernel_log2m(hb, oracle, log2m, variant):
+    """The staged kernel at every chunk width (1 to 16 lanes per counter),
+    light and medium items, standard iterations only (no transpose)."""
+    g = hb.Graph.weblike(9000, cap=1500, window=128, seed=log2m)
+    lockstep(hb, oracle, g, log2m, variant=variant, buckets=(16, 512))
+
+
+@pytest.mark.parametrize("variant", STAGED)
+def test_staged_kernel_filtered_rmat(hb, oracle, variant):
+    """R-MAT leaves many counters unchanged, so standard iterations merge only
+    modified successors (the filtered path of the staged kernel); items with
+    more arcs than the staged ids read the rest from global memory."""
+    g = hb.Graph.rmat(13, 16, seed=4)
+    lockstep(hb, oracle, g, 6, variant=variant, buckets=(64, 4096))
+    lockstep(hb, oracle, g, 8, transpose_on_device=True, variant=variant, buckets=(1024, 4096))
 
 
 def test_autotuner_identical_results(hb):

@@ -148,9 +148,14 @@ struct hb_graph {
 // prefetching measured slower there: they run the first variant.
 // ---------------------------------------------------------------------------
 struct UnionVariant {
-    uint32_t pf, pd, occ;
+    uint32_t pf, pd, occ, staged;
 };
-constexpr UnionVariant kVariants[] = {{0, 0, 0}, {2, 2, 0}, {0, 0, 1}, {2, 2, 1}, {1, 4, 0}};
+// plain loads, L1 prefetch, 4 blocks per SM, both, L2 prefetch; the staged
+// kernel (standard iterations) with one or two counter loads in flight per
+// light lane (staged 1 / 2), at 3 and 4 blocks per SM
+constexpr UnionVariant kVariants[] = {{0, 0, 0, 0}, {2, 2, 0, 0}, {0, 0, 1, 0}, {2, 2, 1, 0},
+                                      {1, 4, 0, 0}, {0, 0, 0, 1}, {0, 0, 1, 1}, {0, 0, 0, 2},
+                                      {0, 0, 1, 2}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 constexpr int kTunedClasses = 2;  // gather-all standard, filtered standard
 constexpr uint64_t kTuneMinArcs = 1ull << 22;  // smaller graphs keep the first variant
@@ -277,6 +282,8 @@ struct hb_handle {
     bool any31 = false;
     int grid_tile = 1, grid_heavy = 1, grid_mark = 1;
     int grid_tile_occ = 1;           // the window kernel's grid in its 4-blocks-per-SM variant
+    int grid_staged = 1, grid_staged_occ = 1;  // the staged kernel's grids
+    uint4* d_items = nullptr;        // item table of the staged kernel (null: not usable)
     Tuner tuner;
     // iterations as CUDA graphs: captured on `cap`, launched on `stream`
     bool use_graphs = true;
@@ -557,7 +564,9 @@ int relabel_csr(hb_handle* h, const uint64_t* off0, const uint32_t* succ0, uint6
     int* bad = nullptr;
     const uint64_t sl = hbk::scan_scratch_len(n + 1);
     if ((r = dalloc(h, d_off, n + 1))) return r;
-    if ((r = dalloc(h, d_succ, m))) return r;
+    // padded: the staged kernel copies successor ids in aligned 16-byte units
+    if ((r = dalloc(h, d_succ, m + 8))) return r;
+    HB_CUDA(h, cudaMemsetAsync(*d_succ + m, 0, 8 * sizeof(uint32_t), h->stream));
     if ((r = dalloc(h, &deg, n + 1))) return r;
     if ((r = dalloc(h, &scratch, sl))) return r;
     if ((r = dalloc(h, &tiles, hbk::arc_tiles(m) + 1))) return r;
@@ -660,6 +669,8 @@ hbk::UnionArgs union_args(hb_handle* h) {
     a.medium_list = nullptr;
     a.list_counts = nullptr;
     a.chunks = h->d_chunks;
+    a.items = h->d_items;
+    a.staged = 0;
     a.gather_all = 0;
     a.indeg = h->d_indeg;
     a.nf_items = h->d_nf_items;
@@ -850,7 +861,9 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
         HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, ah, h->grid_heavy, h->side));
         HB_CUDA(h, cudaEventRecord(h->join, h->side));
     }
-    if (h->n_tiles)
+    if (h->n_tiles && a.staged)
+        HB_LAUNCH(h, hbk::launch_union_staged(h->log2m, a, a.occ ? h->grid_staged_occ : h->grid_staged, s));
+    else if (h->n_tiles)
         HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, a.occ ? h->grid_tile_occ : h->grid_tile, s));
     if (h->n_heavy) HB_CUDA(h, cudaStreamWaitEvent(s, h->join, 0));
     HB_CUDA(h, rec(h->ev[2]));
@@ -948,6 +961,8 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     a.pf = kVariants[variant].pf;
     a.pd = kVariants[variant].pd;
     a.occ = kVariants[variant].occ;
+    // the staged kernel runs standard iterations (systolic ones walk node lists)
+    a.staged = !h->systolic && h->d_items ? kVariants[variant].staged : 0;
     // the values that change from one iteration to the next
     h->h_ic->d1 = (double)(h->iteration + 1);
     h->h_ic->rd1 = 1.0 / h->h_ic->d1;
@@ -1782,11 +1797,23 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     trace.mark("state arrays");
     h->grid_tile = hbk::tile_grid(h->log2m, h->device, 0);
     h->grid_tile_occ = hbk::tile_grid(h->log2m, h->device, 1);
+    h->grid_staged = hbk::staged_grid(h->log2m, h->device, 0);
+    h->grid_staged_occ = hbk::staged_grid(h->log2m, h->device, 1);
     {
         // one warp per chunk, 8 warps per block
         const uint64_t need = (h->n_chunks + 7) / 8 + 1;
         if ((uint64_t)h->grid_tile > need) h->grid_tile = (int)need;
         if ((uint64_t)h->grid_tile_occ > need) h->grid_tile_occ = (int)need;
+        if ((uint64_t)h->grid_staged > need) h->grid_staged = (int)need;
+        if ((uint64_t)h->grid_staged_occ > need) h->grid_staged_occ = (int)need;
+    }
+    // the staged kernel's item table (arc positions are u32 there)
+    if (h->n_chunks && h->m + 64 < (1ull << 32)) {
+        if ((r = dalloc(hp, &h->d_items, h->n_chunks))) return fail(r);
+        if ((r = cuda_err(hp, (cudaError_t)hbk::launch_chunk_items(h->d_chunks, h->n_chunks, h->d_off,
+                                                                   h->d_items, h->stream),
+                          "k_chunk_items")))
+            return fail(r);
     }
     if (o.union_variant != HB_AUTO) {
         if (o.union_variant >= (uint32_t)kNumVariants)

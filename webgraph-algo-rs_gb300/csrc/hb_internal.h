@@ -81,6 +81,8 @@ struct UnionArgs {
     const uint32_t* medium_list;
     const uint64_t* list_counts;
     const uint2* chunks;      // {first node, count | medium << 31}, in node order
+    const uint4* items;       // staged kernel: {first node, count | medium << 31, first arc, arcs}
+    uint32_t staged;          // 1: standard iteration on the staged kernel (k_union_staged)
     int gather_all;           // merge every successor (nearly all changed before)
     const uint32_t* indeg;    // in-degree without self-loops
     double* nf_items;         // neighbourhood-function part of each work item, then of each heavy node
@@ -147,6 +149,12 @@ int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream);
 // for this size (log2m > 8, n >= 2^31) or the driver cannot encode it.
 int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* out);
 int tile_grid(int log2m, int device, int occ);
+// standard iterations on the staged window kernel (items table; m < 2^32)
+int launch_union_staged(int log2m, const UnionArgs& a, int grid, void* stream);
+int staged_grid(int log2m, int device, int occ);
+// items[k] = {first, count | medium << 31, off[first], arcs of the chunk}
+int launch_chunk_items(const uint2* chunks, uint64_t n_chunks, const uint64_t* off, uint4* items,
+                       void* stream);
 // nodes and staged arcs one tile holds at this log2m
 int tile_capacity(int log2m, uint32_t* nodes, uint32_t* arcs);
 // heavy nodes, one CTA each

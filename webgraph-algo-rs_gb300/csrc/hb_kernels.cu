@@ -762,6 +762,336 @@ __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constan
 }
 
 // ---------------------------------------------------------------------------
+// Staged window kernel for standard iterations (every node scanned).
+//
+// k_union_window spends most of a light node's time in dependent round trips
+// that carry few bytes: the cursor atomic, the chunk descriptor, the
+// offsets, the first successor id, the per-node sums after the merge. Here
+// every warp runs a software pipeline over its work items:
+//   * the cursor is read two items ahead and the item descriptor
+//     ({first node, count | medium << 31, first arc, arcs}) one item ahead;
+//   * while item k runs, cp.async copies item k+1's offsets, successor ids
+//     (up to STAGE_IDS of them), cached estimates, per-node sums and
+//     in-degrees into the warp's other shared-memory buffer;
+// so an item starts with everything but the counters on chip: the own
+// counter and the successor gathers are the only global round trips left,
+// and the gathers of a lane are issued PIPE at a time from ids in shared
+// memory. Nodes of an item are consecutive, so the modified bits of an item
+// are one ballot and at most two atomicOr.
+// The counters, the neighbourhood-function part of each item (same items,
+// same lanes, same order) and every per-node value are those of
+// k_union_window. Requires m < 2^32 (item arcs are u32).
+// ---------------------------------------------------------------------------
+constexpr int STAGE_IDS = 256;  // successor ids staged per item
+
+template <int LOG2M>
+struct StageGeo {
+    static constexpr int MAXN = 32 / Geo<LOG2M>::CHUNKS;  // nodes of a light item (>= medium)
+    static constexpr int IDW = STAGE_IDS + 8;             // room for the 16-byte alignment shift
+    // byte offsets inside one buffer
+    static constexpr int OFF_IDS = 0;
+    static constexpr int OFF_OFF = OFF_IDS + IDW * 4;
+    static constexpr int OFF_EST = OFF_OFF + ((MAXN + 2) / 2) * 16;
+    static constexpr int OFF_SOD = OFF_EST + MAXN * 8;
+    static constexpr int OFF_HARM = OFF_SOD + MAXN * 8;
+    static constexpr int OFF_INDEG = OFF_HARM + MAXN * 8;
+    static constexpr int OFF_DESC = OFF_INDEG + ((MAXN * 4 + 15) / 16) * 16;
+    static constexpr int BUF = OFF_DESC + 16;
+    static constexpr int WARP = 2 * BUF;
+};
+
+template <int LOG2M>
+__host__ __device__ constexpr int staged_smem_bytes() {
+    return 8 * StageGeo<LOG2M>::WARP;
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Item k+1's per-node data and successor ids into buffer `buf` (byte address
+// in shared memory) by the 32 lanes of the warp. d = {first, count | medium
+// << 31, first arc, arcs}. The successor array is padded to a multiple of 4
+// ids plus 8, so the last 16-byte copy stays inside it.
+template <int LOG2M>
+__device__ __forceinline__ void stage_item(const UnionArgs& a, uint4 d, uint32_t buf, int lane) {
+    using SG = StageGeo<LOG2M>;
+    const uint32_t first = d.x, cnt = d.y & 0x7fffffffu;
+    // ids: 16-byte units from the aligned word at or below the first arc
+    const uint32_t base = d.z & ~3u;
+    const uint32_t want = min(d.w, (uint32_t)STAGE_IDS);
+    const uint32_t units = (d.z + want - base + 3) >> 2;
+    for (uint32_t u = lane; u < units; u += 32)
+        cp_async16(buf + SG::OFF_IDS + 16 * u, a.succ + base + 4 * u);
+    // cnt + 1 offsets: up to 33 of them
+    for (uint32_t i = lane; i <= cnt; i += 32) cp_async8(buf + SG::OFF_OFF + 8 * i, a.off + first + i);
+    if ((uint32_t)lane < cnt) {
+        cp_async8(buf + SG::OFF_EST + 8 * lane, a.est + first + lane);
+        if (a.sod) cp_async8(buf + SG::OFF_SOD + 8 * lane, a.sod + first + lane);
+        if (a.harm) cp_async8(buf + SG::OFF_HARM + 8 * lane, a.harm + first + lane);
+        cp_async4(buf + SG::OFF_INDEG + 4 * lane, a.indeg + first + lane);
+    }
+    if (lane == 0) {
+        // the descriptor itself, for the lanes that run the item
+        asm volatile("st.shared.v4.u32 [%0], {%1,%2,%3,%4};" ::"r"(buf + SG::OFF_DESC), "r"(d.x),
+                     "r"(d.y), "r"(base), "r"(d.z + want) : "memory");
+    }
+}
+
+template <class T>
+__device__ __forceinline__ T lds(uint32_t addr);
+template <>
+__device__ __forceinline__ uint32_t lds<uint32_t>(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+template <>
+__device__ __forceinline__ unsigned long long lds<unsigned long long>(uint32_t addr) {
+    unsigned long long v;
+    asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(addr));
+    return v;
+}
+template <>
+__device__ __forceinline__ double lds<double>(uint32_t addr) {
+    double v;
+    asm volatile("ld.shared.f64 %0, [%1];" : "=d"(v) : "r"(addr));
+    return v;
+}
+
+// Successor id of arc e: from the staged ids when it is among them.
+struct StagedIds {
+    uint32_t smem;   // address of staged word 0 (arc `base`)
+    uint32_t base;   // arc of staged word 0
+    uint32_t end;    // arcs below this are staged
+    const uint32_t* succ;
+    __device__ __forceinline__ uint32_t operator()(uint32_t e) const {
+        return e < end ? lds<uint32_t>(smem + 4 * (e - base)) : __ldg(succ + e);
+    }
+};
+
+// Merges into acc (chunk c) the counters of arcs e0, e0 + stride, ... (< e1):
+// all of them (gather_all) or the non-loop ones modified in the previous
+// iteration. PIPE counter loads in flight per lane.
+template <int LOG2M, int PIPE>
+__device__ __forceinline__ void staged_gather(const UnionArgs& a, const StagedIds& ids, uint32_t v,
+                                              int c, uint32_t e0, uint32_t e1, uint32_t stride,
+                                              uint32_t (&acc)[Geo<LOG2M>::NW]) {
+    using Gm = Geo<LOG2M>;
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS;
+    if (a.gather_all) {
+        uint32_t y[PIPE][NW];
+        bool have[PIPE];
+#pragma unroll
+        for (int k = 0; k < PIPE; k++) {
+            const uint32_t e = e0 + k * stride;
+            have[k] = e < e1;
+            if (have[k]) load_chunk<LOG2M>(a.curr, ids(e), c, y[k]);
+        }
+        for (uint32_t e = e0 + PIPE * stride; have[0]; e += PIPE * stride) {
+#pragma unroll
+            for (int k = 0; k < PIPE; k++) {
+                if (have[k]) merge_chunk<REGS>(acc, y[k]);
+                const uint32_t ek = e + k * stride;
+                have[k] = ek < e1;
+                if (have[k]) load_chunk<LOG2M>(a.curr, ids(ek), c, y[k]);
+            }
+        }
+        return;
+    }
+    // filtered: the ids and modified bits of 4 arcs load together, then the
+    // counters of the modified ones
+    constexpr int FK = 4;
+    for (uint32_t e = e0; e < e1; e += FK * stride) {
+        uint32_t id[FK];
+#pragma unroll
+        for (int k = 0; k < FK; k++) {
+            const uint32_t ek = e + k * stride;
+            id[k] = ek < e1 ? ids(ek) : v;
+        }
+        uint32_t want = 0;
+#pragma unroll
+        for (int k = 0; k < FK; k++) want |= (uint32_t)(id[k] != v && test_bit(a.curr_mod, id[k])) << k;
+#pragma unroll
+        for (int k = 0; k < FK; k++) {
+            if (!((want >> k) & 1u)) continue;
+            uint32_t y[NW];
+            load_chunk<LOG2M>(a.curr, id[k], c, y);
+            merge_chunk<REGS>(acc, y);
+        }
+    }
+}
+
+// One staged item: nodes [first, first + cnt), TB lanes per node (light:
+// TB = G, medium: the team), from buffer `buf`.
+template <int LOG2M, int TB, int PIPE>
+__device__ __forceinline__ void staged_nodes(const UnionArgs& a, uint32_t buf, int lane, uint32_t& modc,
+                                             uint32_t& scanned, uint32_t& sarcs, uint32_t& vis,
+                                             double& nf) {
+    using Gm = Geo<LOG2M>;
+    using SG = StageGeo<LOG2M>;
+    constexpr int G = Gm::CHUNKS, NW = Gm::NW;
+    constexpr int PB = TB / G;   // arc lanes per node
+    constexpr int NPW = 32 / TB; // nodes per item
+    uint32_t d0, d1, d2, d3;
+    asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(d0), "=r"(d1), "=r"(d2), "=r"(d3)
+                 : "r"(buf + SG::OFF_DESC));
+    const uint32_t first = d0, cnt = d1 & 0x7fffffffu;
+    const StagedIds ids{buf + SG::OFF_IDS, d2, d3, a.succ};
+    const int slot = lane / TB, tl = lane % TB, p = tl / G, c = tl % G;
+    const unsigned tmask = TB == 32 ? 0xffffffffu : (((1u << TB) - 1u) << (slot * TB));
+    const unsigned lmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (slot * TB));
+    const bool live = (uint32_t)slot < cnt;
+    const uint32_t v = first + (uint32_t)slot;
+    bool changed = false;
+    if (live) {
+        const uint32_t s0 = (uint32_t)lds<unsigned long long>(buf + SG::OFF_OFF + 8 * slot);
+        const uint32_t s1 = (uint32_t)lds<unsigned long long>(buf + SG::OFF_OFF + 8 * slot + 8);
+        uint32_t acc[NW];
+        if (PB == 1 || p == 0) {
+            load_chunk<LOG2M>(a.curr, v, c, acc);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NW; k++) acc[k] = 0u;
+        }
+        staged_gather<LOG2M, PIPE>(a, ids, v, c, s0 + p, s1, PB, acc);
+        if constexpr (PB > 1) {
+            __syncwarp(tmask);
+#pragma unroll
+            for (int off = G; off < TB; off <<= 1) {
+#pragma unroll
+                for (int k = 0; k < NW; k += 4) {
+                    uint32_t x4[4], y4[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        x4[j] = acc[k + j];
+                        y4[j] = __shfl_xor_sync(tmask, acc[k + j], off);
+                    }
+                    merge_chunk<16>(x4, y4);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) acc[k + j] = x4[j];
+                }
+            }
+        }
+        if (p == 0) {
+            changed = differs_from<LOG2M>(a.curr, v, c, acc);
+            if constexpr (G > 1) changed = __any_sync(lmask, changed);
+            store_chunk<LOG2M>(a.next, v, c, acc);
+            NodeSums ns{};
+            if (c == 0) {
+                scanned++;
+                sarcs += s1 - s0;
+                ns.pre = lds<double>(buf + SG::OFF_EST + 8 * slot);
+                ns.sod = a.sod ? lds<double>(buf + SG::OFF_SOD + 8 * slot) : 0.0;
+                ns.harm = a.harm ? lds<double>(buf + SG::OFF_HARM + 8 * slot) : 0.0;
+                ns.indeg = lds<uint32_t>(buf + SG::OFF_INDEG + 4 * slot);
+            }
+            finish_node<LOG2M>(a, v, c, lmask, acc, changed, ns, nf, vis);
+        }
+    }
+    // modified bits: the item's nodes are consecutive, one bit per node slot
+    const unsigned ball = __ballot_sync(0xffffffffu, changed && p == 0 && c == 0);
+    if (lane == 0 && ball) {
+        uint32_t bits = 0;
+#pragma unroll
+        for (int k = 0; k < NPW; k++) bits |= ((ball >> (k * TB)) & 1u) << k;
+        const uint32_t w = first >> 5, sh = first & 31;
+        atomicOr(a.next_mod + w, bits << sh);
+        if (sh && (bits >> (32 - sh))) atomicOr(a.next_mod + w + 1, bits >> (32 - sh));
+        modc += __popc(bits);
+    }
+}
+
+// PIPE_L: counter loads in flight per lane of a light node (1 or 2 at
+// 16 words per lane; the narrower chunks of log2m 4 and 5 take more)
+template <int LOG2M, int MINB, int PIPE_L>
+__global__ void __launch_bounds__(256, MINB) k_union_staged(const __grid_constant__ UnionArgs a) {
+    using Gm = Geo<LOG2M>;
+    using SG = StageGeo<LOG2M>;
+    constexpr int G = Gm::CHUNKS;
+    constexpr int TB_MED = team_lanes<LOG2M>();
+    const int lane = threadIdx.x & 31;
+    const uint32_t bufs = (uint32_t)__cvta_generic_to_shared(far_smem) + (threadIdx.x >> 5) * SG::WARP;
+    const uint32_t n_work = (uint32_t)a.n_chunks;
+    uint32_t modc = 0, scanned = 0, sarcs = 0, vis = 0;
+    auto item = [&](uint32_t k) -> uint4 {
+        return k < n_work ? __ldg(a.items + k) : make_uint4(0u, 0u, 0u, 0xffffffffu);
+    };
+    // pipeline: cur (staged), nxt (descriptor loaded), the cursor value of
+    // the item after (lane 0, pending)
+    uint32_t k_cur = 0, k_nxt = 0;
+    unsigned long long atom = 0;
+    if (lane == 0) k_cur = (uint32_t)atomicAdd(a.cursor, 1ull);
+    k_cur = __shfl_sync(0xffffffffu, k_cur, 0);
+    if (lane == 0) k_nxt = (uint32_t)atomicAdd(a.cursor, 1ull);
+    k_nxt = __shfl_sync(0xffffffffu, k_nxt, 0);
+    if (lane == 0) atom = atomicAdd(a.cursor, 1ull);
+    uint4 nxt = item(k_nxt);
+    {
+        const uint4 cur = item(k_cur);
+        if (k_cur < n_work) stage_item<LOG2M>(a, cur, bufs, lane);
+        cp_async_commit();
+    }
+    for (uint32_t it = 0; k_cur < n_work; it++) {
+        const uint32_t k_after = __shfl_sync(0xffffffffu, (uint32_t)atom, 0);
+        if (lane == 0 && k_after < n_work) atom = atomicAdd(a.cursor, 1ull);
+        const uint4 after = item(k_after);
+        if (k_nxt < n_work) stage_item<LOG2M>(a, nxt, bufs + ((it + 1) & 1) * SG::BUF, lane);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncwarp();
+        const uint32_t buf = bufs + (it & 1) * SG::BUF;
+        double nf = 0.0;
+        if (lds<uint32_t>(buf + SG::OFF_DESC + 4) >> 31)
+            staged_nodes<LOG2M, TB_MED, 1>(a, buf, lane, modc, scanned, sarcs, vis, nf);
+        else
+            staged_nodes<LOG2M, G, PIPE_L>(a, buf, lane, modc, scanned, sarcs, vis, nf);
+        nf = warp_sum_f64(nf);
+        if (lane == 0) a.nf_items[k_cur] = nf;
+        __syncwarp();
+        k_cur = k_nxt;
+        k_nxt = k_after;
+        nxt = after;
+    }
+    cp_async_wait<0>();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        modc += __shfl_xor_sync(0xffffffffu, modc, off);
+        scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+        sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
+    }
+    if (lane == 0) {
+        TilePartial* t = a.partials + a.acc_slot;
+        if (modc) atomicAdd(&t->mod, (unsigned long long)modc);
+        if (scanned) atomicAdd(&t->scanned, (unsigned long long)scanned);
+        if (sarcs) atomicAdd(&t->sarcs, (unsigned long long)sarcs);
+        if (vis) atomicAdd(&t->vis, (unsigned long long)vis);
+    }
+}
+
+// item table of the staged kernel: {first, count | medium << 31, first arc, arcs}
+__global__ void k_chunk_items(const uint2* __restrict__ chunks, uint64_t n_chunks,
+                              const uint64_t* __restrict__ off, uint4* __restrict__ items) {
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_chunks;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 d = chunks[k];
+        const uint64_t a0 = off[d.x], a1 = off[d.x + (d.y & 0x7fffffffu)];
+        items[k] = make_uint4(d.x, d.y, (uint32_t)a0, (uint32_t)(a1 - a0));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // heavy nodes: one CTA per node. Lanes split the successors (G lanes per
 // counter), the per-lane partial counters are merged by a butterfly of
 // shuffles and then across warps through shared memory.
@@ -1598,6 +1928,48 @@ static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     return tile_launch<LOG2M, false, 3>(a, grid, s);
 }
 
+template <int LOG2M, int MINB, int PIPE_L>
+static int staged_launch(const UnionArgs& a, int grid, cudaStream_t s) {
+    constexpr int smem = staged_smem_bytes<LOG2M>();
+    if constexpr (smem > 48 * 1024) {
+        static const cudaError_t attr = cudaFuncSetAttribute(
+            k_union_staged<LOG2M, MINB, PIPE_L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (attr != cudaSuccess) return (int)attr;
+    }
+    ++t_launches;
+    k_union_staged<LOG2M, MINB, PIPE_L><<<grid, 256, smem, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+// deep: PIPE_L 2 at 16 words per lane (log2m >= 6), else the narrow pipe
+template <int LOG2M>
+constexpr int staged_pipe(bool deep) {
+    return Geo<LOG2M>::NW >= 16 ? (deep ? 2 : 1) : pipe_depth<Geo<LOG2M>::NW>();
+}
+
+template <int LOG2M>
+static int staged_impl(const UnionArgs& a, int grid, cudaStream_t s) {
+    if (a.staged == 2) {
+        if (a.occ) return staged_launch<LOG2M, 4, staged_pipe<LOG2M>(true)>(a, grid, s);
+        return staged_launch<LOG2M, 3, staged_pipe<LOG2M>(true)>(a, grid, s);
+    }
+    if (a.occ) return staged_launch<LOG2M, 4, staged_pipe<LOG2M>(false)>(a, grid, s);
+    return staged_launch<LOG2M, 3, staged_pipe<LOG2M>(false)>(a, grid, s);
+}
+
+template <int LOG2M>
+static int staged_grid_impl(int device, int occ) {
+    int per_sm = 1;
+    constexpr int smem = staged_smem_bytes<LOG2M>();
+    if (occ)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_union_staged<LOG2M, 4, staged_pipe<LOG2M>(false)>, 256, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_union_staged<LOG2M, 3, staged_pipe<LOG2M>(false)>, 256, smem);
+    return std::max(1, per_sm) * num_sms(device);
+}
+
 template <int LOG2M>
 static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     ++t_launches;
@@ -1724,6 +2096,27 @@ int launch_union_tile(int log2m, const UnionArgs& a, int grid, void* stream) {
 #define CALL(L) tile_impl<L>(a, grid, (cudaStream_t)stream)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
+}
+
+int launch_union_staged(int log2m, const UnionArgs& a, int grid, void* stream) {
+#define CALL(L) staged_impl<L>(a, grid, (cudaStream_t)stream)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int staged_grid(int log2m, int device, int occ) {
+#define CALL(L) staged_grid_impl<L>(device, occ)
+    HB_DISPATCH_LOG2M(log2m, CALL)
+#undef CALL
+}
+
+int launch_chunk_items(const uint2* chunks, uint64_t n_chunks, const uint64_t* off, uint4* items,
+                       void* stream) {
+    if (n_chunks == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n_chunks + 255) / 256, 8192);
+    ++t_launches;
+    k_chunk_items<<<grid, 256, 0, (cudaStream_t)stream>>>(chunks, n_chunks, off, items);
+    return (int)cudaGetLastError();
 }
 
 int launch_union_heavy(int log2m, const UnionArgs& a, int grid, void* stream) {
