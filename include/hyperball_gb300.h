@@ -200,11 +200,11 @@ int hb_get_registers(const hb_handle* h, int which, void* dst, size_t bytes);
 
 /* Variants of the union kernels. They differ in how successor counters are
  * requested (plain loads, or software prefetch into L1 or L2 ahead of the
- * loads), in the registers per thread (3 or 4 resident blocks per SM), and
- * in the kernel that runs standard iterations (variants 5-8: the staged
- * kernel, which copies each work item's offsets, successor ids and per-node
- * sums into shared memory one item ahead, with one or two counter loads in
- * flight per lane); they give bit-identical results. With union_variant = HB_AUTO the library
+ * loads), in the registers per thread (2, 3 or 4 resident blocks per SM;
+ * with 2, two counter loads in flight per lane), and in the kernel that runs
+ * standard iterations (variants 5-8: the staged kernel, which copies each
+ * work item's offsets, per-node sums and, in 5 and 6, successor ids into
+ * shared memory one item ahead); they give bit-identical results. With union_variant = HB_AUTO the library
  * times them on the handle's own standard iterations (one iteration each,
  * per kind of iteration: merging every successor or only modified ones) and
  * keeps the fastest if it beats the first variant by 3%; systolic iterations

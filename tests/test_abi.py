@@ -129,7 +129,7 @@ def test_tuning_entry_points_on_the_host(hb):
     fails loudly without one; bad arguments are rejected first."""
     import ctypes.util
 
-    assert hb.union_variant_count() == 9
+    assert hb.union_variant_count() == 10
     lib = hb.load_library()
     sm, mm = ctypes.c_uint32(), ctypes.c_uint32()
     assert lib.hb_tune_degree_buckets(None, None, 3, ctypes.byref(sm), ctypes.byref(mm), None) == hb.HB_ERR_INVALID

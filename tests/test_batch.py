@@ -63,6 +63,36 @@ def test_batch_equals_instances_alone(hasher):
 
 
 @pytest.mark.gpu
+def test_batch_slice_of_the_benchmark_against_the_oracle(oracle):
+    """The first 64 graphs of the batched benchmark (n log-uniform in
+    [10^3, 2*10^5], Erdos-Renyi and R-MAT, log2m 4, 6 and 8) run as one batch;
+    every instance is compared with the oracle's run of the same graph:
+    iterations, registers bit-exact, neighbourhood function and per-node sums
+    within 1e-12. The batch drops instances once they stop, so this also
+    checks that a stopped instance keeps its final state."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    specs = bench.batch_specs(4096)[:64]
+    gs = bench.make_batch_graphs(specs)
+    log2ms = [sp[3] for sp in specs]
+    b = hb.HyperBallBatch(gs, log2ms, sum_of_distances=True, sum_of_inverse_distances=True)
+    b.run_until_done()
+    for i, (g, l2m) in enumerate(zip(gs, log2ms)):
+        t = g.transpose()
+        o = oracle.OracleHyperBall(g.offsets, g.successors, l2m, t_offsets=t.offsets,
+                                   t_successors=t.successors, sod=True, harm=True, threads=8)
+        o.run_until_done()
+        assert b.iterations(i) == o.iteration, (i, b.iterations(i), o.iteration)
+        np.testing.assert_array_equal(b.registers(i), o.registers(0), err_msg=f"graph {i}")
+        np.testing.assert_allclose(b.neighborhood_function(i), o.neighborhood_function(), rtol=RTOL)
+        np.testing.assert_allclose(b.sum_of_distances(i), o.sum_of_distances(), rtol=RTOL)
+        np.testing.assert_allclose(b.harmonic_centralities(i), o.harmonic_centralities(), rtol=RTOL)
+    b.close()
+
+
+@pytest.mark.gpu
 def test_batch_errors():
     gs, log2ms = _graphs()
     with pytest.raises(hb.InvalidArgumentError):

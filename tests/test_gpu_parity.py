@@ -78,7 +78,7 @@ def test_tma_wait_timeout_reports_and_recovers(hb, oracle):
     assert_close(gpu.sum_of_distances(), orc.sum_of_distances(), 1e-12, "sum of distances")
 
 
-N_VARIANTS = 9
+N_VARIANTS = 10
 STAGED = (5, 6, 7, 8)
 
 

@@ -150,12 +150,14 @@ struct hb_graph {
 struct UnionVariant {
     uint32_t pf, pd, occ, staged;
 };
-// plain loads, L1 prefetch, 4 blocks per SM, both, L2 prefetch; the staged
-// kernel (standard iterations) with one or two counter loads in flight per
-// light lane (staged 1 / 2), at 3 and 4 blocks per SM
+// The window kernel with plain loads, L1 prefetch, 4 blocks per SM, both,
+// L2 prefetch, 2 blocks per SM with two counter loads in flight per light
+// lane (occ 2); the staged kernel (standard iterations) with the successor
+// ids staged (staged 1) or read from global memory (staged 2), at 3 and 4
+// blocks per SM.
 constexpr UnionVariant kVariants[] = {{0, 0, 0, 0}, {2, 2, 0, 0}, {0, 0, 1, 0}, {2, 2, 1, 0},
                                       {1, 4, 0, 0}, {0, 0, 0, 1}, {0, 0, 1, 1}, {0, 0, 0, 2},
-                                      {0, 0, 1, 2}};
+                                      {0, 0, 1, 2}, {0, 0, 2, 0}};
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 constexpr int kTunedClasses = 2;  // gather-all standard, filtered standard
 constexpr uint64_t kTuneMinArcs = 1ull << 22;  // smaller graphs keep the first variant
@@ -251,6 +253,13 @@ struct hb_handle {
     std::vector<uint64_t> inst_start; // batch: instance starts (caller ids), then num_nodes
     uint32_t* d_hash_id = nullptr;    // batch: device node -> its instance's own id
     uint64_t* d_inst_start = nullptr;
+    uint32_t* d_inst_chunk = nullptr;  // batch: first chunk of each instance, then n_chunks
+    uint32_t* d_queue = nullptr;       // batch: chunks of the running instances (standard iterations)
+    uint32_t* d_queue_len = nullptr;
+    unsigned long long* d_q_cnt = nullptr;  // batch: queue construction, instances + 1
+    uint64_t* d_q_at = nullptr;
+    unsigned long long* d_q_scratch = nullptr;
+    uint64_t q_scratch_len = 0;
     unsigned long long* d_inst_mod = nullptr;
     double* d_inst_nf = nullptr;
     std::vector<unsigned long long> inst_mod;    // last iteration, per instance
@@ -282,6 +291,7 @@ struct hb_handle {
     bool any31 = false;
     int grid_tile = 1, grid_heavy = 1, grid_mark = 1;
     int grid_tile_occ = 1;           // the window kernel's grid in its 4-blocks-per-SM variant
+    int grid_tile_two = 1;           // ... and in its 2-blocks-per-SM variant
     int grid_staged = 1, grid_staged_occ = 1;  // the staged kernel's grids
     uint4* d_items = nullptr;        // item table of the staged kernel (null: not usable)
     Tuner tuner;
@@ -780,6 +790,10 @@ int do_init(hb_handle* h) {
                                    h->stream));
     }
     for (int b = 1; b < 4; b++) HB_CUDA(h, cudaMemsetAsync(h->d_bits[b], 0, words * 4, h->stream));
+    // every batch instance runs in the first iteration (the queue keeps
+    // instances whose modified count of the previous iteration is nonzero)
+    if (h->d_inst_mod)
+        HB_CUDA(h, cudaMemsetAsync(h->d_inst_mod, 0xff, (h->inst_start.size() - 1) * 8, h->stream));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     h->any31 = any31 != 0;
     h->iteration = 0;
@@ -808,13 +822,14 @@ int do_init(hb_handle* h) {
     return HB_OK;
 }
 
-// Every asynchronous operation of one iteration, in order, on stream s (the
-// heavy-node kernel on h->side, forked from s and joined back). `external`:
-// the timing events are recorded as graph nodes (stream capture). The host
-// reads the totals from h->h_tot (and, for batches, h->h_inst_*) once s is
-// synchronised; the per-iteration constants come from h->h_ic.
-int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaStream_t s,
-                      bool external) {
+// An iteration's launches in three parts: enqueue_pre (clears, the systolic
+// work lists, a batch's queue of running instances; fills a's lists),
+// enqueue_union (the union kernels of this handle alone) and enqueue_post
+// (predecessor marks, the fixed-order NF sum, totals to the host). Several
+// handles can run their pre and post parts around one shared union launch
+// (multi_iterate).
+int enqueue_pre(hb_handle* h, hbk::UnionArgs& a, bool first_systolic, cudaStream_t s,
+                bool external) {
     const uint64_t n = h->n;
     const uint64_t words = (n + 31) / 32;
     auto rec = [&](cudaEvent_t e) {
@@ -846,8 +861,23 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
         a.light_list = h->d_light_list;
         a.medium_list = h->d_medium_list;
         a.list_counts = h->d_word_off + words;
+    } else if (h->d_queue && h->n_tiles) {
+        // a batch's standard iteration scans the instances still running
+        const uint32_t ni = (uint32_t)(h->inst_start.size() - 1);
+        HB_LAUNCH(h, hbk::launch_inst_queue(h->d_inst_chunk, h->d_inst_mod, ni, 0,
+                                            (uint32_t)h->n_chunks, h->d_q_cnt, h->d_q_at,
+                                            h->d_q_scratch, h->q_scratch_len, h->d_queue,
+                                            h->d_queue_len, s));
+        a.queue = h->d_queue;
+        a.queue_len = h->d_queue_len;
+        a.staged = 0;
     }
     HB_CUDA(h, rec(h->ev[1]));
+    return HB_OK;
+}
+
+// The heavy-node kernel (side stream) and the window kernel of this handle.
+int enqueue_union(hb_handle* h, const hbk::UnionArgs& a, cudaStream_t s, bool window) {
     if (h->n_heavy) {
         // The heavy nodes (one CTA each) start first on the side stream; the
         // window kernel's blocks take the SMs as they free up, so the long
@@ -861,11 +891,26 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
         HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, ah, h->grid_heavy, h->side));
         HB_CUDA(h, cudaEventRecord(h->join, h->side));
     }
-    if (h->n_tiles && a.staged)
+    if (window && h->n_tiles && a.staged)
         HB_LAUNCH(h, hbk::launch_union_staged(h->log2m, a, a.occ ? h->grid_staged_occ : h->grid_staged, s));
-    else if (h->n_tiles)
-        HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a, a.occ ? h->grid_tile_occ : h->grid_tile, s));
+    else if (window && h->n_tiles)
+        HB_LAUNCH(h, hbk::launch_union_tile(h->log2m, a,
+                                            a.occ == 2 ? h->grid_tile_two : a.occ ? h->grid_tile_occ : h->grid_tile,
+                                            s));
+    return HB_OK;
+}
+
+int enqueue_join(hb_handle* h, cudaStream_t s) {
     if (h->n_heavy) HB_CUDA(h, cudaStreamWaitEvent(s, h->join, 0));
+    return HB_OK;
+}
+
+int enqueue_post(hb_handle* h, const hbk::UnionArgs& a, cudaStream_t s, bool external) {
+    const uint64_t n = h->n;
+    auto rec = [&](cudaEvent_t e) {
+        return external ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+    };
+    (void)a;
     HB_CUDA(h, rec(h->ev[2]));
     if (h->systolic)
         HB_LAUNCH(h, hbk::launch_mark_preds(h->d_bits[h->mod_cur ^ 1], h->d_toff, h->d_tsucc,
@@ -883,6 +928,20 @@ int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaS
     HB_CUDA(h, cudaMemcpyAsync(h->h_tot, h->d_partials, sizeof(hbk::TilePartial), cudaMemcpyDeviceToHost, s));
     HB_CUDA(h, rec(h->ev[3]));
     return HB_OK;
+}
+
+// One iteration's launches on s (the union kernels of this handle alone; the
+// heavy-node kernel on h->side, forked from s and joined back). `external`:
+// the timing events are recorded as graph nodes (stream capture). The host
+// reads the totals from h->h_tot (and, for batches, h->h_inst_*) once s is
+// synchronised; the per-iteration constants come from h->h_ic.
+int enqueue_iteration(hb_handle* h, hbk::UnionArgs a, bool first_systolic, cudaStream_t s,
+                      bool external) {
+    int r = enqueue_pre(h, a, first_systolic, s, external);
+    if (!r) r = enqueue_union(h, a, s, true);
+    if (!r) r = enqueue_join(h, s);
+    if (!r) r = enqueue_post(h, a, s, external);
+    return r;
 }
 
 // The executable graph of an iteration of this shape, or null. A shape is
@@ -935,49 +994,59 @@ cudaGraphExec_t iteration_graph(hb_handle* h, const GraphKey& key, const hbk::Un
     return exec;
 }
 
-int do_iterate(hb_handle* h, hb_iter_stats* out) {
+// The host side of one iteration around its launches: iter_plan takes the
+// mode decisions of HB:795-810 and fixes the launch arguments; iter_finish
+// reads the totals back and does the bookkeeping of HB:899-944.
+struct IterPlan {
+    hbk::UnionArgs a;
+    GraphKey key;
+    bool first_systolic = false;
+    int variant = 0;
+    uint64_t merged = 0;
+    uint64_t launches0 = 0;
+    double current_nf = 0.0;
+};
+
+void iter_plan(hb_handle* h, IterPlan& p) {
     const uint64_t n = h->n, m = h->m;
     const uint64_t prev_mod = h->modified_counters;
     const bool prev_was_systolic = h->systolic;
     // HB:795-810
     h->systolic = h->has_transpose && h->iteration > 0 && prev_mod < n / 4;
-    double current_nf = h->systolic ? h->last : 0.0;
+    p.current_nf = h->systolic ? h->last : 0.0;
     h->local = h->pre_local;
     h->pre_local = h->systolic && m > 0 && prev_mod < (n * n) / (m * 10);
 
-    const uint64_t launches0 = hbk::launch_count();
-    cudaStream_t s = h->stream;
-    hbk::UnionArgs a = union_args(h);
+    p.launches0 = hbk::launch_count();
+    hbk::UnionArgs& a = p.a;
+    a = union_args(h);
     // nearly every counter changed in the previous iteration: merge all
     // successors without waiting for their modified bits (init marks every
     // counter modified, HB:1208, so the first iteration merges them all)
     const uint64_t changed_before = h->iteration == 0 ? n : prev_mod;
     a.gather_all = !h->systolic && changed_before >= n - n / 8;
     // the union-kernel variant (identical results; see Tuner)
-    const uint64_t merged = a.gather_all ? m - h->self_loops : h->pending_visited;
+    p.merged = a.gather_all ? m - h->self_loops : h->pending_visited;
     const int cls = h->systolic ? -1 : a.gather_all ? 0 : 1;
-    const bool sample = h->iteration > 0 && m >= kTuneMinArcs && 2 * merged >= m;
-    const int variant = choose_variant(h, cls, sample);
-    a.pf = kVariants[variant].pf;
-    a.pd = kVariants[variant].pd;
-    a.occ = kVariants[variant].occ;
+    const bool sample = h->iteration > 0 && m >= kTuneMinArcs && 2 * p.merged >= m;
+    p.variant = choose_variant(h, cls, sample);
+    a.pf = kVariants[p.variant].pf;
+    a.pd = kVariants[p.variant].pd;
+    a.occ = kVariants[p.variant].occ;
     // the staged kernel runs standard iterations (systolic ones walk node lists)
-    a.staged = !h->systolic && h->d_items ? kVariants[variant].staged : 0;
+    a.staged = !h->systolic && h->d_items ? kVariants[p.variant].staged : 0;
     // the values that change from one iteration to the next
     h->h_ic->d1 = (double)(h->iteration + 1);
     h->h_ic->rd1 = 1.0 / h->h_ic->d1;
     for (size_t k = 0; k < h->d_disc.size(); k++)
         h->h_ic->disc_factor[k] = h->disc_fn[k](h->iteration + 1, h->disc_ctx[k]);
-    const bool first_systolic = h->systolic && !prev_was_systolic;
-    const GraphKey key{h->cur, h->mbc_cur, h->systolic, first_systolic, (bool)a.gather_all, variant};
-    cudaGraphExec_t exec = iteration_graph(h, key, a, first_systolic);
-    if (exec) {
-        HB_CUDA(h, cudaGraphLaunch(exec, s));
-    } else {
-        int r = enqueue_iteration(h, a, first_systolic, s, false);
-        if (r != HB_OK) return r;
-    }
-    HB_CUDA(h, cudaStreamSynchronize(s));
+    p.first_systolic = h->systolic && !prev_was_systolic;
+    p.key = GraphKey{h->cur, h->mbc_cur, h->systolic, p.first_systolic, (bool)a.gather_all, p.variant};
+}
+
+// After the iteration's launches completed (the stream was synchronised).
+// union_ms >= 0 replaces the handle's own union timing (a shared launch).
+int iter_finish(hb_handle* h, IterPlan& p, bool from_graph, double union_ms, hb_iter_stats* out) {
     const hbk::TilePartial tot = *h->h_tot;
     if (tot.timeouts)
         return set_err(h, HB_ERR_TIMEOUT, "a TMA gather did not complete within its bounded wait");
@@ -1000,7 +1069,7 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     // arcs visited in this iteration were fixed by the previous one
     const uint64_t visited = h->pending_visited;
     h->pending_visited = host.st[0];
-    current_nf += host.nf;
+    double current_nf = p.current_nf + host.nf;
     h->last = current_nf;
     const double last_output = h->nf.back();
     if (current_nf < last_output) current_nf = last_output;
@@ -1032,15 +1101,265 @@ int do_iterate(hb_handle* h, hb_iter_stats* out) {
     float ms_union = 0.f, ms_all = 0.f;
     cudaEventElapsedTime(&ms_union, h->ev[1], h->ev[2]);
     cudaEventElapsedTime(&ms_all, h->ev[0], h->ev[3]);
-    st.union_ms = ms_union;
+    st.union_ms = union_ms >= 0.0 ? union_ms : ms_union;
     st.iteration_ms = ms_all;
     st.scanned_arcs = host.st[3];
     st.union_variant = h->tuner.last;
-    st.from_graph = exec != nullptr;
-    record_variant(h, ms_union, host.st[3] + merged);
-    st.kernel_launches = hbk::launch_count() - launches0;
+    st.from_graph = from_graph;
+    if (union_ms < 0.0) record_variant(h, ms_union, host.st[3] + p.merged);
+    st.kernel_launches = hbk::launch_count() - p.launches0;
     h->stats.push_back(st);
     if (out) *out = st;
+    return HB_OK;
+}
+
+int do_iterate(hb_handle* h, hb_iter_stats* out) {
+    IterPlan p;
+    iter_plan(h, p);
+    cudaStream_t s = h->stream;
+    cudaGraphExec_t exec = iteration_graph(h, p.key, p.a, p.first_systolic);
+    if (exec) {
+        HB_CUDA(h, cudaGraphLaunch(exec, s));
+    } else {
+        int r = enqueue_iteration(h, p.a, p.first_systolic, s, false);
+        if (r != HB_OK) return r;
+    }
+    HB_CUDA(h, cudaStreamSynchronize(s));
+    return iter_finish(h, p, exec != nullptr, -1.0, out);
+}
+
+// ---------------------------------------------------------------------------
+// Several handles, one union launch per iteration (no reference
+// counterpart). The log2m groups of a batch and the running jobs of a server
+// advance together: each handle's pre part (clears, work lists, queue), one
+// k_union_jobs launch that drains every handle's window work from one cursor
+// (the heavy-node kernels beside it on the handles' side streams), each
+// handle's post part, one synchronisation, each handle's bookkeeping. The
+// launch sequence of a set of shapes is captured as a CUDA graph the second
+// time it comes and replayed afterwards.
+// ---------------------------------------------------------------------------
+struct MultiCtx {
+    int device = 0;
+    cudaStream_t s = nullptr;         // every launch of a step (the handles' buffers are ordered before it)
+    cudaStream_t cap = nullptr;       // capture stream
+    unsigned long long* d_cursor = nullptr;
+    hbk::UnionArgs* d_jobs = nullptr;
+    int* d_log2m = nullptr;
+    hbk::UnionArgs* h_jobs = nullptr;  // page-locked
+    int* h_log2m = nullptr;
+    int grid = 1;
+    cudaEvent_t u0 = nullptr, u1 = nullptr;
+    bool use_graphs = true;
+    struct Shape {
+        std::vector<const hb_handle*> hs;
+        std::vector<GraphKey> keys;
+        bool operator==(const Shape& o) const { return hs == o.hs && keys == o.keys; }
+    };
+    struct Graph {
+        Shape shape;
+        cudaGraphExec_t exec;
+        uint64_t launches;
+    };
+    std::vector<Graph> graphs;
+    std::vector<Shape> seen;
+    uint64_t steps = 0, replays = 0;
+    double union_ms = 0.0;
+    std::string err;
+};
+
+static bool job_kernel_log2m(int l) { return l == 4 || l == 6 || l == 8; }
+static constexpr uint32_t kMaxJobs = 64;   // k_union_jobs' MAX_JOBS
+static constexpr size_t kMaxMultiGraphs = 64;
+
+static void multi_free(MultiCtx& mc) {
+    cudaSetDevice(mc.device);
+    if (mc.s) cudaStreamSynchronize(mc.s);
+    for (auto& g : mc.graphs) cudaGraphExecDestroy(g.exec);
+    mc.graphs.clear();
+    mc.seen.clear();
+    if (mc.d_cursor) cudaFree(mc.d_cursor);
+    if (mc.d_jobs) cudaFree(mc.d_jobs);
+    if (mc.d_log2m) cudaFree(mc.d_log2m);
+    if (mc.h_jobs) cudaFreeHost(mc.h_jobs);
+    if (mc.h_log2m) cudaFreeHost(mc.h_log2m);
+    if (mc.u0) cudaEventDestroy(mc.u0);
+    if (mc.u1) cudaEventDestroy(mc.u1);
+    if (mc.cap) cudaStreamDestroy(mc.cap);
+    mc.d_cursor = nullptr;
+    mc.d_jobs = nullptr;
+    mc.d_log2m = nullptr;
+    mc.h_jobs = nullptr;
+    mc.h_log2m = nullptr;
+    mc.u0 = mc.u1 = nullptr;
+    mc.cap = nullptr;
+}
+
+static int multi_init(MultiCtx& mc, int device, cudaStream_t s) {
+    mc.device = device;
+    mc.s = s;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_cursor, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_jobs, kMaxJobs * sizeof(hbk::UnionArgs));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_log2m, kMaxJobs * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&mc.h_jobs, kMaxJobs * sizeof(hbk::UnionArgs));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&mc.h_log2m, kMaxJobs * sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&mc.u0);
+    if (e == cudaSuccess) e = cudaEventCreate(&mc.u1);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mc.cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        mc.err = std::string("multi-instance setup: ") + cudaGetErrorString(e);
+        multi_free(mc);
+        return e == cudaErrorMemoryAllocation ? HB_ERR_OOM : HB_ERR_CUDA;
+    }
+    mc.grid = hbk::jobs_grid(device);
+    return HB_OK;
+}
+
+// The launches of one step on stream x (the handles' plans are final).
+static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& plans, MultiCtx& mc,
+                         cudaStream_t x, bool external, uint32_t* njobs) {
+    auto rec = [&](cudaEvent_t e) {
+        return external ? cudaEventRecordWithFlags(e, x, cudaEventRecordExternal) : cudaEventRecord(e, x);
+    };
+    int r;
+    for (size_t j = 0; j < hs.size(); j++)
+        if ((r = enqueue_pre(hs[j], plans[j].a, plans[j].first_systolic, x, external))) return r;
+    uint32_t J = 0;
+    for (size_t j = 0; j < hs.size(); j++) {
+        hb_handle* h = hs[j];
+        if (!h->n_tiles || !job_kernel_log2m(h->log2m) || plans[j].a.far_tma) continue;
+        mc.h_jobs[J] = plans[j].a;
+        mc.h_log2m[J] = h->log2m;
+        J++;
+    }
+    *njobs = J;
+    if (J) {
+        cudaError_t e = cudaMemcpyAsync(mc.d_jobs, mc.h_jobs, J * sizeof(hbk::UnionArgs),
+                                        cudaMemcpyHostToDevice, x);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(mc.d_log2m, mc.h_log2m, J * sizeof(int), cudaMemcpyHostToDevice, x);
+        if (e == cudaSuccess) e = cudaMemsetAsync(mc.d_cursor, 0, sizeof(unsigned long long), x);
+        if (e != cudaSuccess) {
+            mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
+            return HB_ERR_CUDA;
+        }
+    }
+    if (cudaError_t e = rec(mc.u0); e != cudaSuccess) {
+        mc.err = cudaGetErrorString(e);
+        return HB_ERR_CUDA;
+    }
+    for (size_t j = 0; j < hs.size(); j++) {
+        hb_handle* h = hs[j];
+        // handles outside the shared kernel launch their own window kernel
+        const bool own = h->n_tiles && (!job_kernel_log2m(h->log2m) || plans[j].a.far_tma);
+        if ((r = enqueue_union(h, plans[j].a, x, own))) return r;
+    }
+    if (J) {
+        const int e = hbk::launch_union_jobs(mc.d_jobs, mc.d_log2m, J, mc.d_cursor, mc.grid, x);
+        if (e) {
+            mc.err = std::string("k_union_jobs: ") + cudaGetErrorString((cudaError_t)e);
+            return HB_ERR_CUDA;
+        }
+    }
+    for (size_t j = 0; j < hs.size(); j++)
+        if ((r = enqueue_join(hs[j], x))) return r;
+    if (cudaError_t e = rec(mc.u1); e != cudaSuccess) {
+        mc.err = cudaGetErrorString(e);
+        return HB_ERR_CUDA;
+    }
+    for (size_t j = 0; j < hs.size(); j++)
+        if ((r = enqueue_post(hs[j], plans[j].a, x, external))) return r;
+    return HB_OK;
+}
+
+// One iteration of every handle in hs (at most kMaxJobs of them, all on
+// mc.device).
+static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
+    if (hs.empty()) return HB_OK;
+    if (hs.size() > kMaxJobs) {
+        mc.err = "more than 64 instances in one step";
+        return HB_ERR_INVALID;
+    }
+    std::vector<IterPlan> plans(hs.size());
+    MultiCtx::Shape shape;
+    for (size_t j = 0; j < hs.size(); j++) {
+        iter_plan(hs[j], plans[j]);
+        plans[j].a.staged = 0;
+        shape.hs.push_back(hs[j]);
+        shape.keys.push_back(plans[j].key);
+    }
+    const uint64_t c0 = hbk::launch_count();
+    cudaGraphExec_t exec = nullptr;
+    if (mc.use_graphs) {
+        for (const auto& g : mc.graphs)
+            if (g.shape == shape) {
+                exec = g.exec;
+                hbk::count_launches((int64_t)g.launches);
+                break;
+            }
+        const bool again = std::find(mc.seen.begin(), mc.seen.end(), shape) != mc.seen.end();
+        if (!exec && again && mc.graphs.size() < kMaxMultiGraphs) {
+            // capture; a failed capture turns graphs off (they change no result)
+            uint32_t J = 0;
+            cudaError_t e = cudaStreamBeginCapture(mc.cap, cudaStreamCaptureModeThreadLocal);
+            int r = e == cudaSuccess ? multi_enqueue(hs, plans, mc, mc.cap, true, &J) : HB_ERR_CUDA;
+            cudaGraph_t graph = nullptr;
+            if (e == cudaSuccess) e = cudaStreamEndCapture(mc.cap, &graph);
+            const uint64_t launches = hbk::launch_count() - c0;
+            hbk::count_launches(-(int64_t)launches);
+            if (r == HB_OK && e == cudaSuccess && graph) {
+                cudaGraphExec_t x = nullptr;
+                if (cudaGraphInstantiate(&x, graph, 0) == cudaSuccess) {
+                    mc.graphs.push_back(MultiCtx::Graph{shape, x, launches});
+                    exec = x;
+                    hbk::count_launches((int64_t)launches);
+                }
+            }
+            if (graph) cudaGraphDestroy(graph);
+            if (!exec) {
+                cudaGetLastError();
+                mc.use_graphs = false;
+                for (hb_handle* h : hs) h->err.clear();
+                mc.err.clear();
+            }
+        } else if (!exec && !again) {
+            mc.seen.push_back(shape);
+        }
+    }
+    if (exec) {
+        cudaError_t e = cudaGraphLaunch(exec, mc.s);
+        if (e != cudaSuccess) {
+            mc.err = std::string("cudaGraphLaunch: ") + cudaGetErrorString(e);
+            return HB_ERR_CUDA;
+        }
+        mc.replays++;
+    } else {
+        uint32_t J = 0;
+        int r = multi_enqueue(hs, plans, mc, mc.s, false, &J);
+        if (r) {
+            if (mc.err.empty())
+                for (hb_handle* h : hs)
+                    if (!h->err.empty()) mc.err = h->err;
+            return r;
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(mc.s);
+    if (e != cudaSuccess) {
+        mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
+        return HB_ERR_CUDA;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, mc.u0, mc.u1);
+    mc.union_ms += ms;
+    mc.steps++;
+    for (size_t j = 0; j < hs.size(); j++) {
+        int r = iter_finish(hs[j], plans[j], exec != nullptr, ms, nullptr);
+        if (r) {
+            mc.err = hs[j]->err;
+            return r;
+        }
+    }
     return HB_OK;
 }
 
@@ -1116,6 +1435,53 @@ int check_len(const hb_handle* h, size_t len) {
 
 }  // namespace
 
+struct hb_multi {
+    MultiCtx mc;
+};
+
+int hb_multi_create(int device, void* stream, hb_multi** out, std::string& err) {
+    hb_multi* m = new hb_multi();
+    // a server's set of handles changes as jobs come and go, and a captured
+    // graph holds the buffers of the handles it was captured with: no graphs
+    m->mc.use_graphs = false;
+    int r = multi_init(m->mc, device, (cudaStream_t)stream);
+    if (r) {
+        err = m->mc.err;
+        delete m;
+        return r;
+    }
+    *out = m;
+    return HB_OK;
+}
+
+void hb_multi_destroy(hb_multi* m) {
+    if (!m) return;
+    multi_free(m->mc);
+    delete m;
+}
+
+int hb_multi_start(hb_handle* h) {
+    h->tuner.fixed = 0;  // the shared union kernel has one configuration
+    HB_CUDA(h, cudaSetDevice(h->device));
+    return do_init(h);
+}
+
+int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err) {
+    std::vector<hb_handle*> v(hs, hs + count);
+    int r = multi_iterate(v, m->mc);
+    if (r) err = m->mc.err;
+    return r;
+}
+
+bool hb_multi_done(const hb_handle* h) {
+    return h->n == 0 || (h->iteration > 0 && (h->modified_counters == 0 || h->iteration >= h->n));
+}
+
+uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays) {
+    if (replays) *replays = m->mc.replays;
+    return m->mc.steps;
+}
+
 extern "C" {
 
 void hb_options_default(hb_options* o) {
@@ -1144,8 +1510,6 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
 struct hb_batch {
     struct Group {
         hb_handle* h = nullptr;
-        cudaStream_t stream = nullptr;
-        bool own_stream = false;
     };
     struct Member {
         uint32_t group = 0, inst = 0;
@@ -1155,15 +1519,19 @@ struct hb_batch {
     std::vector<Member> members;
     int device = 0;
     bool ran = false;
+    // every group's launches run on this stream, one step for all groups
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    MultiCtx mc;
 };
 
 static void batch_free(hb_batch* b) {
     if (!b) return;
     cudaSetDevice(b->device);
-    for (auto& g : b->groups) {
+    multi_free(b->mc);
+    for (auto& g : b->groups)
         if (g.h) hb_destroy(g.h);
-        if (g.own_stream && g.stream) cudaStreamDestroy(g.stream);
-    }
+    if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
 
@@ -1198,6 +1566,16 @@ int hb_batch_create(const hb_graph_view* graphs, uint32_t count, const int32_t* 
         cudaGetLastError();
         return set_err(nullptr, HB_ERR_NO_DEVICE, "no CUDA device available (this library has no CPU path)");
     }
+    if (o.stream) {
+        b->stream = (cudaStream_t)o.stream;
+    } else {
+        ce = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (ce != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(nullptr, HB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+        }
+        b->own_stream = true;
+    }
     for (auto& kv : by_log2m) {
         const std::vector<uint32_t>& idx = kv.second;
         // the disjoint union: instance k's nodes start at inst[k]
@@ -1229,23 +1607,15 @@ int hb_batch_create(const hb_graph_view* graphs, uint32_t count, const int32_t* 
         off[n] = m;
         hb_graph_view uv{n, m, off.data(), succ.data()};
         hb_batch::Group g;
-        if (o.stream) {
-            g.stream = (cudaStream_t)o.stream;
-        } else {
-            ce = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
-            if (ce != cudaSuccess) {
-                cudaGetLastError();
-                return set_err(nullptr, HB_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
-            }
-            g.own_stream = true;
-        }
         hb_options go = o;
         go.log2m = kv.first;
-        go.stream = g.stream;
+        go.stream = b->stream;
         go.num_elements = 0;
         b->groups.push_back(g);
         int r = create_impl(&uv, nullptr, &go, &inst, &b->groups.back().h);
         if (r) return r;
+        // the shared union kernel has one configuration (no variant tuning)
+        b->groups.back().h->tuner.fixed = 0;
         for (size_t k = 0; k < idx.size(); k++) {
             hb_batch::Member& mb = b->members[idx[k]];
             mb.group = (uint32_t)(b->groups.size() - 1);
@@ -1260,21 +1630,34 @@ int hb_batch_create(const hb_graph_view* graphs, uint32_t count, const int32_t* 
 
 void hb_batch_destroy(hb_batch* b) { batch_free(b); }
 
+// All groups advance together: one step runs one iteration of every group
+// whose instances are not all done, with one union launch for all of them
+// (multi_iterate). A group stops after an iteration that modified no counter
+// (every instance done, HB:559-570) or after num_nodes iterations (HB:541).
 int hb_batch_run_until_done(hb_batch* b) {
     if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
-    // groups run side by side, each on its own stream
-    std::vector<int> rc(b->groups.size(), HB_OK);
-    std::vector<std::string> msg(b->groups.size());
-    std::vector<std::thread> th;
-    for (size_t gi = 0; gi < b->groups.size(); gi++)
-        th.emplace_back([&, gi] {
-            cudaSetDevice(b->device);
-            rc[gi] = hb_run_until_done(b->groups[gi].h);
-            if (rc[gi]) msg[gi] = b->groups[gi].h->err;
-        });
-    for (auto& x : th) x.join();
-    for (size_t gi = 0; gi < b->groups.size(); gi++)
-        if (rc[gi]) return set_err(nullptr, rc[gi], msg[gi]);
+    cudaError_t ce = cudaSetDevice(b->device);
+    if (ce != cudaSuccess) return set_err(nullptr, HB_ERR_CUDA, cudaGetErrorString(ce));
+    if (!b->mc.d_jobs) {
+        int r = multi_init(b->mc, b->device, b->stream);
+        if (r) return set_err(nullptr, r, b->mc.err);
+    }
+    std::vector<hb_handle*> running;
+    for (auto& g : b->groups) {
+        int r = do_init(g.h);
+        if (r) return set_err(nullptr, r, g.h->err);
+        if (g.h->n) running.push_back(g.h);
+    }
+    b->mc.steps = b->mc.replays = 0;
+    b->mc.union_ms = 0.0;
+    while (!running.empty()) {
+        int r = multi_iterate(running, b->mc);
+        if (r) return set_err(nullptr, r, b->mc.err);
+        std::vector<hb_handle*> still;
+        for (hb_handle* h : running)
+            if (h->modified_counters != 0 && h->iteration < h->n) still.push_back(h);
+        running.swap(still);
+    }
     b->ran = true;
     return HB_OK;
 }
@@ -1376,14 +1759,8 @@ int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_ar
 
 int hb_batch_graph_replays(const hb_batch* b, uint64_t* replayed, uint64_t* iterations) {
     if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
-    uint64_t r = 0, it = 0;
-    for (const auto& g : b->groups)
-        for (const auto& s : g.h->stats) {
-            r += s.from_graph ? 1 : 0;
-            it += 1;
-        }
-    if (replayed) *replayed = r;
-    if (iterations) *iterations = it;
+    if (replayed) *replayed = b->mc.replays;
+    if (iterations) *iterations = b->mc.steps;
     return HB_OK;
 }
 
@@ -1722,6 +2099,21 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
                 return fail(r);
             if ((r = dalloc(hp, &h->d_inst_mod, ni))) return fail(r);
             if ((r = dalloc(hp, &h->d_inst_nf, ni))) return fail(r);
+            // the chunks of each instance, for the queue of running instances
+            if (h->n_chunks && ni && h->n_chunks < (1ull << 32)) {
+                if ((r = dalloc(hp, &h->d_inst_chunk, ni + 1))) return fail(r);
+                if ((r = dalloc(hp, &h->d_queue, h->n_chunks))) return fail(r);
+                if ((r = dalloc(hp, &h->d_queue_len, 1))) return fail(r);
+                if ((r = dalloc(hp, &h->d_q_cnt, ni + 1))) return fail(r);
+                if ((r = dalloc(hp, &h->d_q_at, ni + 1))) return fail(r);
+                h->q_scratch_len = hbk::scan_scratch_len(ni + 1);
+                if ((r = dalloc(hp, &h->d_q_scratch, h->q_scratch_len))) return fail(r);
+                if ((r = cuda_err(hp, (cudaError_t)hbk::launch_inst_first_chunk(
+                                          h->d_chunks, h->n_chunks, h->d_inst_start, (uint32_t)ni,
+                                          h->d_inst_chunk, h->stream),
+                                  "k_inst_first_chunk")))
+                    return fail(r);
+            }
         }
         // renumbering; the same pass counts in-degrees without self-loops and,
         // with a transpose to build, each node's self-loops (its row lengths
@@ -1797,6 +2189,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
     trace.mark("state arrays");
     h->grid_tile = hbk::tile_grid(h->log2m, h->device, 0);
     h->grid_tile_occ = hbk::tile_grid(h->log2m, h->device, 1);
+    h->grid_tile_two = hbk::tile_grid(h->log2m, h->device, 2);
     h->grid_staged = hbk::staged_grid(h->log2m, h->device, 0);
     h->grid_staged_occ = hbk::staged_grid(h->log2m, h->device, 1);
     {
@@ -1804,6 +2197,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         const uint64_t need = (h->n_chunks + 7) / 8 + 1;
         if ((uint64_t)h->grid_tile > need) h->grid_tile = (int)need;
         if ((uint64_t)h->grid_tile_occ > need) h->grid_tile_occ = (int)need;
+        if ((uint64_t)h->grid_tile_two > need) h->grid_tile_two = (int)need;
         if ((uint64_t)h->grid_staged > need) h->grid_staged = (int)need;
         if ((uint64_t)h->grid_staged_occ > need) h->grid_staged_occ = (int)need;
     }

@@ -81,6 +81,10 @@ struct UnionArgs {
     const uint32_t* medium_list;
     const uint64_t* list_counts;
     const uint2* chunks;      // {first node, count | medium << 31}, in node order
+    // batches, standard iterations: the chunks of the running instances
+    // (indices into chunks) and their number (device word); null otherwise
+    const uint32_t* queue;
+    const uint32_t* queue_len;
     const uint4* items;       // staged kernel: {first node, count | medium << 31, first arc, arcs}
     uint32_t staged;          // 1: standard iteration on the staged kernel (k_union_staged)
     int gather_all;           // merge every successor (nearly all changed before)
@@ -152,6 +156,21 @@ int tile_grid(int log2m, int device, int occ);
 // standard iterations on the staged window kernel (items table; m < 2^32)
 int launch_union_staged(int log2m, const UnionArgs& a, int grid, void* stream);
 int staged_grid(int log2m, int device, int occ);
+// the window work of several handles in one launch (log2m 4, 6 or 8 each;
+// jobs and log2m in device memory; at most 64 jobs)
+int launch_union_jobs(const UnionArgs* jobs, const int* log2m, uint32_t njobs,
+                      unsigned long long* cursor, int grid, void* stream);
+int jobs_grid(int device);
+// batches: queue = the chunks of the running instances (modified count of
+// the previous iteration nonzero, or every instance when `all`), queue_len its
+// length; cnt and at hold count + 1 words
+int launch_inst_queue(const uint32_t* inst_chunk, const unsigned long long* inst_mod, uint32_t count,
+                      int all, uint32_t n_chunks, unsigned long long* cnt, uint64_t* at,
+                      unsigned long long* scratch, uint64_t scratch_len, uint32_t* queue,
+                      uint32_t* queue_len, void* stream);
+// inst_chunk[i] = the first chunk of instance i (count + 1 words; start has count + 1)
+int launch_inst_first_chunk(const uint2* chunks, uint64_t n_chunks, const uint64_t* start,
+                            uint32_t count, uint32_t* inst_chunk, void* stream);
 // items[k] = {first, count | medium << 31, off[first], arcs of the chunk}
 int launch_chunk_items(const uint2* chunks, uint64_t n_chunks, const uint64_t* off, uint4* items,
                        void* stream);
@@ -218,3 +237,21 @@ uint64_t launch_count();
 void count_launches(int64_t delta);
 
 }  // namespace hbk
+
+// ---------------------------------------------------------------------------
+// Several handles advanced together (hb_engine.cpp; used by the job server):
+// each step runs one iteration of every handle given, with one shared union
+// launch. Handles must be on the context's device and idle.
+// ---------------------------------------------------------------------------
+struct hb_multi;
+int hb_multi_create(int device, void* stream, hb_multi** out, std::string& err);
+void hb_multi_destroy(hb_multi* m);
+// hb_init of a handle that will be stepped (its own stream, synchronous)
+int hb_multi_start(hb_handle* h);
+// one iteration of each of the count handles (count <= 64)
+int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err);
+// the handle's run is over: its last iteration modified no counter, or it
+// ran num_nodes iterations (the stop rules of run_until_done, HB:541, HB:559-570)
+bool hb_multi_done(const hb_handle* h);
+uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays);
+

@@ -290,12 +290,13 @@ __device__ __forceinline__ void filtered_gather(const UnionArgs& a, uint32_t v, 
 // (< e1) of node v: all of them, or (filter) only the non-loop ones modified
 // in the previous iteration; the first `skip` far ones that qualify are left
 // out (they arrive by TMA). PIPE counter loads stay in flight per lane.
-template <int LOG2M>
+// PIPEX: counter loads in flight per lane (0: pipe_depth)
+template <int LOG2M, int PIPEX = 0>
 __device__ __forceinline__ void gather_rolling(const UnionArgs& a, uint32_t v, int c, uint64_t e0,
                                                uint64_t e1, uint32_t stride, bool filter,
                                                uint32_t (&acc)[Geo<LOG2M>::NW], int skip) {
     using Gm = Geo<LOG2M>;
-    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIPE = pipe_depth<NW>();
+    constexpr int NW = Gm::NW, REGS = Gm::CHUNK_REGS, PIPE = PIPEX ? PIPEX : pipe_depth<NW>();
     auto wanted = [&](uint32_t s) {
         bool w = !filter || (s != v && test_bit(a.curr_mod, s));
         if (skip > 0 && w && is_far(s, v, a.far_rows)) {
@@ -518,7 +519,7 @@ __device__ __forceinline__ bool differs_from(const uint8_t* __restrict__ base, u
 // One warp-step over up to 32/TB nodes: the consecutive nodes [b, e), or
 // list[b .. e) when a list is given. Scan, copy or nothing; sets the modified
 // bits and counts scanned nodes, their arcs and the changed counters.
-template <int LOG2M, int TB, bool FAR>
+template <int LOG2M, int TB, bool FAR, int PIPEX = 0>
 __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __restrict__ list,
                                           uint32_t b, uint32_t e, uint32_t& modc, uint32_t& scanned,
                                           uint32_t& sarcs, uint32_t& vis, double& nf, FarState& fs) {
@@ -578,7 +579,7 @@ __device__ __forceinline__ void run_nodes(const UnionArgs& a, const uint32_t* __
 #pragma unroll
                 for (int k = 0; k < NW; k++) acc[k] = 0u;
             }
-            gather_rolling<LOG2M>(a, v, c, s0 + p, s1, PB, filter, acc, nfar);
+            gather_rolling<LOG2M, PIPEX>(a, v, c, s0 + p, s1, PB, filter, acc, nfar);
             if (nfar > 0) {
                 if (mbar_wait(far_barrier(), fs.bits & 1u, a.mbar_polls)) {
                     merge_far<LOG2M>(far_region<LOG2M>(lane), c, nfar, acc);
@@ -669,7 +670,10 @@ struct WorkItems {
 template <int NPW_L, int NPW_M>
 __device__ __forceinline__ WorkItems work_items(const UnionArgs& a) {
     WorkItems w{};
-    if (a.light_list) {
+    if (a.queue) {
+        // a batch's standard iteration: the chunks of its running instances
+        w.n_work = *a.queue_len;
+    } else if (a.light_list) {
         const uint64_t c = *a.list_counts;
         w.n_light = (uint32_t)c;
         w.n_medium = (uint32_t)(c >> 32);
@@ -685,6 +689,7 @@ template <int NPW_L, int NPW_M>
 __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
                                          uint32_t k) {
     if (k >= w.n_work) return make_uint2(0u, 0u);
+    if (a.queue) return __ldg(a.chunks + __ldg(a.queue + k));
     if (!a.light_list) return __ldg(a.chunks + k);
     if (k < w.light_items) {
         const uint32_t f = (uint32_t)(k * NPW_L);
@@ -698,7 +703,9 @@ __device__ __forceinline__ uint2 item_at(const UnionArgs& a, const WorkItems& w,
 // loads on the web-like and R-MAT workloads)
 // MINB: resident blocks per SM the registers are sized for (3: 80 registers
 // a thread, 4: 64; the autotuner picks one per graph)
-template <int LOG2M, bool FAR, int MINB>
+// PIPEX: counter loads in flight per light lane (0: pipe_depth; the 2-block
+// build has the registers for 2 at 16 words per lane)
+template <int LOG2M, bool FAR, int MINB, int PIPEX = 0>
 __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
@@ -737,7 +744,7 @@ __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constan
         if (d.y >> 31)
             run_medium<LOG2M, TB_MED, FAR>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         else
-            run_nodes<LOG2M, G, FAR>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
+            run_nodes<LOG2M, G, FAR, PIPEX>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
         // the item's neighbourhood-function part: fixed lanes, fixed order
         nf = warp_sum_f64(nf);
         if (lane == 0) a.nf_items[k - 1] = nf;
@@ -759,6 +766,152 @@ __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constan
     }
     if (__any_sync(0xffffffffu, (fs.bits & 2u) != 0) && lane == 0)
         atomicAdd(&a.partials[a.acc_slot].timeouts, 1ull);
+}
+
+// ---------------------------------------------------------------------------
+// Several HyperBall instances in one launch: the window work of up to
+// MAX_JOBS handles (the log2m groups of a batch, the running jobs of a
+// server), each with its own arguments and log2m in {4, 6, 8}, drained from
+// one cursor. A block first turns the jobs' work-item counts into a prefix
+// in shared memory; a warp maps each item it takes to its job and runs it
+// exactly as k_union_window would (same items, lanes and order, so every
+// counter and per-item neighbourhood-function part is that job's alone).
+// Integer totals go to each job's partial slot when the warp moves to
+// another job.
+// ---------------------------------------------------------------------------
+constexpr int MAX_JOBS = 64;
+
+template <int LOG2M>
+__device__ __forceinline__ uint32_t job_work(const UnionArgs& a) {
+    constexpr int G = Geo<LOG2M>::CHUNKS, TB_MED = team_lanes<LOG2M>();
+    return work_items<32 / G, 32 / TB_MED>(a).n_work;
+}
+
+template <int LOG2M>
+__device__ __forceinline__ void job_item(const UnionArgs& a, uint32_t k, uint32_t& modc,
+                                         uint32_t& scanned, uint32_t& sarcs, uint32_t& vis) {
+    using Gm = Geo<LOG2M>;
+    constexpr int G = Gm::CHUNKS;
+    constexpr int TB_MED = team_lanes<LOG2M>();
+    constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
+    const WorkItems wi = work_items<NPW_L, NPW_M>(a);
+    const uint2 d = item_at<NPW_L, NPW_M>(a, wi, k);
+    const uint32_t cnt = d.y & 0x7fffffffu;
+    FarState fs{0u};
+    double nf = 0.0;
+    if (d.y >> 31)
+        run_medium<LOG2M, TB_MED, false>(a, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
+    else
+        run_nodes<LOG2M, G, false>(a, a.light_list, d.x, d.x + cnt, modc, scanned, sarcs, vis, nf, fs);
+    nf = warp_sum_f64(nf);
+    if ((threadIdx.x & 31) == 0) a.nf_items[k] = nf;
+}
+
+__device__ __forceinline__ void flush_totals(const UnionArgs& a, uint32_t& modc, uint32_t& scanned,
+                                             uint32_t& sarcs, uint32_t& vis) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        modc += __shfl_xor_sync(0xffffffffu, modc, off);
+        scanned += __shfl_xor_sync(0xffffffffu, scanned, off);
+        sarcs += __shfl_xor_sync(0xffffffffu, sarcs, off);
+        vis += __shfl_xor_sync(0xffffffffu, vis, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        TilePartial* t = a.partials + a.acc_slot;
+        if (modc) atomicAdd(&t->mod, (unsigned long long)modc);
+        if (scanned) atomicAdd(&t->scanned, (unsigned long long)scanned);
+        if (sarcs) atomicAdd(&t->sarcs, (unsigned long long)sarcs);
+        if (vis) atomicAdd(&t->vis, (unsigned long long)vis);
+    }
+    modc = scanned = sarcs = vis = 0;
+}
+
+__global__ void __launch_bounds__(256, 2) k_union_jobs(const UnionArgs* __restrict__ jobs,
+                                                       const int* __restrict__ log2m, uint32_t njobs,
+                                                       unsigned long long* cursor) {
+    __shared__ uint32_t s_first[MAX_JOBS + 1];
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t j = 0; j < njobs; j++) {
+            s_first[j] = t;
+            const UnionArgs& a = jobs[j];
+            switch (log2m[j]) {
+                case 4: t += job_work<4>(a); break;
+                case 6: t += job_work<6>(a); break;
+                case 8: t += job_work<8>(a); break;
+                default: break;
+            }
+        }
+        s_first[njobs] = t;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint32_t total = s_first[njobs];
+    uint32_t modc = 0, scanned = 0, sarcs = 0, vis = 0;
+    uint32_t cur_job = 0xffffffffu;
+    for (;;) {
+        uint32_t w = 0;
+        if (lane == 0) w = (uint32_t)atomicAdd(cursor, 1ull);
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (w >= total) break;
+        uint32_t j = 0;
+        while (j + 1 < njobs && s_first[j + 1] <= w) j++;
+        if (j != cur_job) {
+            if (cur_job != 0xffffffffu) flush_totals(jobs[cur_job], modc, scanned, sarcs, vis);
+            cur_job = j;
+        }
+        const UnionArgs& a = jobs[j];
+        const uint32_t k = w - s_first[j];
+        switch (log2m[j]) {
+            case 4: job_item<4>(a, k, modc, scanned, sarcs, vis); break;
+            case 6: job_item<6>(a, k, modc, scanned, sarcs, vis); break;
+            case 8: job_item<8>(a, k, modc, scanned, sarcs, vis); break;
+            default: break;
+        }
+    }
+    if (cur_job != 0xffffffffu) flush_totals(jobs[cur_job], modc, scanned, sarcs, vis);
+}
+
+// batches: the chunks of the running instances, in chunk order. inst_chunk[i]
+// is instance i's first chunk (inst_chunk[count] = n_chunks); an instance
+// runs when its modified count of the previous iteration is nonzero (`all`:
+// every instance, the first iteration). One thread per chunk; `at` holds the
+// exclusive scan of the running instances' chunk counts (count + 1 words).
+__global__ void k_inst_chunk_counts(const uint32_t* __restrict__ inst_chunk,
+                                    const unsigned long long* __restrict__ inst_mod, uint32_t count,
+                                    int all, unsigned long long* __restrict__ cnt) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x)
+        cnt[i] = i < count && (all || inst_mod[i] != 0) ? inst_chunk[i + 1] - inst_chunk[i] : 0;
+}
+__global__ void k_inst_queue(const uint32_t* __restrict__ inst_chunk,
+                             const unsigned long long* __restrict__ inst_mod, uint32_t count, int all,
+                             const uint64_t* __restrict__ at, uint32_t n_chunks,
+                             uint32_t* __restrict__ queue, uint32_t* __restrict__ queue_len) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_chunks; k += gridDim.x * blockDim.x) {
+        // the instance of chunk k: the last i with inst_chunk[i] <= k
+        uint32_t lo = 0, hi = count;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (inst_chunk[mid] <= k) lo = mid;
+            else hi = mid;
+        }
+        if (all || inst_mod[lo] != 0) queue[at[lo] + (k - inst_chunk[lo])] = k;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *queue_len = (uint32_t)at[count];
+}
+// inst_chunk[i] = the first chunk whose first node is at or after start[i]
+__global__ void k_inst_first_chunk(const uint2* __restrict__ chunks, uint64_t n_chunks,
+                                   const uint64_t* __restrict__ start, uint32_t count,
+                                   uint32_t* __restrict__ inst_chunk) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x) {
+        uint64_t lo = 0, hi = n_chunks;
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if ((uint64_t)__ldg(&chunks[mid].x) < start[i]) lo = mid + 1;
+            else hi = mid;
+        }
+        inst_chunk[i] = (uint32_t)lo;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -822,13 +975,13 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // in shared memory) by the 32 lanes of the warp. d = {first, count | medium
 // << 31, first arc, arcs}. The successor array is padded to a multiple of 4
 // ids plus 8, so the last 16-byte copy stays inside it.
-template <int LOG2M>
+template <int LOG2M, bool IDS>
 __device__ __forceinline__ void stage_item(const UnionArgs& a, uint4 d, uint32_t buf, int lane) {
     using SG = StageGeo<LOG2M>;
     const uint32_t first = d.x, cnt = d.y & 0x7fffffffu;
     // ids: 16-byte units from the aligned word at or below the first arc
     const uint32_t base = d.z & ~3u;
-    const uint32_t want = min(d.w, (uint32_t)STAGE_IDS);
+    const uint32_t want = IDS ? min(d.w, (uint32_t)STAGE_IDS) : 0u;
     const uint32_t units = (d.z + want - base + 3) >> 2;
     for (uint32_t u = lane; u < units; u += 32)
         cp_async16(buf + SG::OFF_IDS + 16 * u, a.succ + base + 4 * u);
@@ -1012,9 +1165,9 @@ __device__ __forceinline__ void staged_nodes(const UnionArgs& a, uint32_t buf, i
     }
 }
 
-// PIPE_L: counter loads in flight per lane of a light node (1 or 2 at
-// 16 words per lane; the narrower chunks of log2m 4 and 5 take more)
-template <int LOG2M, int MINB, int PIPE_L>
+// PIPE_L: counter loads in flight per lane of a light node (pipe_depth);
+// IDS: successor ids staged too (else read from global memory in the loop)
+template <int LOG2M, int MINB, int PIPE_L, bool IDS>
 __global__ void __launch_bounds__(256, MINB) k_union_staged(const __grid_constant__ UnionArgs a) {
     using Gm = Geo<LOG2M>;
     using SG = StageGeo<LOG2M>;
@@ -1039,14 +1192,14 @@ __global__ void __launch_bounds__(256, MINB) k_union_staged(const __grid_constan
     uint4 nxt = item(k_nxt);
     {
         const uint4 cur = item(k_cur);
-        if (k_cur < n_work) stage_item<LOG2M>(a, cur, bufs, lane);
+        if (k_cur < n_work) stage_item<LOG2M, IDS>(a, cur, bufs, lane);
         cp_async_commit();
     }
     for (uint32_t it = 0; k_cur < n_work; it++) {
         const uint32_t k_after = __shfl_sync(0xffffffffu, (uint32_t)atom, 0);
         if (lane == 0 && k_after < n_work) atom = atomicAdd(a.cursor, 1ull);
         const uint4 after = item(k_after);
-        if (k_nxt < n_work) stage_item<LOG2M>(a, nxt, bufs + ((it + 1) & 1) * SG::BUF, lane);
+        if (k_nxt < n_work) stage_item<LOG2M, IDS>(a, nxt, bufs + ((it + 1) & 1) * SG::BUF, lane);
         cp_async_commit();
         cp_async_wait<1>();
         __syncwarp();
@@ -1907,16 +2060,16 @@ int encode_far_map(int log2m, const uint8_t* counters, uint64_t n, CUtensorMap* 
 #undef CALL
 }
 
-template <int LOG2M, bool FAR, int MINB>
+template <int LOG2M, bool FAR, int MINB, int PIPEX = 0>
 static int tile_launch(const UnionArgs& a, int grid, cudaStream_t s) {
     constexpr int smem = far_bytes<LOG2M, FAR>();
     if constexpr (smem > 48 * 1024) {
         static const cudaError_t attr = cudaFuncSetAttribute(
-            k_union_window<LOG2M, FAR, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            k_union_window<LOG2M, FAR, MINB, PIPEX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (attr != cudaSuccess) return (int)attr;
     }
     ++t_launches;
-    k_union_window<LOG2M, FAR, MINB><<<grid, 256, smem, s>>>(a);
+    k_union_window<LOG2M, FAR, MINB, PIPEX><<<grid, 256, smem, s>>>(a);
     return (int)cudaGetLastError();
 }
 
@@ -1924,49 +2077,47 @@ template <int LOG2M>
 static int tile_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     if constexpr (FarGeo<LOG2M>::ON)
         if (a.far_tma) return tile_launch<LOG2M, true, 3>(a, grid, s);
+    if (a.occ == 2) return tile_launch<LOG2M, false, 2, Geo<LOG2M>::NW >= 16 ? 2 : 0>(a, grid, s);
     if (a.occ) return tile_launch<LOG2M, false, 4>(a, grid, s);
     return tile_launch<LOG2M, false, 3>(a, grid, s);
 }
 
-template <int LOG2M, int MINB, int PIPE_L>
+template <int LOG2M, int MINB, bool IDS>
 static int staged_launch(const UnionArgs& a, int grid, cudaStream_t s) {
     constexpr int smem = staged_smem_bytes<LOG2M>();
+    constexpr int PIPE_L = pipe_depth<Geo<LOG2M>::NW>();
     if constexpr (smem > 48 * 1024) {
         static const cudaError_t attr = cudaFuncSetAttribute(
-            k_union_staged<LOG2M, MINB, PIPE_L>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            k_union_staged<LOG2M, MINB, PIPE_L, IDS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (attr != cudaSuccess) return (int)attr;
     }
     ++t_launches;
-    k_union_staged<LOG2M, MINB, PIPE_L><<<grid, 256, smem, s>>>(a);
+    k_union_staged<LOG2M, MINB, PIPE_L, IDS><<<grid, 256, smem, s>>>(a);
     return (int)cudaGetLastError();
 }
 
-// deep: PIPE_L 2 at 16 words per lane (log2m >= 6), else the narrow pipe
-template <int LOG2M>
-constexpr int staged_pipe(bool deep) {
-    return Geo<LOG2M>::NW >= 16 ? (deep ? 2 : 1) : pipe_depth<Geo<LOG2M>::NW>();
-}
-
+// a.staged: 1 = ids staged, 2 = ids from global memory
 template <int LOG2M>
 static int staged_impl(const UnionArgs& a, int grid, cudaStream_t s) {
     if (a.staged == 2) {
-        if (a.occ) return staged_launch<LOG2M, 4, staged_pipe<LOG2M>(true)>(a, grid, s);
-        return staged_launch<LOG2M, 3, staged_pipe<LOG2M>(true)>(a, grid, s);
+        if (a.occ) return staged_launch<LOG2M, 4, false>(a, grid, s);
+        return staged_launch<LOG2M, 3, false>(a, grid, s);
     }
-    if (a.occ) return staged_launch<LOG2M, 4, staged_pipe<LOG2M>(false)>(a, grid, s);
-    return staged_launch<LOG2M, 3, staged_pipe<LOG2M>(false)>(a, grid, s);
+    if (a.occ) return staged_launch<LOG2M, 4, true>(a, grid, s);
+    return staged_launch<LOG2M, 3, true>(a, grid, s);
 }
 
 template <int LOG2M>
 static int staged_grid_impl(int device, int occ) {
     int per_sm = 1;
     constexpr int smem = staged_smem_bytes<LOG2M>();
+    constexpr int PIPE_L = pipe_depth<Geo<LOG2M>::NW>();
     if (occ)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_union_staged<LOG2M, 4, staged_pipe<LOG2M>(false)>, 256, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_staged<LOG2M, 4, PIPE_L, true>,
+                                                      256, smem);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_union_staged<LOG2M, 3, staged_pipe<LOG2M>(false)>, 256, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_staged<LOG2M, 3, PIPE_L, true>,
+                                                      256, smem);
     return std::max(1, per_sm) * num_sms(device);
 }
 
@@ -1983,7 +2134,10 @@ static int heavy_impl(const UnionArgs& a, int grid, cudaStream_t s) {
 template <int LOG2M>
 static int tile_grid_impl(int device, int occ) {
     int per_sm = 1;
-    if (occ)
+    if (occ == 2)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_union_window<LOG2M, false, 2, Geo<LOG2M>::NW >= 16 ? 2 : 0>, 256, 0);
+    else if (occ)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false, 4>, 256, 0);
     else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_window<LOG2M, false, 3>, 256, 0);
@@ -2108,6 +2262,46 @@ int staged_grid(int log2m, int device, int occ) {
 #define CALL(L) staged_grid_impl<L>(device, occ)
     HB_DISPATCH_LOG2M(log2m, CALL)
 #undef CALL
+}
+
+int launch_union_jobs(const UnionArgs* jobs, const int* log2m, uint32_t njobs,
+                      unsigned long long* cursor, int grid, void* stream) {
+    if (njobs > (uint32_t)MAX_JOBS) return (int)cudaErrorInvalidValue;
+    ++t_launches;
+    k_union_jobs<<<grid, 256, 0, (cudaStream_t)stream>>>(jobs, log2m, njobs, cursor);
+    return (int)cudaGetLastError();
+}
+
+int jobs_grid(int device) {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_jobs, 256, 0);
+    return std::max(1, per_sm) * num_sms(device);
+}
+
+int launch_inst_queue(const uint32_t* inst_chunk, const unsigned long long* inst_mod, uint32_t count,
+                      int all, uint32_t n_chunks, unsigned long long* cnt, uint64_t* at,
+                      unsigned long long* scratch, uint64_t scratch_len, uint32_t* queue,
+                      uint32_t* queue_len, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const int g1 = (int)std::min<uint64_t>((count + 256) / 256, 4096);
+    ++t_launches;
+    k_inst_chunk_counts<<<g1, 256, 0, s>>>(inst_chunk, inst_mod, count, all, cnt);
+    int e = (int)cudaGetLastError();
+    if (e) return e;
+    e = launch_exclusive_scan_u64(cnt, at, count + 1, scratch, scratch_len, stream);
+    if (e) return e;
+    const int g2 = (int)std::min<uint64_t>((n_chunks + 255) / 256 + 1, 8192);
+    ++t_launches;
+    k_inst_queue<<<g2, 256, 0, s>>>(inst_chunk, inst_mod, count, all, at, n_chunks, queue, queue_len);
+    return (int)cudaGetLastError();
+}
+
+int launch_inst_first_chunk(const uint2* chunks, uint64_t n_chunks, const uint64_t* start,
+                            uint32_t count, uint32_t* inst_chunk, void* stream) {
+    const int grid = (int)std::min<uint64_t>((count + 256) / 256, 4096);
+    ++t_launches;
+    k_inst_first_chunk<<<grid, 256, 0, (cudaStream_t)stream>>>(chunks, n_chunks, start, count, inst_chunk);
+    return (int)cudaGetLastError();
 }
 
 int launch_chunk_items(const uint2* chunks, uint64_t n_chunks, const uint64_t* off, uint4* items,

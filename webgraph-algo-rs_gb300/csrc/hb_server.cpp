@@ -1,15 +1,23 @@
-// HyperBall job server: continuous admission of independent HyperBall jobs
-// against a device-memory budget (no reference counterpart; each job returns
+// HyperBall job server: continuous batching of independent HyperBall jobs
+// under a device-memory budget (no reference counterpart; each job returns
 // what HyperBallBuilder::build + run_until_done returns for its graph alone).
 //
-// Jobs wait in a FIFO queue. A scheduler thread admits the head job as soon as
-// a slot is free (at most max_active jobs on the device) and its estimated
-// device footprint fits the budget next to the jobs already running. Each
-// admitted job runs on its own CUDA stream from its own host thread, so the
-// iterations of all running jobs overlap on the device; when a job finishes,
-// its results are copied to the host, its device memory is released and the
-// scheduler admits the next jobs. Latency is measured from submission to the
-// moment the results are on the host.
+// Jobs wait in a FIFO queue. The scheduler admits the head job as soon as a
+// slot is free (at most max_active jobs past admission) and its estimated
+// device footprint fits the budget next to the admitted jobs. Admitted jobs
+// go through three stages, each with its own host thread(s):
+//   creation  (two threads)  hb_create on the job's own stream: CSR upload,
+//                            partition, renumbering, transpose;
+//   stepping  (one thread)   every running job advances one iteration per
+//                            step, and the union work of all of them runs as
+//                            one kernel launch (hb_multi_step); a job created
+//                            meanwhile joins at the next step, a finished one
+//                            leaves after the step that stopped it;
+//   results   (two threads)  neighbourhood function, sums and registers to
+//                            the host, handle destroyed, budget released.
+// So requests that arrive while others run are admitted as slots and memory
+// free up, and their iterations interleave in the shared kernel. Latency is
+// measured from submission to the moment the results are on the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,6 +41,8 @@ using Clock = std::chrono::steady_clock;
 
 struct Job {
     uint64_t id = 0;
+    hb_handle* h = nullptr;           // from creation to the results stage
+    cudaStream_t stream = nullptr;
     Csr graph;                // the copied graph (hb_server_submit)
     hb_graph_view borrowed{}; // the caller's graph (hb_server_submit_borrowed), else empty
     bool is_borrowed = false;
@@ -57,13 +67,20 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 struct hb_server {
     hb_server_options opts{};
     std::mutex mu;
-    std::condition_variable cv;        // scheduler wake-ups and job completions
-    std::deque<std::shared_ptr<Job>> queue;
+    std::condition_variable cv;        // every stage's wake-ups and job completions
+    std::deque<std::shared_ptr<Job>> queue;      // submitted, waiting for admission
+    std::deque<std::shared_ptr<Job>> to_create;  // admitted
+    std::deque<std::shared_ptr<Job>> ready;      // created, joining the next step
+    std::deque<std::shared_ptr<Job>> to_finish;  // stopped (or failed)
     std::map<uint64_t, std::shared_ptr<Job>> jobs;
-    std::thread scheduler;
+    std::thread scheduler, stepper;
+    std::vector<std::thread> creators, finishers;
+    hb_multi* multi = nullptr;
+    cudaStream_t step_stream = nullptr;
     uint64_t next_id = 1, used = 0;
-    uint32_t active = 0;
-    bool stopping = false;
+    uint32_t active = 0;               // admitted and not finished
+    bool stopping = false;             // no more admissions
+    bool shutdown = false;             // stage threads exit
     std::string err;
 };
 
@@ -84,71 +101,10 @@ uint64_t hb_job_footprint(uint64_t num_nodes, uint64_t num_arcs, int log2m) {
     return 3 * csr + 2 * n * (1ull << log2m) + 64 * n + (64ull << 20);
 }
 
-static void run_job(hb_server* s, std::shared_ptr<Job> job) {
-    cudaStream_t stream = nullptr;
-    int r = HB_OK;
-    std::string msg;
-    hb_handle* h = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-        cudaGetLastError();
-        r = HB_ERR_NO_DEVICE;
-        msg = "no CUDA device available (this library has no CPU path)";
-    } else if (cudaSetDevice(s->opts.device) != cudaSuccess ||
-               cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) {
-        cudaGetLastError();
-        r = HB_ERR_CUDA;
-        msg = "cudaStreamCreate failed";
-    }
-    if (!r) {
-        hb_options o = job->opts;
-        o.stream = stream;
-        hb_graph_view v = job->is_borrowed ? job->borrowed
-                                           : hb_graph_view{job->graph.n, job->graph.m,
-                                                           job->graph.offsets.data(),
-                                                           job->graph.successors.data()};
-        r = hb_create(&v, nullptr, &o, &h);
-        if (r) msg = hb_global_last_error();
-    }
-    if (!r) {
-        r = hb_run_until_done(h);
-        if (r) msg = hb_last_error(h);
-    }
-    if (!r) {
-        job->iterations = hb_num_iterations(h);
-        for (uint64_t i = 0; i < job->iterations; i++) {
-            hb_iter_stats st{};
-            hb_get_iteration_stats(h, i, &st);
-            job->visited_arcs += st.visited_arcs;
-        }
-        const uint64_t n = job->graph.n;
-        if (job->iterations) {
-            size_t len = 0;
-            hb_get_neighborhood_function(h, nullptr, 0, &len);
-            job->nf.resize(len);
-            r = hb_get_neighborhood_function(h, job->nf.data(), len, &len);
-            if (!r && (job->opts.flags & HB_SUM_OF_DISTANCES)) {
-                job->sod.resize(n);
-                r = hb_get_sum_of_distances(h, job->sod.data(), n);
-            }
-            if (!r && (job->opts.flags & HB_SUM_OF_INVERSE_DISTANCES)) {
-                job->harm.resize(n);
-                r = hb_get_harmonic_centralities(h, job->harm.data(), n);
-            }
-        }
-        if (!r && s->opts.keep_registers) {
-            uint64_t cb = 0;
-            int rs = 0;
-            hb_counter_layout(h, &cb, &rs);
-            job->registers.resize(n * cb);
-            r = hb_get_registers(h, HB_CURRENT_STATE, job->registers.data(), job->registers.size());
-        }
-        if (r) msg = hb_last_error(h);
-    }
-    if (h) hb_destroy(h);
-    if (stream) cudaStreamDestroy(stream);
-    // the last touch of the server happens under its lock, so a shutdown
-    // waiting for active == 0 cannot free it under this thread
+// The end of a job (results on the host or a failure): bookkeeping under
+// the lock, so a shutdown waiting for active == 0 cannot free the server
+// under this thread.
+static void job_done(hb_server* s, const std::shared_ptr<Job>& job, int r, const std::string& msg) {
     std::lock_guard<std::mutex> lock(s->mu);
     job->finished = Clock::now();
     job->error = r;
@@ -158,6 +114,157 @@ static void run_job(hb_server* s, std::shared_ptr<Job> job) {
     s->used -= job->footprint;
     s->active--;
     s->cv.notify_all();
+}
+
+// creation stage: the job's handle on its own stream
+static void creator(hb_server* s) {
+    for (;;) {
+        std::shared_ptr<Job> job;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait(lock, [&] { return s->shutdown || !s->to_create.empty(); });
+            if (s->to_create.empty()) return;
+            job = s->to_create.front();
+            s->to_create.pop_front();
+        }
+        int r = HB_OK;
+        std::string msg;
+        if (!s->multi) {
+            r = HB_ERR_NO_DEVICE;
+            msg = "no CUDA device available (this library has no CPU path)";
+        } else if (cudaSetDevice(s->opts.device) != cudaSuccess ||
+                   cudaStreamCreateWithFlags(&job->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            r = HB_ERR_CUDA;
+            msg = "cudaStreamCreate failed";
+        }
+        if (!r) {
+            hb_options o = job->opts;
+            o.stream = job->stream;
+            hb_graph_view v = job->is_borrowed ? job->borrowed
+                                               : hb_graph_view{job->graph.n, job->graph.m,
+                                                               job->graph.offsets.data(),
+                                                               job->graph.successors.data()};
+            r = hb_create(&v, nullptr, &o, &job->h);
+            if (r) msg = hb_global_last_error();
+        }
+        if (!r) {
+            r = hb_multi_start(job->h);
+            if (r) msg = hb_last_error(job->h);
+        }
+        if (r) {
+            if (job->h) hb_destroy(job->h);
+            job->h = nullptr;
+            if (job->stream) cudaStreamDestroy(job->stream);
+            job->stream = nullptr;
+            job_done(s, job, r, msg);
+            continue;
+        }
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->ready.push_back(job);
+        s->cv.notify_all();
+    }
+}
+
+// stepping stage: one iteration of every running job per step, one shared
+// union launch
+static void stepper(hb_server* s) {
+    cudaSetDevice(s->opts.device);
+    std::vector<std::shared_ptr<Job>> running;
+    std::vector<hb_handle*> hs;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait(lock, [&] {
+                return !s->ready.empty() || !running.empty() || (s->shutdown && s->to_create.empty());
+            });
+            if (running.empty() && s->ready.empty() && s->shutdown) return;
+            // newly created jobs join at this step
+            while (!s->ready.empty() && running.size() < 64) {
+                std::shared_ptr<Job> j = s->ready.front();
+                s->ready.pop_front();
+                if (hb_multi_done(j->h))
+                    s->to_finish.push_back(j);  // no nodes: nothing to iterate
+                else
+                    running.push_back(j);
+            }
+            s->cv.notify_all();
+        }
+        if (running.empty()) continue;
+        hs.clear();
+        for (auto& j : running) hs.push_back(j->h);
+        std::string msg;
+        const int r = hb_multi_step(s->multi, hs.data(), (uint32_t)hs.size(), msg);
+        std::lock_guard<std::mutex> lock(s->mu);
+        std::vector<std::shared_ptr<Job>> still;
+        for (auto& j : running) {
+            if (r) {
+                j->error = r;
+                j->message = msg;
+                s->to_finish.push_back(j);
+            } else if (hb_multi_done(j->h)) {
+                s->to_finish.push_back(j);
+            } else {
+                still.push_back(j);
+            }
+        }
+        running.swap(still);
+        s->cv.notify_all();
+    }
+}
+
+// results stage
+static void finisher(hb_server* s) {
+    cudaSetDevice(s->opts.device);
+    for (;;) {
+        std::shared_ptr<Job> job;
+        {
+            std::unique_lock<std::mutex> lock(s->mu);
+            s->cv.wait(lock, [&] { return s->shutdown || !s->to_finish.empty(); });
+            if (s->to_finish.empty()) return;
+            job = s->to_finish.front();
+            s->to_finish.pop_front();
+        }
+        int r = job->error;
+        std::string msg = job->message;
+        hb_handle* h = job->h;
+        if (!r) {
+            job->iterations = hb_num_iterations(h);
+            for (uint64_t i = 0; i < job->iterations; i++) {
+                hb_iter_stats st{};
+                hb_get_iteration_stats(h, i, &st);
+                job->visited_arcs += st.visited_arcs;
+            }
+            const uint64_t n = job->graph.n;
+            if (job->iterations) {
+                size_t len = 0;
+                hb_get_neighborhood_function(h, nullptr, 0, &len);
+                job->nf.resize(len);
+                r = hb_get_neighborhood_function(h, job->nf.data(), len, &len);
+                if (!r && (job->opts.flags & HB_SUM_OF_DISTANCES)) {
+                    job->sod.resize(n);
+                    r = hb_get_sum_of_distances(h, job->sod.data(), n);
+                }
+                if (!r && (job->opts.flags & HB_SUM_OF_INVERSE_DISTANCES)) {
+                    job->harm.resize(n);
+                    r = hb_get_harmonic_centralities(h, job->harm.data(), n);
+                }
+            }
+            if (!r && s->opts.keep_registers) {
+                uint64_t cb = 0;
+                int rs = 0;
+                hb_counter_layout(h, &cb, &rs);
+                job->registers.resize(n * cb);
+                r = hb_get_registers(h, HB_CURRENT_STATE, job->registers.data(), job->registers.size());
+            }
+            if (r) msg = hb_last_error(h);
+        }
+        if (h) hb_destroy(h);
+        job->h = nullptr;
+        if (job->stream) cudaStreamDestroy(job->stream);
+        job->stream = nullptr;
+        job_done(s, job, r, msg);
+    }
 }
 
 static void schedule(hb_server* s) {
@@ -178,8 +285,9 @@ static void schedule(hb_server* s) {
             s->active++;
             job->state = HB_JOB_RUNNING;
             job->started = Clock::now();
-            std::thread(run_job, s, job).detach();
+            s->to_create.push_back(job);
         }
+        s->cv.notify_all();
     }
 }
 
@@ -203,10 +311,31 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
             return server_err(HB_ERR_INVALID, "hb_server_options.struct_size mismatch");
         o = *opts;
     }
-    if (o.max_active == 0) return server_err(HB_ERR_INVALID, "max_active must be at least 1");
+    if (o.max_active == 0 || o.max_active > 64)
+        return server_err(HB_ERR_INVALID, "max_active must be in [1, 64]");
     hb_server* s = new hb_server();
     s->opts = o;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && cudaSetDevice(o.device) == cudaSuccess) {
+        std::string err;
+        cudaError_t ce = cudaStreamCreateWithFlags(&s->step_stream, cudaStreamNonBlocking);
+        int r = ce == cudaSuccess ? hb_multi_create(o.device, s->step_stream, &s->multi, err) : HB_ERR_CUDA;
+        if (r) {
+            cudaGetLastError();
+            if (s->step_stream) cudaStreamDestroy(s->step_stream);
+            delete s;
+            return server_err(r, "server setup: " + (err.empty() ? std::string("cudaStreamCreate failed") : err));
+        }
+    } else {
+        // no device: every job fails at creation with HB_ERR_NO_DEVICE
+        cudaGetLastError();
+    }
     s->scheduler = std::thread(schedule, s);
+    s->stepper = std::thread(stepper, s);
+    for (int i = 0; i < 2; i++) {
+        s->creators.emplace_back(creator, s);
+        s->finishers.emplace_back(finisher, s);
+    }
     *out = s;
     return HB_OK;
 }
@@ -383,10 +512,17 @@ void hb_server_destroy(hb_server* s) {
     s->cv.notify_all();
     if (s->scheduler.joinable()) s->scheduler.join();
     {
-        // running jobs finish
+        // admitted jobs finish
         std::unique_lock<std::mutex> lock(s->mu);
         s->cv.wait(lock, [&] { return s->active == 0; });
+        s->shutdown = true;
     }
+    s->cv.notify_all();
+    for (auto& t : s->creators) t.join();
+    if (s->stepper.joinable()) s->stepper.join();
+    for (auto& t : s->finishers) t.join();
+    if (s->multi) hb_multi_destroy(s->multi);
+    if (s->step_stream) cudaStreamDestroy(s->step_stream);
     delete s;
 }
 
