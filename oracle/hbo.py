@@ -98,6 +98,13 @@ def lib():
             "hbo_graph_offsets": (V, [V]),
             "hbo_graph_successors": (V, [V]),
             "hbo_graph_free": (None, [V]),
+            "hbo_visit_create": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32)]),
+            "hbo_visit_destroy": (None, [V]),
+            "hbo_visit_reset": (None, [V]),
+            "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
+                                                ctypes.c_uint64, _P(ctypes.c_uint64),
+                                                _P(ctypes.c_uint64), _P(ctypes.c_uint64),
+                                                ctypes.c_uint64, _P(ctypes.c_uint64)]),
         }
         for k, (r, a) in sig.items():
             f = getattr(L, k)
@@ -303,3 +310,38 @@ class SeqHyperBall:
         out = np.zeros((self.n, self.counter_bytes), dtype=np.uint8)
         lib().hbo_seq_get_array(self._h, which, out.ctypes.data)
         return out
+
+
+class OracleVisit:
+    """The reference's sequential breadth-first visit (seq.rs:113-224)
+    restated: visit(roots) returns the Unknown events (node, pred, distance)
+    in event order; the visited set persists until reset()."""
+
+    def __init__(self, offsets, successors):
+        self._off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        self._suc = np.ascontiguousarray(successors, dtype=np.uint32)
+        self.n = len(self._off) - 1
+        self._h = lib().hbo_visit_create(self.n, self._off.ctypes.data_as(_P(ctypes.c_uint64)),
+                                         self._suc.ctypes.data_as(_P(ctypes.c_uint32)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().hbo_visit_destroy(self._h)
+            self._h = None
+
+    def reset(self):
+        lib().hbo_visit_reset(self._h)
+
+    def visit(self, roots, max_distance=None):
+        r = np.ascontiguousarray(roots, dtype=np.uint64)
+        cap = self.n
+        nodes = np.zeros(cap, dtype=np.uint64)
+        preds = np.zeros(cap, dtype=np.uint64)
+        dists = np.zeros(cap, dtype=np.uint64)
+        known = ctypes.c_uint64()
+        md = 2**64 - 1 if max_distance is None else int(max_distance)
+        P = lambda a: a.ctypes.data_as(_P(ctypes.c_uint64))
+        k = lib().hbo_visit_run(self._h, P(r), len(r), md, P(nodes), P(preds), P(dists), cap,
+                                ctypes.byref(known))
+        return nodes[:k], preds[:k], dists[:k]
+

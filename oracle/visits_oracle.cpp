@@ -1,0 +1,91 @@
+// CPU oracle of the breadth-first visits — test infrastructure only.
+//
+// A restatement of the reference's sequential breadth-first visit
+// (webgraph-algo 0.1.0, src/algo/visits/breadth_first/seq.rs:113-224: roots
+// already visited are skipped, each root is an Unknown event at distance 0,
+// a FIFO queue with a level separator gives the distances) with the
+// distance filter of its documentation example (seq.rs:78-80: nodes farther
+// than max_distance are neither reported nor marked). Only tests/ and
+// bench.py's CPU-baseline leg load it; the product never does.
+#include <cstdint>
+#include <deque>
+#include <vector>
+
+struct hbo_visit {
+    uint64_t n;
+    const uint64_t* off;
+    const uint32_t* succ;
+    std::vector<uint8_t> visited;
+};
+
+extern "C" {
+
+void* hbo_visit_create(uint64_t n, const uint64_t* off, const uint32_t* succ) {
+    return new hbo_visit{n, off, succ, std::vector<uint8_t>(n, 0)};
+}
+
+void hbo_visit_destroy(void* v) { delete (hbo_visit*)v; }
+
+// seq.rs:221-224
+void hbo_visit_reset(void* vv) {
+    hbo_visit* v = (hbo_visit*)vv;
+    std::fill(v->visited.begin(), v->visited.end(), 0);
+}
+
+// One visit (seq.rs:113-219). The Unknown events go to nodes / preds /
+// dists in event order (at most `capacity`); returns their number. Known
+// events (arcs to visited nodes) are counted into *known.
+uint64_t hbo_visit_run(void* vv, const uint64_t* roots, uint64_t nroots, uint64_t max_distance,
+                       uint64_t* nodes, uint64_t* preds, uint64_t* dists, uint64_t capacity,
+                       uint64_t* known) {
+    hbo_visit* v = (hbo_visit*)vv;
+    uint64_t cnt = 0, kn = 0;
+    auto emit = [&](uint64_t node, uint64_t pred, uint64_t d) {
+        if (cnt < capacity) {
+            nodes[cnt] = node;
+            preds[cnt] = pred;
+            dists[cnt] = d;
+        }
+        cnt++;
+    };
+    // a separator of levels: UINT64_MAX
+    std::deque<uint64_t> queue;
+    for (uint64_t i = 0; i < nroots; i++) {
+        const uint64_t r = roots[i];
+        if (v->visited[r]) continue;
+        v->visited[r] = 1;
+        queue.push_back(r);
+        emit(r, r, 0);
+    }
+    if (queue.empty()) {
+        if (known) *known = 0;
+        return 0;
+    }
+    queue.push_back(UINT64_MAX);
+    uint64_t distance = 1;
+    while (!queue.empty()) {
+        const uint64_t node = queue.front();
+        queue.pop_front();
+        if (node != UINT64_MAX) {
+            for (uint64_t e = v->off[node]; e < v->off[node + 1]; e++) {
+                const uint64_t s = v->succ[e];
+                if (!v->visited[s]) {
+                    if (distance <= max_distance) {
+                        v->visited[s] = 1;
+                        emit(s, node, distance);
+                        queue.push_back(s);
+                    }
+                } else {
+                    kn++;
+                }
+            }
+        } else if (!queue.empty()) {
+            distance++;
+            queue.push_back(UINT64_MAX);
+        }
+    }
+    if (known) *known = kn;
+    return cnt;
+}
+
+}  // extern "C"

@@ -1159,6 +1159,10 @@ struct MultiCtx {
         Shape shape;
         cudaGraphExec_t exec;
         uint64_t launches;
+        // the job table the captured copy reads from the page-locked buffer:
+        // put back before every replay
+        std::vector<hbk::UnionArgs> jobs;
+        std::vector<int> log2m;
     };
     std::vector<Graph> graphs;
     std::vector<Shape> seen;
@@ -1295,6 +1299,8 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
         for (const auto& g : mc.graphs)
             if (g.shape == shape) {
                 exec = g.exec;
+                std::copy(g.jobs.begin(), g.jobs.end(), mc.h_jobs);
+                std::copy(g.log2m.begin(), g.log2m.end(), mc.h_log2m);
                 hbk::count_launches((int64_t)g.launches);
                 break;
             }
@@ -1311,7 +1317,9 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
             if (r == HB_OK && e == cudaSuccess && graph) {
                 cudaGraphExec_t x = nullptr;
                 if (cudaGraphInstantiate(&x, graph, 0) == cudaSuccess) {
-                    mc.graphs.push_back(MultiCtx::Graph{shape, x, launches});
+                    mc.graphs.push_back(MultiCtx::Graph{shape, x, launches,
+                                                        std::vector<hbk::UnionArgs>(mc.h_jobs, mc.h_jobs + J),
+                                                        std::vector<int>(mc.h_log2m, mc.h_log2m + J)});
                     exec = x;
                     hbk::count_launches((int64_t)launches);
                 }
