@@ -353,6 +353,50 @@ uint64_t hb_job_footprint(uint64_t num_nodes, uint64_t num_arcs, int log2m);
 /* Last error of a server call on this thread (never NULL). */
 const char* hb_server_last_error(void);
 
+/* ---- breadth-first visits ------------------------------------------------------ */
+/* The fair parallel breadth-first visit of the reference (ParFair,
+ * src/algo/visits/breadth_first/par_fair.rs:92-330) on the device. The
+ * reference reports a visit through callbacks (EventPred::Unknown {node,
+ * pred, distance}, Known, mod.rs:17-60), which cannot cross this boundary;
+ * here a visit returns its Unknown events as arrays, level by level (within
+ * a level in no particular order, as in the parallel reference), and counts
+ * the Known ones. The visited set persists across visits until
+ * hb_visit_reset (par_fair.rs:101, 322-324), so a second visit skips nodes
+ * an earlier one reached, as the reference's does. */
+typedef struct hb_visit hb_visit;
+
+typedef struct hb_visit_stats {
+    uint64_t visited;     /* Unknown events: nodes reached by this visit */
+    uint64_t levels;      /* distinct distances of those nodes */
+    uint64_t known_arcs;  /* Known events: arcs from the visit to already visited nodes */
+} hb_visit_stats;
+
+/* ParFair::new (par_fair.rs:117-124): copies the graph to `device` (checked
+ * like hb_create); `stream` may be NULL (an own stream). The reference's
+ * granularity has no equivalent: the device balances work by warps. */
+int hb_visit_create(const hb_graph_view* graph, int device, void* stream, hb_visit** out);
+void hb_visit_destroy(hb_visit* v);
+/* Parallel::reset (par_fair.rs:322-324): forget every visited node. */
+int hb_visit_reset(hb_visit* v);
+/* One visit (par_visit_filtered_with, par_fair.rs:127-221) from `roots`
+ * (roots already visited are skipped, par_fair.rs:142-156), with the filter
+ * "distance <= max_distance" (UINT64_MAX: none; seq.rs:78-80 shows this
+ * filter): nodes farther away are neither reported nor marked. Event k is
+ * (nodes[k], preds[k], dists[k]); a root is its own predecessor at
+ * distance 0. Any of the three arrays may be NULL. Fewer than the visit's
+ * events fit in `capacity`: the first ones are written and HB_ERR_INVALID is
+ * returned (the visit itself is complete). */
+int hb_visit_run(hb_visit* v, const uint64_t* roots, size_t nroots, uint64_t max_distance,
+                 uint32_t* nodes, uint32_t* preds, uint32_t* dists, size_t capacity,
+                 hb_visit_stats* stats);
+/* visit([root]) for each root in order, the pattern of the reference's tests
+ * (tests/test_bfv.rs:89-101): dist[node] (and pred[node]) is set for every
+ * node a visit reaches; other entries are left as they are. `len` must be
+ * num_nodes; pred may be NULL. */
+int hb_visit_each(hb_visit* v, const uint64_t* roots, size_t nroots, uint32_t* dist, uint32_t* pred,
+                  size_t len);
+const char* hb_visit_last_error(const hb_visit* v);
+
 /* ---- device CSR utilities ----------------------------------------------------- */
 
 /* Transpose of a device-resident CSR graph: d_offsets[num_nodes + 1] and

@@ -101,6 +101,7 @@ def lib():
             "hbo_visit_create": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32)]),
             "hbo_visit_destroy": (None, [V]),
             "hbo_visit_reset": (None, [V]),
+            "hbo_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, _P(ctypes.c_uint64)]),
             "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
                                                 _P(ctypes.c_uint64), _P(ctypes.c_uint64),
@@ -344,4 +345,11 @@ class OracleVisit:
         k = lib().hbo_visit_run(self._h, P(r), len(r), md, P(nodes), P(preds), P(dists), cap,
                                 ctypes.byref(known))
         return nodes[:k], preds[:k], dists[:k]
+
+    def visit_each(self, roots):
+        r = np.ascontiguousarray(roots, dtype=np.uint64)
+        d = np.zeros(self.n, dtype=np.uint64)
+        lib().hbo_visit_each(self._h, r.ctypes.data_as(_P(ctypes.c_uint64)), len(r),
+                             d.ctypes.data_as(_P(ctypes.c_uint64)))
+        return d
 

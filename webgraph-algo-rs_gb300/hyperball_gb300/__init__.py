@@ -148,6 +148,11 @@ class JobInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class VisitStats(ctypes.Structure):
+    _fields_ = [("visited", ctypes.c_uint64), ("levels", ctypes.c_uint64),
+                ("known_arcs", ctypes.c_uint64)]
+
+
 class IterStats(ctypes.Structure):
     _fields_ = [
         ("iteration", ctypes.c_uint64),
@@ -263,6 +268,16 @@ EXPORTS = [
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
     ("hb_debug_far_wait", ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),
+    ("hb_visit_create", ctypes.c_int, [ctypes.POINTER(GraphView), ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    ("hb_visit_destroy", None, [_H]),
+    ("hb_visit_reset", ctypes.c_int, [_H]),
+    ("hb_visit_run", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t,
+                                    ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(VisitStats)]),
+    ("hb_visit_each", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    ("hb_visit_last_error", ctypes.c_char_p, [_H]),
 ]
 
 _lib = None
@@ -1012,4 +1027,76 @@ def release_cached_memory(device=0):
     """Returns the device memory the library keeps for reuse (freed by
     closed handles) to the device."""
     _check(load_library().hb_release_cached_memory(device))
+
+
+# ---------------------------------------------------------------------------
+# breadth-first visits (src/algo/visits/breadth_first/par_fair.rs)
+# ---------------------------------------------------------------------------
+class ParFair:
+    """The fair parallel breadth-first visit of the reference (ParFairPred /
+    ParFairNoPred, par_fair.rs:92-124) on the device. The reference reports
+    a visit through a callback; par_visit returns its Unknown events as
+    arrays (nodes, preds, distances), level by level. The visited set
+    persists across visits until reset(). `granularity` is accepted for
+    parity with ParFair::new; the device balances work by warps."""
+
+    def __init__(self, graph, granularity=1, device=0, stream=None):
+        lib = load_library()
+        self._lib = lib
+        self._graph = graph  # the view below points into it
+        self.num_nodes = graph.num_nodes
+        self.granularity = int(granularity)
+        h = ctypes.c_void_p()
+        v = graph.view()
+        code = lib.hb_visit_create(ctypes.byref(v), int(device), stream, ctypes.byref(h))
+        if code:
+            msg = (lib.hb_visit_last_error(None) or b"").decode(errors="replace")
+            raise _ERRORS.get(code, HyperBallError)(code, msg)
+        self._h = h
+
+    def _check(self, code):
+        if code:
+            msg = (self._lib.hb_visit_last_error(self._h) or b"").decode(errors="replace")
+            raise _ERRORS.get(code, HyperBallError)(code, msg)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.hb_visit_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def reset(self):
+        """Parallel::reset (par_fair.rs:322-324)."""
+        self._check(self._lib.hb_visit_reset(self._h))
+
+    def par_visit(self, roots, max_distance=None):
+        """One visit from `roots` (visited roots skipped); nodes farther than
+        max_distance are neither reported nor marked. Returns (nodes, preds,
+        distances) as uint32 arrays, and the visit's statistics."""
+        r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint64).reshape(-1))
+        n = max(self.num_nodes, 1)
+        nodes = np.zeros(n, dtype=np.uint32)
+        preds = np.zeros(n, dtype=np.uint32)
+        dists = np.zeros(n, dtype=np.uint32)
+        st = VisitStats()
+        md = 2**64 - 1 if max_distance is None else int(max_distance)
+        self._check(self._lib.hb_visit_run(self._h, r.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                           len(r), md, nodes.ctypes.data, preds.ctypes.data,
+                                           dists.ctypes.data, n, ctypes.byref(st)))
+        k = st.visited
+        return nodes[:k], preds[:k], dists[:k], {"visited": st.visited, "levels": st.levels,
+                                                 "known_arcs": st.known_arcs}
+
+    def visit_each(self, roots, dist=None, pred=None):
+        """visit([root]) for each root in order (tests/test_bfv.rs:89-101):
+        dist[node] (and pred[node]) for every node a visit reaches."""
+        r = np.ascontiguousarray(np.asarray(roots, dtype=np.uint64).reshape(-1))
+        if dist is None:
+            dist = np.zeros(self.num_nodes, dtype=np.uint32)
+        pp = pred.ctypes.data if pred is not None else None
+        self._check(self._lib.hb_visit_each(self._h, r.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                            len(r), dist.ctypes.data, pp, self.num_nodes))
+        return dist
 
