@@ -58,7 +58,8 @@ def parse_args():
                    help="graph size (2^log2n nodes; default 26 web-like, 24 R-MAT)")
     p.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: --steps)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served"], default="weblike",
+    p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served", "visit"],
+                   default="weblike",
                    help="weblike: the 2^26 web-like graph (default); rmat: R-MAT 2^24 x 16, "
                         "log2m 8; batched: many small graphs; served: a Poisson stream of jobs "
                         "through the job server")
@@ -603,6 +604,7 @@ def run_batched(args):
     arcs = sum(g.num_arcs for g in graphs)
 
     replays = [None]
+    union_ms = [0.0]
 
     def batch_run():
         b = hb.HyperBallBatch(graphs, log2ms, sum_of_distances=True, sum_of_inverse_distances=True)
@@ -614,6 +616,7 @@ def run_batched(args):
         st = b.stats()
         b.close()
         replays[0] = f'{st["graph_replays"]} of {st["group_iterations"]}'
+        union_ms[0] = st["union_ms"]
         return st["register_updates"], dt, st["iterations"]
 
     for _ in range(max(args.warmup - 2, 1)):
@@ -652,7 +655,8 @@ def run_batched(args):
                    "arcs": arcs, "graphs": "n log-uniform in [1e3, 2e5]; even seeds Erdos-Renyi "
                    "out-degree U[4,32], odd seeds R-MAT(.57,.19,.19,.05) 16 arcs/node; "
                    "log2m in {4,6,8}", "iterations": iters,
-                   "graph_replayed_group_iterations": replays[0]},
+                   "graph_replayed_steps": replays[0],
+                   "union_ms_per_run": union_ms[0]},
         "one_at_a_time": {"value": alone, "unit": UNIT, "graphs": len(sample),
                           "seconds": a_secs,
                           "note": "single-instance API, each graph alone (same graphs, run to "
@@ -801,6 +805,63 @@ def run_served(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# breadth-first visit of the web-like graph (the reference's ParFair)
+# ---------------------------------------------------------------------------
+def run_visit(args):
+    """One step = one visit from node 0 of the web-like graph (every node it
+    reaches, no filter), after a reset; the unit is the arc examined (each
+    arc of every visited node: the reference's Unknown and Known events)."""
+    import numpy as np
+    import torch
+    import hyperball_gb300 as hb
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    torch.cuda.set_device(0)
+    g = hb.Graph.weblike(1 << args.log2n)
+    stream = torch.cuda.Stream()
+    v = hb.ParFair(g, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        v.reset()
+        nodes, _, _, st = v.par_visit([0])
+    off = np.asarray(g.offsets)
+    arcs = int(np.sum(off[nodes.astype(np.int64) + 1] - off[nodes.astype(np.int64)]))
+    secs = []
+    for _ in range(args.steps):
+        v.reset()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        _, _, _, st = v.par_visit([0])
+        torch.cuda.synchronize()
+        secs.append(time.perf_counter() - t)
+    ms = 1e3 * sum(secs) / len(secs)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import hbo
+        o = hbo.OracleVisit(g.offsets, g.successors)
+        t = time.perf_counter()
+        on = o.visit([0])[0]
+        dt = time.perf_counter() - t
+        if len(on) != st["visited"]:
+            raise RuntimeError("the oracle's visit reached another number of nodes")
+        cpu = {"value": arcs / dt, "unit": "arcs/s", "cores": 1, "kind": "port",
+               "sample": f"sequential breadth-first visit (seq.rs restated), the same visit, {dt:.1f} s"}
+    line = {
+        "metric": "breadth-first visit arcs examined/s", "value": arcs / (ms / 1e3),
+        "unit": "arcs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"weblike-2^{args.log2n} breadth-first visit from node 0",
+                   "nodes": g.num_nodes, "arcs": g.num_arcs, "visited": st["visited"],
+                   "levels": st["levels"], "arcs_examined": arcs,
+                   "note": "the step includes the events' copy to the host"},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -809,6 +870,8 @@ def main():
         return run_batched(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "visit":
+        return run_visit(args)
     return run_gb300(args)
 
 

@@ -277,12 +277,13 @@ int hb_batch_get_harmonic_centralities(const hb_batch* b, uint32_t graph, double
 int hb_batch_get_registers(const hb_batch* b, uint32_t graph, void* dst, size_t bytes);
 /* Totals over the batch: iterations of the longest group, visited arcs and
  * arc-register updates (visited arcs * 2^log2m) summed over every instance and
- * iteration, device time of the iterations (summed over groups). */
+ * iteration, and the device time of the shared union launches of the run. */
 int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_arcs,
                    uint64_t* register_updates, double* device_ms);
-/* Union iterations of the batch's groups that ran as replays of a captured
- * CUDA graph, and all of them (a batch captures an iteration shape the second
- * time it comes). No reference counterpart. */
+/* Steps of the last run (one iteration of every running group each) that ran
+ * as replays of a captured CUDA graph, and all steps (a step's launch
+ * sequence is captured the second time its shape comes). No reference
+ * counterpart. */
 int hb_batch_graph_replays(const hb_batch* b, uint64_t* replayed, uint64_t* iterations);
 void hb_batch_destroy(hb_batch* b);
 

@@ -1149,6 +1149,10 @@ struct MultiCtx {
     int* h_log2m = nullptr;
     int grid = 1;
     cudaEvent_t u0 = nullptr, u1 = nullptr;
+    // a handle with a stream of its own runs its pre and post parts there, so
+    // that the small kernels of different handles overlap (steps launched
+    // directly, not captured)
+    cudaEvent_t fork_ev[64] = {}, join_ev[64] = {};
     bool use_graphs = true;
     struct Shape {
         std::vector<const hb_handle*> hs;
@@ -1188,6 +1192,11 @@ static void multi_free(MultiCtx& mc) {
     if (mc.h_log2m) cudaFreeHost(mc.h_log2m);
     if (mc.u0) cudaEventDestroy(mc.u0);
     if (mc.u1) cudaEventDestroy(mc.u1);
+    for (int j = 0; j < 64; j++) {
+        if (mc.fork_ev[j]) cudaEventDestroy(mc.fork_ev[j]);
+        if (mc.join_ev[j]) cudaEventDestroy(mc.join_ev[j]);
+        mc.fork_ev[j] = mc.join_ev[j] = nullptr;
+    }
     if (mc.cap) cudaStreamDestroy(mc.cap);
     mc.d_cursor = nullptr;
     mc.d_jobs = nullptr;
@@ -1210,6 +1219,10 @@ static int multi_init(MultiCtx& mc, int device, cudaStream_t s) {
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u0);
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mc.cap, cudaStreamNonBlocking);
+    for (int j = 0; j < 64 && e == cudaSuccess; j++) {
+        e = cudaEventCreateWithFlags(&mc.fork_ev[j], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mc.join_ev[j], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         mc.err = std::string("multi-instance setup: ") + cudaGetErrorString(e);
@@ -1227,8 +1240,28 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
         return external ? cudaEventRecordWithFlags(e, x, cudaEventRecordExternal) : cudaEventRecord(e, x);
     };
     int r;
-    for (size_t j = 0; j < hs.size(); j++)
-        if ((r = enqueue_pre(hs[j], plans[j].a, plans[j].first_systolic, x, external))) return r;
+    // the stream a handle's pre and post parts run on, forked from x and joined back
+    auto own = [&](size_t j) { return !external && hs[j]->stream && hs[j]->stream != x; };
+    auto fork = [&](size_t j) -> cudaError_t {
+        cudaError_t e = cudaEventRecord(mc.fork_ev[j], x);
+        return e == cudaSuccess ? cudaStreamWaitEvent(hs[j]->stream, mc.fork_ev[j], 0) : e;
+    };
+    auto join = [&](size_t j) -> cudaError_t {
+        cudaError_t e = cudaEventRecord(mc.join_ev[j], hs[j]->stream);
+        return e == cudaSuccess ? cudaStreamWaitEvent(x, mc.join_ev[j], 0) : e;
+    };
+    auto fail = [&](cudaError_t e) {
+        mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
+        return HB_ERR_CUDA;
+    };
+    for (size_t j = 0; j < hs.size(); j++) {
+        const cudaStream_t y = own(j) ? hs[j]->stream : x;
+        if (y != x)
+            if (cudaError_t e = fork(j); e != cudaSuccess) return fail(e);
+        if ((r = enqueue_pre(hs[j], plans[j].a, plans[j].first_systolic, y, external))) return r;
+        if (y != x)
+            if (cudaError_t e = join(j); e != cudaSuccess) return fail(e);
+    }
     uint32_t J = 0;
     for (size_t j = 0; j < hs.size(); j++) {
         hb_handle* h = hs[j];
@@ -1272,8 +1305,14 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
         mc.err = cudaGetErrorString(e);
         return HB_ERR_CUDA;
     }
-    for (size_t j = 0; j < hs.size(); j++)
-        if ((r = enqueue_post(hs[j], plans[j].a, x, external))) return r;
+    for (size_t j = 0; j < hs.size(); j++) {
+        const cudaStream_t y = own(j) ? hs[j]->stream : x;
+        if (y != x)
+            if (cudaError_t e = fork(j); e != cudaSuccess) return fail(e);
+        if ((r = enqueue_post(hs[j], plans[j].a, y, external))) return r;
+        if (y != x)
+            if (cudaError_t e = join(j); e != cudaSuccess) return fail(e);
+    }
     return HB_OK;
 }
 
@@ -1749,15 +1788,14 @@ int hb_batch_stats(const hb_batch* b, uint64_t* iterations, uint64_t* visited_ar
                    uint64_t* register_updates, double* device_ms) {
     if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
     uint64_t it = 0, vis = 0, upd = 0;
-    double ms = 0.0;
     for (const auto& g : b->groups) {
         it = std::max<uint64_t>(it, g.h->iteration);
         for (const auto& s : g.h->stats) {
             vis += s.visited_arcs;
             upd += s.visited_arcs << g.h->log2m;
-            ms += s.iteration_ms;
         }
     }
+    const double ms = b->mc.union_ms;
     if (iterations) *iterations = it;
     if (visited_arcs) *visited_arcs = vis;
     if (register_updates) *register_updates = upd;

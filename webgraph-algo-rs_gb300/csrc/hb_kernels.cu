@@ -782,19 +782,19 @@ __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constan
 constexpr int MAX_JOBS = 64;
 
 template <int LOG2M>
-__device__ __forceinline__ uint32_t job_work(const UnionArgs& a) {
+__device__ __forceinline__ WorkItems job_items(const UnionArgs& a) {
     constexpr int G = Geo<LOG2M>::CHUNKS, TB_MED = team_lanes<LOG2M>();
-    return work_items<32 / G, 32 / TB_MED>(a).n_work;
+    return work_items<32 / G, 32 / TB_MED>(a);
 }
 
 template <int LOG2M>
-__device__ __forceinline__ void job_item(const UnionArgs& a, uint32_t k, uint32_t& modc,
-                                         uint32_t& scanned, uint32_t& sarcs, uint32_t& vis) {
+__device__ __forceinline__ void job_item(const UnionArgs& a, const WorkItems& wi, uint32_t k,
+                                         uint32_t& modc, uint32_t& scanned, uint32_t& sarcs,
+                                         uint32_t& vis) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS;
     constexpr int TB_MED = team_lanes<LOG2M>();
     constexpr int NPW_L = 32 / G, NPW_M = 32 / TB_MED;
-    const WorkItems wi = work_items<NPW_L, NPW_M>(a);
     const uint2 d = item_at<NPW_L, NPW_M>(a, wi, k);
     const uint32_t cnt = d.y & 0x7fffffffu;
     FarState fs{0u};
@@ -830,17 +830,21 @@ __global__ void __launch_bounds__(256, 2) k_union_jobs(const UnionArgs* __restri
                                                        const int* __restrict__ log2m, uint32_t njobs,
                                                        unsigned long long* cursor) {
     __shared__ uint32_t s_first[MAX_JOBS + 1];
+    __shared__ WorkItems s_wi[MAX_JOBS];
     if (threadIdx.x == 0) {
         uint32_t t = 0;
         for (uint32_t j = 0; j < njobs; j++) {
             s_first[j] = t;
             const UnionArgs& a = jobs[j];
+            WorkItems wi{};
             switch (log2m[j]) {
-                case 4: t += job_work<4>(a); break;
-                case 6: t += job_work<6>(a); break;
-                case 8: t += job_work<8>(a); break;
+                case 4: wi = job_items<4>(a); break;
+                case 6: wi = job_items<6>(a); break;
+                case 8: wi = job_items<8>(a); break;
                 default: break;
             }
+            s_wi[j] = wi;
+            t += wi.n_work;
         }
         s_first[njobs] = t;
     }
@@ -862,10 +866,11 @@ __global__ void __launch_bounds__(256, 2) k_union_jobs(const UnionArgs* __restri
         }
         const UnionArgs& a = jobs[j];
         const uint32_t k = w - s_first[j];
+        const WorkItems wi = s_wi[j];
         switch (log2m[j]) {
-            case 4: job_item<4>(a, k, modc, scanned, sarcs, vis); break;
-            case 6: job_item<6>(a, k, modc, scanned, sarcs, vis); break;
-            case 8: job_item<8>(a, k, modc, scanned, sarcs, vis); break;
+            case 4: job_item<4>(a, wi, k, modc, scanned, sarcs, vis); break;
+            case 6: job_item<6>(a, wi, k, modc, scanned, sarcs, vis); break;
+            case 8: job_item<8>(a, wi, k, modc, scanned, sarcs, vis); break;
             default: break;
         }
     }

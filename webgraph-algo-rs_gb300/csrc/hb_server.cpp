@@ -6,14 +6,14 @@
 // slot is free (at most max_active jobs past admission) and its estimated
 // device footprint fits the budget next to the admitted jobs. Admitted jobs
 // go through three stages, each with its own host thread(s):
-//   creation  (two threads)  hb_create on the job's own stream: CSR upload,
+//   creation  (up to 8 threads) hb_create on the job's own stream: CSR upload,
 //                            partition, renumbering, transpose;
 //   stepping  (one thread)   every running job advances one iteration per
 //                            step, and the union work of all of them runs as
 //                            one kernel launch (hb_multi_step); a job created
 //                            meanwhile joins at the next step, a finished one
 //                            leaves after the step that stopped it;
-//   results   (two threads)  neighbourhood function, sums and registers to
+//   results   (up to 8 threads) neighbourhood function, sums and registers to
 //                            the host, handle destroyed, budget released.
 // So requests that arrive while others run are admitted as slots and memory
 // free up, and their iterations interleave in the shared kernel. Latency is
@@ -332,7 +332,10 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
     }
     s->scheduler = std::thread(schedule, s);
     s->stepper = std::thread(stepper, s);
-    for (int i = 0; i < 2; i++) {
+    // creation and results of different jobs overlap (host copies, device
+    // set-up kernels on the jobs' own streams) beside the stepping thread
+    const uint32_t workers = std::min<uint32_t>(o.max_active, 8);
+    for (uint32_t i = 0; i < workers; i++) {
         s->creators.emplace_back(creator, s);
         s->finishers.emplace_back(finisher, s);
     }

@@ -913,7 +913,7 @@ class HyperBallBatch:
         rep, total = ctypes.c_uint64(), ctypes.c_uint64()
         _check(self._lib.hb_batch_graph_replays(self._h, ctypes.byref(rep), ctypes.byref(total)))
         return {"iterations": it.value, "visited_arcs": vis.value, "register_updates": upd.value,
-                "device_ms": ms.value, "graph_replays": rep.value, "group_iterations": total.value}
+                "union_ms": ms.value, "graph_replays": rep.value, "group_iterations": total.value}
 
 
 # ---------------------------------------------------------------------------
