@@ -301,7 +301,7 @@ typedef struct hb_server_options {
     uint32_t struct_size;      /* sizeof(hb_server_options) */
     int32_t device;            /* CUDA device ordinal */
     uint64_t hbm_budget_bytes; /* device bytes the running jobs may hold together; default 150e9 */
-    uint32_t max_active;       /* jobs on the device at once; default 16 */
+    uint32_t max_active;       /* jobs past admission at once, 1 to 48; default 16 */
     uint32_t keep_registers;   /* 1: keep each finished job's counters for hb_server_get_registers */
 } hb_server_options;
 

@@ -1143,10 +1143,8 @@ struct MultiCtx {
     cudaStream_t s = nullptr;         // every launch of a step (the handles' buffers are ordered before it)
     cudaStream_t cap = nullptr;       // capture stream
     unsigned long long* d_cursor = nullptr;
-    hbk::UnionArgs* d_jobs = nullptr;
-    int* d_log2m = nullptr;
-    hbk::UnionArgs* h_jobs = nullptr;  // page-locked
-    int* h_log2m = nullptr;
+    // the shared launch's job table (its kernel parameters)
+    std::unique_ptr<hbk::JobsArgs> jobs;
     int grid = 1;
     cudaEvent_t u0 = nullptr, u1 = nullptr;
     // a handle with a stream of its own runs its pre and post parts there, so
@@ -1163,10 +1161,6 @@ struct MultiCtx {
         Shape shape;
         cudaGraphExec_t exec;
         uint64_t launches;
-        // the job table the captured copy reads from the page-locked buffer:
-        // put back before every replay
-        std::vector<hbk::UnionArgs> jobs;
-        std::vector<int> log2m;
     };
     std::vector<Graph> graphs;
     std::vector<Shape> seen;
@@ -1176,7 +1170,7 @@ struct MultiCtx {
 };
 
 static bool job_kernel_log2m(int l) { return l == 4 || l == 6 || l == 8; }
-static constexpr uint32_t kMaxJobs = 64;   // k_union_jobs' MAX_JOBS
+static constexpr uint32_t kMaxJobs = hbk::MAX_JOBS;
 static constexpr size_t kMaxMultiGraphs = 64;
 
 static void multi_free(MultiCtx& mc) {
@@ -1186,10 +1180,7 @@ static void multi_free(MultiCtx& mc) {
     mc.graphs.clear();
     mc.seen.clear();
     if (mc.d_cursor) cudaFree(mc.d_cursor);
-    if (mc.d_jobs) cudaFree(mc.d_jobs);
-    if (mc.d_log2m) cudaFree(mc.d_log2m);
-    if (mc.h_jobs) cudaFreeHost(mc.h_jobs);
-    if (mc.h_log2m) cudaFreeHost(mc.h_log2m);
+    mc.jobs.reset();
     if (mc.u0) cudaEventDestroy(mc.u0);
     if (mc.u1) cudaEventDestroy(mc.u1);
     for (int j = 0; j < 64; j++) {
@@ -1199,10 +1190,6 @@ static void multi_free(MultiCtx& mc) {
     }
     if (mc.cap) cudaStreamDestroy(mc.cap);
     mc.d_cursor = nullptr;
-    mc.d_jobs = nullptr;
-    mc.d_log2m = nullptr;
-    mc.h_jobs = nullptr;
-    mc.h_log2m = nullptr;
     mc.u0 = mc.u1 = nullptr;
     mc.cap = nullptr;
 }
@@ -1212,10 +1199,7 @@ static int multi_init(MultiCtx& mc, int device, cudaStream_t s) {
     mc.s = s;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_cursor, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_jobs, kMaxJobs * sizeof(hbk::UnionArgs));
-    if (e == cudaSuccess) e = cudaMalloc((void**)&mc.d_log2m, kMaxJobs * sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&mc.h_jobs, kMaxJobs * sizeof(hbk::UnionArgs));
-    if (e == cudaSuccess) e = cudaMallocHost((void**)&mc.h_log2m, kMaxJobs * sizeof(int));
+    mc.jobs.reset(new hbk::JobsArgs());
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u0);
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mc.cap, cudaStreamNonBlocking);
@@ -1263,20 +1247,19 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
             if (cudaError_t e = join(j); e != cudaSuccess) return fail(e);
     }
     uint32_t J = 0;
+    hbk::JobsArgs& p = *mc.jobs;
     for (size_t j = 0; j < hs.size(); j++) {
         hb_handle* h = hs[j];
         if (!h->n_tiles || !job_kernel_log2m(h->log2m) || plans[j].a.far_tma) continue;
-        mc.h_jobs[J] = plans[j].a;
-        mc.h_log2m[J] = h->log2m;
+        p.job[J] = plans[j].a;
+        p.log2m[J] = h->log2m;
         J++;
     }
+    p.njobs = J;
+    p.cursor = mc.d_cursor;
     *njobs = J;
     if (J) {
-        cudaError_t e = cudaMemcpyAsync(mc.d_jobs, mc.h_jobs, J * sizeof(hbk::UnionArgs),
-                                        cudaMemcpyHostToDevice, x);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(mc.d_log2m, mc.h_log2m, J * sizeof(int), cudaMemcpyHostToDevice, x);
-        if (e == cudaSuccess) e = cudaMemsetAsync(mc.d_cursor, 0, sizeof(unsigned long long), x);
+        cudaError_t e = cudaMemsetAsync(mc.d_cursor, 0, sizeof(unsigned long long), x);
         if (e != cudaSuccess) {
             mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
             return HB_ERR_CUDA;
@@ -1293,7 +1276,7 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
         if ((r = enqueue_union(h, plans[j].a, x, own))) return r;
     }
     if (J) {
-        const int e = hbk::launch_union_jobs(mc.d_jobs, mc.d_log2m, J, mc.d_cursor, mc.grid, x);
+        const int e = hbk::launch_union_jobs(p, mc.grid, x);
         if (e) {
             mc.err = std::string("k_union_jobs: ") + cudaGetErrorString((cudaError_t)e);
             return HB_ERR_CUDA;
@@ -1321,7 +1304,7 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
 static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
     if (hs.empty()) return HB_OK;
     if (hs.size() > kMaxJobs) {
-        mc.err = "more than 64 instances in one step";
+        mc.err = "more than 48 instances in one step";
         return HB_ERR_INVALID;
     }
     std::vector<IterPlan> plans(hs.size());
@@ -1338,8 +1321,6 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
         for (const auto& g : mc.graphs)
             if (g.shape == shape) {
                 exec = g.exec;
-                std::copy(g.jobs.begin(), g.jobs.end(), mc.h_jobs);
-                std::copy(g.log2m.begin(), g.log2m.end(), mc.h_log2m);
                 hbk::count_launches((int64_t)g.launches);
                 break;
             }
@@ -1356,9 +1337,7 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
             if (r == HB_OK && e == cudaSuccess && graph) {
                 cudaGraphExec_t x = nullptr;
                 if (cudaGraphInstantiate(&x, graph, 0) == cudaSuccess) {
-                    mc.graphs.push_back(MultiCtx::Graph{shape, x, launches,
-                                                        std::vector<hbk::UnionArgs>(mc.h_jobs, mc.h_jobs + J),
-                                                        std::vector<int>(mc.h_log2m, mc.h_log2m + J)});
+                    mc.graphs.push_back(MultiCtx::Graph{shape, x, launches});
                     exec = x;
                     hbk::count_launches((int64_t)launches);
                 }
@@ -1685,7 +1664,7 @@ int hb_batch_run_until_done(hb_batch* b) {
     if (!b) return set_err(nullptr, HB_ERR_INVALID, "batch is NULL");
     cudaError_t ce = cudaSetDevice(b->device);
     if (ce != cudaSuccess) return set_err(nullptr, HB_ERR_CUDA, cudaGetErrorString(ce));
-    if (!b->mc.d_jobs) {
+    if (!b->mc.jobs) {
         int r = multi_init(b->mc, b->device, b->stream);
         if (r) return set_err(nullptr, r, b->mc.err);
     }

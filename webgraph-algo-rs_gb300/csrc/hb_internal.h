@@ -156,10 +156,17 @@ int tile_grid(int log2m, int device, int occ);
 // standard iterations on the staged window kernel (items table; m < 2^32)
 int launch_union_staged(int log2m, const UnionArgs& a, int grid, void* stream);
 int staged_grid(int log2m, int device, int occ);
-// the window work of several handles in one launch (log2m 4, 6 or 8 each;
-// jobs and log2m in device memory; at most 64 jobs)
-int launch_union_jobs(const UnionArgs* jobs, const int* log2m, uint32_t njobs,
-                      unsigned long long* cursor, int grid, void* stream);
+// the window work of several handles in one launch (log2m 4, 6 or 8 each):
+// every job's arguments travel as kernel parameters (constant bank), so at
+// most 48 jobs fit the 32 KB parameter space
+constexpr int MAX_JOBS = 48;
+struct JobsArgs {
+    UnionArgs job[MAX_JOBS];
+    int log2m[MAX_JOBS];
+    uint32_t njobs;
+    unsigned long long* cursor;  // zero at launch
+};
+int launch_union_jobs(const JobsArgs& p, int grid, void* stream);
 int jobs_grid(int device);
 // batches: queue = the chunks of the running instances (modified count of
 // the previous iteration nonzero, or every instance when `all`), queue_len its
@@ -248,7 +255,7 @@ int hb_multi_create(int device, void* stream, hb_multi** out, std::string& err);
 void hb_multi_destroy(hb_multi* m);
 // hb_init of a handle that will be stepped (its own stream, synchronous)
 int hb_multi_start(hb_handle* h);
-// one iteration of each of the count handles (count <= 64)
+// one iteration of each of the count handles (count <= MAX_JOBS)
 int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err);
 // the handle's run is over: its last iteration modified no counter, or it
 // ran num_nodes iterations (the stop rules of run_until_done, HB:541, HB:559-570)

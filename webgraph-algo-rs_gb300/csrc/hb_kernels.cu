@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <mutex>
 
@@ -779,7 +780,6 @@ __global__ void __launch_bounds__(256, MINB) k_union_window(const __grid_constan
 // Integer totals go to each job's partial slot when the warp moves to
 // another job.
 // ---------------------------------------------------------------------------
-constexpr int MAX_JOBS = 64;
 
 template <int LOG2M>
 __device__ __forceinline__ WorkItems job_items(const UnionArgs& a) {
@@ -826,18 +826,18 @@ __device__ __forceinline__ void flush_totals(const UnionArgs& a, uint32_t& modc,
     modc = scanned = sarcs = vis = 0;
 }
 
-__global__ void __launch_bounds__(256, 2) k_union_jobs(const UnionArgs* __restrict__ jobs,
-                                                       const int* __restrict__ log2m, uint32_t njobs,
-                                                       unsigned long long* cursor) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_union_jobs(const __grid_constant__ JobsArgs p) {
     __shared__ uint32_t s_first[MAX_JOBS + 1];
     __shared__ WorkItems s_wi[MAX_JOBS];
+    const uint32_t njobs = p.njobs;
     if (threadIdx.x == 0) {
         uint32_t t = 0;
         for (uint32_t j = 0; j < njobs; j++) {
             s_first[j] = t;
-            const UnionArgs& a = jobs[j];
+            const UnionArgs& a = p.job[j];
             WorkItems wi{};
-            switch (log2m[j]) {
+            switch (p.log2m[j]) {
                 case 4: wi = job_items<4>(a); break;
                 case 6: wi = job_items<6>(a); break;
                 case 8: wi = job_items<8>(a); break;
@@ -855,26 +855,26 @@ __global__ void __launch_bounds__(256, 2) k_union_jobs(const UnionArgs* __restri
     uint32_t cur_job = 0xffffffffu;
     for (;;) {
         uint32_t w = 0;
-        if (lane == 0) w = (uint32_t)atomicAdd(cursor, 1ull);
+        if (lane == 0) w = (uint32_t)atomicAdd(p.cursor, 1ull);
         w = __shfl_sync(0xffffffffu, w, 0);
         if (w >= total) break;
         uint32_t j = 0;
         while (j + 1 < njobs && s_first[j + 1] <= w) j++;
         if (j != cur_job) {
-            if (cur_job != 0xffffffffu) flush_totals(jobs[cur_job], modc, scanned, sarcs, vis);
+            if (cur_job != 0xffffffffu) flush_totals(p.job[cur_job], modc, scanned, sarcs, vis);
             cur_job = j;
         }
-        const UnionArgs& a = jobs[j];
+        const UnionArgs& a = p.job[j];
         const uint32_t k = w - s_first[j];
         const WorkItems wi = s_wi[j];
-        switch (log2m[j]) {
+        switch (p.log2m[j]) {
             case 4: job_item<4>(a, wi, k, modc, scanned, sarcs, vis); break;
             case 6: job_item<6>(a, wi, k, modc, scanned, sarcs, vis); break;
             case 8: job_item<8>(a, wi, k, modc, scanned, sarcs, vis); break;
             default: break;
         }
     }
-    if (cur_job != 0xffffffffu) flush_totals(jobs[cur_job], modc, scanned, sarcs, vis);
+    if (cur_job != 0xffffffffu) flush_totals(p.job[cur_job], modc, scanned, sarcs, vis);
 }
 
 // batches: the chunks of the running instances, in chunk order. inst_chunk[i]
@@ -1458,28 +1458,47 @@ __global__ void k_sum_f64(const double* __restrict__ in, uint64_t count, double*
 // ---------------------------------------------------------------------------
 // batches: per instance (a device id range) the number of modified counters
 // and the neighbourhood function (sum of the cached estimates) of the
-// iteration just run; one warp per instance, fixed order
+// iteration just run; one block per running instance, fixed order
 // ---------------------------------------------------------------------------
-__global__ void k_inst_stats(const uint32_t* __restrict__ next_mod, const double* __restrict__ est,
-                             const uint64_t* __restrict__ starts, uint32_t count,
-                             unsigned long long* __restrict__ mods, double* __restrict__ nfs) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t i = gw; i < count; i += nw) {
+__global__ void __launch_bounds__(256) k_inst_stats(const uint32_t* __restrict__ next_mod,
+                                                    const double* __restrict__ est,
+                                                    const uint64_t* __restrict__ starts, uint32_t count,
+                                                    unsigned long long* __restrict__ mods,
+                                                    double* __restrict__ nfs) {
+    // one block per instance, a fixed order: thread t sums nodes b + t,
+    // b + t + 256, ..., then a fixed tree. An instance whose previous
+    // iteration modified nothing has stopped: its values stay.
+    __shared__ double s_nf[256];
+    __shared__ unsigned long long s_mc[256];
+    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        if (mods[i] == 0) continue;  // uniform over the block
+        __syncthreads();
         const uint64_t b = __ldg(starts + i), e = __ldg(starts + i + 1);
+        double sum = 0.0;
+        for (uint64_t v = b + threadIdx.x; v < e; v += blockDim.x) sum = __dadd_rn(sum, est[v]);
         unsigned long long mc = 0;
-        double s = 0.0;
-        for (uint64_t v = b + lane; v < e; v += 32) {
-            s = __dadd_rn(s, est[v]);
-            mc += (__ldg(next_mod + (v >> 5)) >> (v & 31)) & 1u;
+        if (e > b) {
+            const uint64_t w0 = b >> 5, w1 = (e - 1) >> 5;
+            for (uint64_t w = w0 + threadIdx.x; w <= w1; w += blockDim.x) {
+                uint32_t bits = __ldg(next_mod + w);
+                if (w == w0) bits &= 0xffffffffu << (b & 31);
+                if (w == w1 && ((e & 31) != 0)) bits &= 0xffffffffu >> (32 - (e & 31));
+                mc += __popc(bits);
+            }
         }
-        s = warp_sum_f64(s);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) mc += __shfl_xor_sync(0xffffffffu, mc, off);
-        if (lane == 0) {
-            mods[i] = mc;
-            nfs[i] = s;
+        s_nf[threadIdx.x] = sum;
+        s_mc[threadIdx.x] = mc;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) {
+                s_nf[threadIdx.x] = __dadd_rn(s_nf[threadIdx.x], s_nf[threadIdx.x + w]);
+                s_mc[threadIdx.x] += s_mc[threadIdx.x + w];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            mods[i] = s_mc[0];
+            nfs[i] = s_nf[0];
         }
     }
 }
@@ -2186,9 +2205,9 @@ int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n
 
 int launch_inst_stats(const uint32_t* next_mod, const double* est, const uint64_t* starts,
                       uint32_t count, unsigned long long* mods, double* nfs, void* stream) {
-    const int grid = (int)std::min<uint64_t>(((uint64_t)count * 32 + 255) / 256 + 1, 8192);
+    const int grid = (int)std::min<uint64_t>((uint64_t)count, 16384);
     ++t_launches;
-    k_inst_stats<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, est, starts, count, mods, nfs);
+    if (grid) k_inst_stats<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, est, starts, count, mods, nfs);
     return (int)cudaGetLastError();
 }
 
@@ -2269,17 +2288,30 @@ int staged_grid(int log2m, int device, int occ) {
 #undef CALL
 }
 
-int launch_union_jobs(const UnionArgs* jobs, const int* log2m, uint32_t njobs,
-                      unsigned long long* cursor, int grid, void* stream) {
-    if (njobs > (uint32_t)MAX_JOBS) return (int)cudaErrorInvalidValue;
+static int jobs_minb() {
+    static const int v = [] {
+        const char* e = std::getenv("HB_JOBS_BLOCKS");
+        return e && std::atoi(e) == 3 ? 3 : 2;
+    }();
+    return v;
+}
+
+int launch_union_jobs(const JobsArgs& p, int grid, void* stream) {
+    if (p.njobs > (uint32_t)MAX_JOBS) return (int)cudaErrorInvalidValue;
     ++t_launches;
-    k_union_jobs<<<grid, 256, 0, (cudaStream_t)stream>>>(jobs, log2m, njobs, cursor);
+    if (jobs_minb() == 3)
+        k_union_jobs<3><<<grid, 256, 0, (cudaStream_t)stream>>>(p);
+    else
+        k_union_jobs<2><<<grid, 256, 0, (cudaStream_t)stream>>>(p);
     return (int)cudaGetLastError();
 }
 
 int jobs_grid(int device) {
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_jobs, 256, 0);
+    if (jobs_minb() == 3)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_jobs<3>, 256, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_union_jobs<2>, 256, 0);
     return std::max(1, per_sm) * num_sms(device);
 }
 

@@ -180,7 +180,7 @@ static void stepper(hb_server* s) {
             });
             if (running.empty() && s->ready.empty() && s->shutdown) return;
             // newly created jobs join at this step
-            while (!s->ready.empty() && running.size() < 64) {
+            while (!s->ready.empty() && running.size() < (size_t)hbk::MAX_JOBS) {
                 std::shared_ptr<Job> j = s->ready.front();
                 s->ready.pop_front();
                 if (hb_multi_done(j->h))
@@ -311,8 +311,8 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
             return server_err(HB_ERR_INVALID, "hb_server_options.struct_size mismatch");
         o = *opts;
     }
-    if (o.max_active == 0 || o.max_active > 64)
-        return server_err(HB_ERR_INVALID, "max_active must be in [1, 64]");
+    if (o.max_active == 0 || o.max_active > (uint32_t)hbk::MAX_JOBS)
+        return server_err(HB_ERR_INVALID, "max_active must be in [1, 48]");
     hb_server* s = new hb_server();
     s->opts = o;
     int ndev = 0;
