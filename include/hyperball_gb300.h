@@ -370,6 +370,7 @@ typedef struct hb_visit_stats {
     uint64_t visited;     /* Unknown events: nodes reached by this visit */
     uint64_t levels;      /* distinct distances of those nodes */
     uint64_t known_arcs;  /* Known events: arcs from the visit to already visited nodes */
+    double device_ms;     /* device time of the visit's kernels (roots to the last level) */
 } hb_visit_stats;
 
 /* ParFair::new (par_fair.rs:117-124): copies the graph to `device` (checked

@@ -155,9 +155,8 @@ struct hb_visit {
     unsigned long long* h_cnt = nullptr;   // page-locked copy
     uint64_t tail = 0;
     int sms = 1;
-    std::vector<uint64_t> host_visited;    // mirror of d_visited (visit_each)
-    uint32_t* h_nodes = nullptr;           // page-locked staging of a visit's events
-    uint32_t* h_preds = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<uint32_t> host_visited;    // copy of d_visited (visit_each)
     std::string err;
 };
 
@@ -197,8 +196,8 @@ static void visit_free(hb_visit* v) {
     cudaFree(v->d_roots);
     cudaFree(v->d_cnt);
     if (v->h_cnt) cudaFreeHost(v->h_cnt);
-    if (v->h_nodes) cudaFreeHost(v->h_nodes);
-    if (v->h_preds) cudaFreeHost(v->h_preds);
+    if (v->ev0) cudaEventDestroy(v->ev0);
+    if (v->ev1) cudaEventDestroy(v->ev1);
     if (v->own_stream && v->stream) cudaStreamDestroy(v->stream);
     delete v;
 }
@@ -270,7 +269,10 @@ int hb_visit_create(const hb_graph_view* g, int device, void* stream, hb_visit**
         (r = visit_cuda(v, cudaStreamSynchronize(v->stream), "cudaStreamSynchronize")))
         return fail(r);
     if (bad) return fail(visit_err(v, HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes"));
-    v->host_visited.assign((n + 63) / 64, 0);
+    v->host_visited.assign(std::max<uint64_t>(words, 1), 0);
+    if ((r = visit_cuda(v, cudaEventCreate(&v->ev0), "cudaEventCreate")) ||
+        (r = visit_cuda(v, cudaEventCreate(&v->ev1), "cudaEventCreate")))
+        return fail(r);
     if ((r = visit_cuda(v, cudaMemsetAsync(v->d_visited, 0, std::max<uint64_t>(words, 1) * 4, v->stream),
                         "cudaMemsetAsync")) ||
         (r = visit_cuda(v, cudaStreamSynchronize(v->stream), "cudaStreamSynchronize")))
@@ -287,7 +289,6 @@ int hb_visit_reset(hb_visit* v) {
     const uint64_t words = (v->n + 31) / 32;
     VC(v, cudaMemsetAsync(v->d_visited, 0, std::max<uint64_t>(words, 1) * 4, v->stream), "cudaMemsetAsync");
     VC(v, cudaStreamSynchronize(v->stream), "cudaStreamSynchronize");
-    std::fill(v->host_visited.begin(), v->host_visited.end(), 0);
     v->tail = 0;
     return HB_OK;
 }
@@ -311,6 +312,7 @@ int hb_visit_run(hb_visit* v, const uint64_t* roots, size_t nroots, uint64_t max
         const uint64_t nr = std::min<uint64_t>(nroots, std::max<uint64_t>(v->n, 1));
         unsigned long long zero2[3] = {q0, 0, 0};
         VC(v, cudaMemcpyAsync(v->d_cnt, zero2, 3 * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        VC(v, cudaEventRecord(v->ev0, s), "cudaEventRecord");
         for (size_t at = 0; at < nroots; at += nr) {
             const uint64_t k = std::min<uint64_t>(nr, nroots - at);
             VC(v, cudaMemcpyAsync(v->d_roots, r32.data() + at, k * 4, cudaMemcpyHostToDevice, s),
@@ -344,32 +346,26 @@ int hb_visit_run(hb_visit* v, const uint64_t* roots, size_t nroots, uint64_t max
             if (e > b) level_end.push_back(e);
             d++;
         }
+        VC(v, cudaEventRecord(v->ev1, s), "cudaEventRecord");
         VC(v, cudaMemcpyAsync(v->h_cnt, v->d_cnt, 3 * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
         VC(v, cudaStreamSynchronize(s), "cudaStreamSynchronize");
         v->tail = v->h_cnt[0];
         st.known_arcs = v->h_cnt[2];
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, v->ev0, v->ev1);
+        st.device_ms = ms;
     }
     const uint64_t count = v->tail - q0;
     st.visited = count;
     st.levels = level_end.size();
-    // the events into the caller's buffers, and the host mirror of the visited set
-    if (count) {
-        if (!v->h_nodes) {
-            VC(v, cudaMallocHost((void**)&v->h_nodes, std::max<uint64_t>(v->n, 1) * 4), "cudaMallocHost");
-            VC(v, cudaMallocHost((void**)&v->h_preds, std::max<uint64_t>(v->n, 1) * 4), "cudaMallocHost");
-        }
-        VC(v, cudaMemcpyAsync(v->h_nodes, v->d_queue + q0, count * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
-        if (preds)
-            VC(v, cudaMemcpyAsync(v->h_preds, v->d_pred + q0, count * 4, cudaMemcpyDeviceToHost, s),
-               "cudaMemcpyAsync");
-        VC(v, cudaStreamSynchronize(s), "cudaStreamSynchronize");
-        for (uint64_t i = 0; i < count; i++) {
-            const uint32_t x = v->h_nodes[i];
-            v->host_visited[x >> 6] |= 1ull << (x & 63);
-        }
+    // the events into the caller's buffers
+    if (count && (nodes || preds || dists)) {
         const size_t k = std::min<uint64_t>(capacity, count);
-        if (nodes) std::memcpy(nodes, v->h_nodes, k * 4);
-        if (preds) std::memcpy(preds, v->h_preds, k * 4);
+        if (nodes)
+            VC(v, cudaMemcpyAsync(nodes, v->d_queue + q0, k * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        if (preds)
+            VC(v, cudaMemcpyAsync(preds, v->d_pred + q0, k * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        VC(v, cudaStreamSynchronize(s), "cudaStreamSynchronize");
         if (dists) {
             uint64_t lvl = 0;
             for (uint64_t i = 0; i < k; i++) {
@@ -391,10 +387,18 @@ int hb_visit_each(hb_visit* v, const uint64_t* roots, size_t nroots, uint32_t* d
     if ((dist && len != v->n) || (pred && len != v->n))
         return visit_err(v, HB_ERR_INVALID, "dist and pred must hold num_nodes entries");
     std::vector<uint32_t> nodes(v->n), preds(pred ? v->n : 0), ds(v->n);
+    const uint64_t words = (v->n + 31) / 32;
+    if (words) {
+        VC(v, cudaSetDevice(v->device), "cudaSetDevice");
+        VC(v, cudaMemcpyAsync(v->host_visited.data(), v->d_visited, words * 4, cudaMemcpyDeviceToHost,
+                              v->stream),
+           "cudaMemcpyAsync");
+        VC(v, cudaStreamSynchronize(v->stream), "cudaStreamSynchronize");
+    }
     for (size_t i = 0; i < nroots; i++) {
         const uint64_t r = roots[i];
         if (r >= v->n) return visit_err(v, HB_ERR_INVALID, "root " + std::to_string(r) + " >= num_nodes");
-        if ((v->host_visited[r >> 6] >> (r & 63)) & 1) continue;  // seq.rs:130: already visited
+        if ((v->host_visited[r >> 5] >> (r & 31)) & 1) continue;  // seq.rs:130: already visited
         hb_visit_stats st{};
         int rc = hb_visit_run(v, &r, 1, UINT64_MAX, nodes.data(), pred ? preds.data() : nullptr, ds.data(),
                               v->n, &st);
@@ -402,6 +406,7 @@ int hb_visit_each(hb_visit* v, const uint64_t* roots, size_t nroots, uint32_t* d
         for (uint64_t k = 0; k < st.visited; k++) {
             if (dist) dist[nodes[k]] = ds[k];
             if (pred) pred[nodes[k]] = preds[k];
+            v->host_visited[nodes[k] >> 5] |= 1u << (nodes[k] & 31);
         }
     }
     return HB_OK;

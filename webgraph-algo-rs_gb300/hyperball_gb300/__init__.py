@@ -150,7 +150,7 @@ class JobInfo(ctypes.Structure):
 
 class VisitStats(ctypes.Structure):
     _fields_ = [("visited", ctypes.c_uint64), ("levels", ctypes.c_uint64),
-                ("known_arcs", ctypes.c_uint64)]
+                ("known_arcs", ctypes.c_uint64), ("device_ms", ctypes.c_double)]
 
 
 class IterStats(ctypes.Structure):
@@ -1087,7 +1087,8 @@ class ParFair:
                                            dists.ctypes.data, n, ctypes.byref(st)))
         k = st.visited
         return nodes[:k], preds[:k], dists[:k], {"visited": st.visited, "levels": st.levels,
-                                                 "known_arcs": st.known_arcs}
+                                                 "known_arcs": st.known_arcs,
+                                                 "device_ms": st.device_ms}
 
     def visit_each(self, roots, dist=None, pred=None):
         """visit([root]) for each root in order (tests/test_bfv.rs:89-101):
