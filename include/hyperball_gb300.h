@@ -353,6 +353,13 @@ void hb_server_destroy(hb_server* s);
 uint64_t hb_job_footprint(uint64_t num_nodes, uint64_t num_arcs, int log2m);
 /* Last error of a server call on this thread (never NULL). */
 const char* hb_server_last_error(void);
+/* Stepping statistics of a server since its creation: steps run, their wall
+ * time on the stepping thread (planning, launches, synchronisation and
+ * bookkeeping of every running job), the device time of their shared union
+ * launches, and the jobs that took part summed over the steps. No reference
+ * counterpart: a diagnostic of the continuous batching. */
+int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* union_ms,
+                    uint64_t* job_steps);
 
 /* ---- breadth-first visits ------------------------------------------------------ */
 /* The fair parallel breadth-first visit of the reference (ParFair,

@@ -1503,8 +1503,9 @@ bool hb_multi_done(const hb_handle* h) {
     return h->n == 0 || (h->iteration > 0 && (h->modified_counters == 0 || h->iteration >= h->n));
 }
 
-uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays) {
+uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms) {
     if (replays) *replays = m->mc.replays;
+    if (union_ms) *union_ms = m->mc.union_ms;
     return m->mc.steps;
 }
 

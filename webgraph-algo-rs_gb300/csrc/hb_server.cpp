@@ -78,6 +78,8 @@ struct hb_server {
     hb_multi* multi = nullptr;
     cudaStream_t step_stream = nullptr;
     uint64_t next_id = 1, used = 0;
+    uint64_t steps = 0, job_steps = 0; // stepping statistics (hb_server_stats)
+    double step_ms = 0.0;
     uint32_t active = 0;               // admitted and not finished
     bool stopping = false;             // no more admissions
     bool shutdown = false;             // stage threads exit
@@ -194,8 +196,12 @@ static void stepper(hb_server* s) {
         hs.clear();
         for (auto& j : running) hs.push_back(j->h);
         std::string msg;
+        const Clock::time_point t0 = Clock::now();
         const int r = hb_multi_step(s->multi, hs.data(), (uint32_t)hs.size(), msg);
         std::lock_guard<std::mutex> lock(s->mu);
+        s->steps++;
+        s->job_steps += hs.size();
+        s->step_ms += ms_between(t0, Clock::now());
         std::vector<std::shared_ptr<Job>> still;
         for (auto& j : running) {
             if (r) {
@@ -530,3 +536,16 @@ void hb_server_destroy(hb_server* s) {
 }
 
 const char* hb_server_last_error(void) { return t_server_err.c_str(); }
+
+int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* union_ms,
+                    uint64_t* job_steps) {
+    if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (steps) *steps = s->steps;
+    if (step_ms) *step_ms = s->step_ms;
+    if (job_steps) *job_steps = s->job_steps;
+    double ums = 0.0;
+    if (s->multi) hb_multi_steps(s->multi, nullptr, &ums);
+    if (union_ms) *union_ms = ums;
+    return HB_OK;
+}

@@ -261,6 +261,10 @@ EXPORTS = [
     ("hb_server_destroy", None, [_H]),
     ("hb_job_footprint", ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]),
     ("hb_server_last_error", ctypes.c_char_p, []),
+    ("hb_server_stats", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_uint64)]),
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
@@ -946,6 +950,16 @@ class HyperBallServer:
         self._h = h
         self._nodes = {}
         self._borrowed = {}
+
+    def stats(self):
+        """Stepping statistics (hb_server_stats): steps, their wall time on
+        the stepping thread, the device time of the shared union launches,
+        and the job-steps (jobs per step, summed)."""
+        st, sm, um, js = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        _scheck(self._lib.hb_server_stats(self._h, ctypes.byref(st), ctypes.byref(sm),
+                                          ctypes.byref(um), ctypes.byref(js)))
+        return {"steps": st.value, "step_ms": sm.value, "union_ms": um.value,
+                "job_steps": js.value}
 
     def submit(self, graph, log2m, hasher=None, sum_of_distances=False,
                sum_of_inverse_distances=False, transpose_on_device=True, borrow=False):
