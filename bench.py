@@ -72,6 +72,8 @@ def parse_args():
     p.add_argument("--max-active", type=int, default=16, help="served: jobs on the device at once")
     p.add_argument("--sustained-rate", type=float, default=40.0,
                    help="served: a second, lower arrival rate (0: none)")
+    p.add_argument("--setup-threads", type=int, default=0,
+                   help="served: job creation / results threads (0: the server's default)")
     args = p.parse_args()
     set_workload(args)
     return args
@@ -766,7 +768,7 @@ def run_served(args):
 
     with ThreadPoolExecutor(max_workers=host_cores()) as ex:
         graphs = list(ex.map(make, gspecs))
-    server = hb.HyperBallServer(max_active=args.max_active)
+    server = hb.HyperBallServer(max_active=args.max_active, setup_threads=args.setup_threads)
     # warm-up: one job of each log2m
     for l2m in (4, 6, 8):
         j = server.submit(graphs[0], l2m, sum_of_distances=True, sum_of_inverse_distances=True)

@@ -303,6 +303,8 @@ typedef struct hb_server_options {
     uint64_t hbm_budget_bytes; /* device bytes the running jobs may hold together; default 150e9 */
     uint32_t max_active;       /* jobs past admission at once, 1 to 48; default 16 */
     uint32_t keep_registers;   /* 1: keep each finished job's counters for hb_server_get_registers */
+    uint32_t setup_threads;    /* threads that create jobs, and as many that fetch results; 0 = min(max_active, 8) */
+    uint32_t reserved;
 } hb_server_options;
 
 typedef struct hb_job_info {
@@ -356,10 +358,11 @@ const char* hb_server_last_error(void);
 /* Stepping statistics of a server since its creation: steps run, their wall
  * time on the stepping thread (planning, launches, synchronisation and
  * bookkeeping of every running job), the device time of their shared union
- * launches, and the jobs that took part summed over the steps. No reference
- * counterpart: a diagnostic of the continuous batching. */
+ * launches, the jobs that took part summed over the steps, and the host time
+ * the steps spent planning and launching. No reference counterpart: a
+ * diagnostic of the continuous batching. */
 int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* union_ms,
-                    uint64_t* job_steps);
+                    uint64_t* job_steps, double* launch_ms);
 
 /* ---- breadth-first visits ------------------------------------------------------ */
 /* The fair parallel breadth-first visit of the reference (ParFair,

@@ -1166,6 +1166,7 @@ struct MultiCtx {
     std::vector<Shape> seen;
     uint64_t steps = 0, replays = 0;
     double union_ms = 0.0;
+    double host_ms = 0.0, wait_ms = 0.0;  // planning and launches; waiting for the step's end
     std::string err;
 };
 
@@ -1309,6 +1310,7 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
         mc.err = "more than 48 instances in one step";
         return HB_ERR_INVALID;
     }
+    const auto t_start = std::chrono::steady_clock::now();
     std::vector<IterPlan> plans(hs.size());
     MultiCtx::Shape shape;
     for (size_t j = 0; j < hs.size(); j++) {
@@ -1372,11 +1374,15 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
             return r;
         }
     }
+    const auto t_launched = std::chrono::steady_clock::now();
     cudaError_t e = cudaStreamSynchronize(mc.s);
     if (e != cudaSuccess) {
         mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
         return HB_ERR_CUDA;
     }
+    const auto t_done = std::chrono::steady_clock::now();
+    mc.host_ms += std::chrono::duration<double, std::milli>(t_launched - t_start).count();
+    mc.wait_ms += std::chrono::duration<double, std::milli>(t_done - t_launched).count();
     float ms = 0.f;
     cudaEventElapsedTime(&ms, mc.u0, mc.u1);
     mc.union_ms += ms;
@@ -1505,9 +1511,12 @@ bool hb_multi_done(const hb_handle* h) {
     return h->n == 0 || (h->iteration > 0 && (h->modified_counters == 0 || h->iteration >= h->n));
 }
 
-uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms) {
+uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms, double* host_ms,
+                        double* wait_ms) {
     if (replays) *replays = m->mc.replays;
     if (union_ms) *union_ms = m->mc.union_ms;
+    if (host_ms) *host_ms = m->mc.host_ms;
+    if (wait_ms) *wait_ms = m->mc.wait_ms;
     return m->mc.steps;
 }
 

@@ -260,6 +260,8 @@ int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string
 // the handle's run is over: its last iteration modified no counter, or it
 // ran num_nodes iterations (the stop rules of run_until_done, HB:541, HB:559-570)
 bool hb_multi_done(const hb_handle* h);
-// steps run so far, of them replayed from graphs, device time of the shared launches
-uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms);
+// steps run so far, of them replayed from graphs, device time of the shared
+// launches, host time planning and launching, host time waiting for the steps
+uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms, double* host_ms,
+                        double* wait_ms);
 

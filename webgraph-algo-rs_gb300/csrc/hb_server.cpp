@@ -340,7 +340,7 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
     s->stepper = std::thread(stepper, s);
     // creation and results of different jobs overlap (host copies, device
     // set-up kernels on the jobs' own streams) beside the stepping thread
-    const uint32_t workers = std::min<uint32_t>(o.max_active, 8);
+    const uint32_t workers = o.setup_threads ? o.setup_threads : std::min<uint32_t>(o.max_active, 8);
     for (uint32_t i = 0; i < workers; i++) {
         s->creators.emplace_back(creator, s);
         s->finishers.emplace_back(finisher, s);
@@ -538,14 +538,15 @@ void hb_server_destroy(hb_server* s) {
 const char* hb_server_last_error(void) { return t_server_err.c_str(); }
 
 int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* union_ms,
-                    uint64_t* job_steps) {
+                    uint64_t* job_steps, double* launch_ms) {
     if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
     std::lock_guard<std::mutex> lock(s->mu);
     if (steps) *steps = s->steps;
     if (step_ms) *step_ms = s->step_ms;
     if (job_steps) *job_steps = s->job_steps;
-    double ums = 0.0;
-    if (s->multi) hb_multi_steps(s->multi, nullptr, &ums);
+    double ums = 0.0, hms = 0.0;
+    if (s->multi) hb_multi_steps(s->multi, nullptr, &ums, &hms, nullptr);
     if (union_ms) *union_ms = ums;
+    if (launch_ms) *launch_ms = hms;
     return HB_OK;
 }

@@ -128,6 +128,8 @@ class ServerOptions(ctypes.Structure):
         ("hbm_budget_bytes", ctypes.c_uint64),
         ("max_active", ctypes.c_uint32),
         ("keep_registers", ctypes.c_uint32),
+        ("setup_threads", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
     ]
 
 
@@ -264,7 +266,8 @@ EXPORTS = [
     ("hb_server_stats", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_double),
-                                       ctypes.POINTER(ctypes.c_uint64)]),
+                                       ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.POINTER(ctypes.c_double)]),
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
@@ -936,7 +939,7 @@ class HyperBallServer:
     returns for its graph alone."""
 
     def __init__(self, hbm_budget_bytes=150 * 10**9, max_active=16, keep_registers=False,
-                 device=0):
+                 device=0, setup_threads=0):
         lib = load_library()
         self._lib = lib
         o = ServerOptions()
@@ -945,6 +948,7 @@ class HyperBallServer:
         o.max_active = int(max_active)
         o.keep_registers = 1 if keep_registers else 0
         o.device = int(device)
+        o.setup_threads = int(setup_threads)
         h = ctypes.c_void_p()
         _scheck(lib.hb_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h
@@ -956,10 +960,11 @@ class HyperBallServer:
         the stepping thread, the device time of the shared union launches,
         and the job-steps (jobs per step, summed)."""
         st, sm, um, js = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        lm = ctypes.c_double()
         _scheck(self._lib.hb_server_stats(self._h, ctypes.byref(st), ctypes.byref(sm),
-                                          ctypes.byref(um), ctypes.byref(js)))
+                                          ctypes.byref(um), ctypes.byref(js), ctypes.byref(lm)))
         return {"steps": st.value, "step_ms": sm.value, "union_ms": um.value,
-                "job_steps": js.value}
+                "job_steps": js.value, "launch_ms": lm.value}
 
     def submit(self, graph, log2m, hasher=None, sum_of_distances=False,
                sum_of_inverse_distances=False, transpose_on_device=True, borrow=False):
