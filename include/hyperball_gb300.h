@@ -303,7 +303,7 @@ typedef struct hb_server_options {
     uint64_t hbm_budget_bytes; /* device bytes the running jobs may hold together; default 150e9 */
     uint32_t max_active;       /* jobs past admission at once, 1 to 48; default 16 */
     uint32_t keep_registers;   /* 1: keep each finished job's counters for hb_server_get_registers */
-    uint32_t setup_threads;    /* threads that create jobs, and as many that fetch results; 0 = min(max_active, 8) */
+    uint32_t setup_threads;    /* threads that create jobs, and as many that fetch results; 0 = min(max_active, 2) */
     uint32_t reserved;
 } hb_server_options;
 
@@ -447,7 +447,7 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
 
 /* Test hook of the TMA far-gather variant (HB_TMA_GATHER): every bounded
  * mbarrier wait of the handle's union kernel gives up after `polls` polls
- * (0: the default limit), and `extra_tx_bytes` (at most 2^20) are added to
+ * (0: the default limit), and `extra_tx_bytes` (at most 2^19) are added to
  * every expected transaction count, so that no wait can complete and the
  * timeout path runs: the kernel releases the extra bytes, waits (bounded)
  * for its copies in flight, issues no more TMA copies, and the iteration

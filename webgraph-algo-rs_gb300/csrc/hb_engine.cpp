@@ -1923,8 +1923,8 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
 
 int hb_debug_far_wait(hb_handle* h, uint32_t polls, uint32_t extra_tx_bytes) {
     if (!h) return set_err(nullptr, HB_ERR_INVALID, "null handle");
-    if (extra_tx_bytes > (1u << 20))
-        return set_err(h, HB_ERR_INVALID, "extra_tx_bytes must be at most 2^20");
+    if (extra_tx_bytes > (1u << 19))
+        return set_err(h, HB_ERR_INVALID, "extra_tx_bytes must be at most 2^19 (the expected count stays below the 2^20 limit of an mbarrier)");
     h->far_polls = polls;
     h->far_extra_tx = extra_tx_bytes;
     // captured iterations hold the old values: capture again
