@@ -520,19 +520,31 @@ def run_gb300(args):
     sod_pin = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
     harm_pin = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
 
+    phases = {"create": 0.0, "run": 0.0, "results": 0.0, "destroy": 0.0}
+
     def e2e_step():
+        # every call below returns after its device work completed
+        t = [time.perf_counter()]
         hh = (hb.HyperBallBuilder.new(view, logic).transpose_on_device(True)
               .sum_of_distances(True).sum_of_inverse_distances(True).degree_buckets(small, medium)
               .stream(stream.cuda_stream).device(local).build())
+        t.append(time.perf_counter())
         hh.run_until_done()
+        t.append(time.perf_counter())
         nf = hh.neighborhood_function()
         hh.sum_of_distances(out=sod_pin)
         hh.harmonic_centralities(out=harm_pin)
+        t.append(time.perf_counter())
         k = hh.kernel_launches()
         hh.close()
+        t.append(time.perf_counter())
+        for i, name in enumerate(phases):
+            phases[name] += 1e3 * (t[i + 1] - t[i])
         return len(nf), k
 
     e2e_step()  # warm-up
+    for name in phases:
+        phases[name] = 0.0
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -549,6 +561,7 @@ def run_gb300(args):
         "h2d_bytes_per_step": 8 * (n + 1) + 4 * m,
         "d2h_bytes_per_step": 16 * n + 8 * nf_len,
         "ms_per_step": 1e3 * e2e_s / e2e_steps,
+        "phases_ms": {k: v / max(e2e_steps, 1) for k, v in phases.items()},
         "gpu_launches_per_step": e2e_launches // max(e2e_steps, 1),
     }
 
