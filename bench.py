@@ -14,7 +14,9 @@ summed over the iterations (the visited arcs are deterministic). `value` is
 measured with the graph resident in HBM; `e2e` goes through the public API
 from pinned host buffers (hb_create copies the CSR in and builds the transpose
 on the device, then the run, then the neighbourhood function, sums of
-distances and harmonic centralities are read back).
+distances and harmonic centralities are read back). At one GPU the 2^26
+web-like line also carries `rmat24`: the whole line of `--workload rmat` (R-MAT 2^24
+with 2^8 registers per counter), run in a child process after the headline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -58,6 +60,8 @@ def parse_args():
                    help="graph size (2^log2n nodes; default 26 web-like, 24 R-MAT)")
     p.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default: --steps)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-rmat", action="store_true",
+                   help="web-like workload: skip the R-MAT 2^24 run reported beside it (rmat24)")
     p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served", "visit"],
                    default="weblike",
                    help="weblike: the 2^26 web-like graph (default); rmat: R-MAT 2^24 x 16, "
@@ -441,6 +445,13 @@ def run_gb300(args):
 
     for _ in range(args.warmup):
         h.run_until_done()
+    # The union-kernel autotuner times one variant per sampled iteration (at
+    # most one or two per run); the timed runs start once it has chosen for
+    # both kinds of standard iteration, or after as many runs as variants.
+    tuning_runs = 0
+    while -1 in list(h.union_variants_chosen())[:2] and tuning_runs < hb.union_variant_count():
+        h.run_until_done()
+        tuning_runs += 1
     ref_stats = [dict(s) for s in h.iteration_stats()]
     units_per_step = sum(s["visited_arcs"] for s in ref_stats) << LOG2M
     # the run just finished against the oracle's digest of this workload
@@ -591,15 +602,38 @@ def run_gb300(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": workload(args, m, len(ref_stats)),
             "tuning": {"degree_buckets": [small, medium], "bucket_tuning_s": round(t_tune, 2),
-                       "union_variants": variants,
+                       "union_variants": variants, "variant_tuning_runs": tuning_runs,
                        "graph_replayed_iterations": f"{replayed} of {len(st)}"},
             "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e,
             "parity": parity, "clocks": clk, "gpu_launches": launches,
             "iteration_union_ms": [round(s["union_ms"], 3) for s in st],
         }
-        print(json.dumps(line), flush=True)
     ranks.close()
+    if rank == 0 and world == 1 and args.workload == "weblike" and args.log2n == 26 and not args.no_rmat:
+        # the R-MAT 2^24 configuration in its own process, reported beside
+        # the headline; this process's cached device memory is returned first
+        del g
+        hb.release_cached_memory(local)
+        line["rmat24"] = rmat_subrun(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     return 0
+
+
+def rmat_subrun(args):
+    """`bench.py --workload rmat` (R-MAT 2^24 x 16, log2m 8: every figure of
+    its own line, parity against its oracle digest included) as a child
+    process; a failure there fails this run."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--workload", "rmat",
+           "--steps", str(min(args.steps, 5)), "--warmup", str(args.warmup), "--no-cpu-baseline"]
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=ROOT)
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    if r.returncode != 0 or not lines:
+        sys.stderr.write(r.stdout[-2000:] + r.stderr[-4000:])
+        raise RuntimeError(f"the R-MAT 2^24 run failed (exit {r.returncode})")
+    sub = json.loads(lines[-1])
+    sub["command"] = " ".join(["python", "bench.py"] + cmd[2:])
+    return sub
 
 
 # ---------------------------------------------------------------------------
