@@ -447,11 +447,17 @@ def run_gb300(args):
         h.run_until_done()
     # The union-kernel autotuner times one variant per sampled iteration (at
     # most one or two per run); the timed runs start once it has chosen for
-    # both kinds of standard iteration, or after as many runs as variants.
+    # both kinds of standard iteration, or once a run used the same variants
+    # as the run before (a kind of iteration it never samples stays -1).
     tuning_runs = 0
+    used = [s["union_variant"] for s in h.iteration_stats()]
     while -1 in list(h.union_variants_chosen())[:2] and tuning_runs < hb.union_variant_count():
         h.run_until_done()
         tuning_runs += 1
+        now = [s["union_variant"] for s in h.iteration_stats()]
+        if now == used:
+            break
+        used = now
     ref_stats = [dict(s) for s in h.iteration_stats()]
     units_per_step = sum(s["visited_arcs"] for s in ref_stats) << LOG2M
     # the run just finished against the oracle's digest of this workload

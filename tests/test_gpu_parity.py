@@ -102,6 +102,33 @@ def test_staged_kernel_log2m(hb, oracle, log2m, variant):
     lockstep(hb, oracle, g, log2m, variant=variant, buckets=(16, 512))
 
 
+def _hub_graph(hb, seed):
+    """A web-like graph plus hubs of 32,768 to about 60,000 successors: the
+    heavy kernel splits every node above 32,768 arcs into segments."""
+    rng = np.random.default_rng(seed)
+    base = hb.Graph.weblike(60_000, cap=500, window=256, seed=seed)
+    off = np.asarray(base.offsets).astype(np.int64)
+    suc = np.asarray(base.successors).astype(np.uint32)
+    n = base.num_nodes
+    rows = [suc[off[v]:off[v + 1]] for v in range(n)]
+    for v, d in ((11, 59_000), (400, 40_000), (12_345, 32_769), (50_000, 32_000), (7, 16_384)):
+        extra = rng.choice(n, size=d, replace=False).astype(np.uint32)
+        rows[v] = np.unique(np.concatenate([rows[v], extra]))
+    deg = np.array([len(r) for r in rows], dtype=np.uint64)
+    offsets = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint64)
+    return hb.Graph.from_csr(offsets, np.concatenate(rows).astype(np.uint32))
+
+
+@pytest.mark.parametrize("log2m", [4, 6, 8, 10])
+def test_heavy_nodes_split_into_segments(hb, oracle, log2m):
+    """Heavy nodes above 32,768 arcs run as segments on several CTAs whose
+    partial counters the last one merges: the oracle's counters in standard
+    (merging every or only modified successors) and systolic iterations."""
+    g = _hub_graph(hb, seed=log2m)
+    assert int(np.max(np.diff(np.asarray(g.offsets).astype(np.int64)))) > 50_000
+    lockstep(hb, oracle, g, log2m, transpose_on_device=True, buckets=(64, 4096))
+
+
 @pytest.mark.parametrize("variant", STAGED)
 def test_staged_kernel_filtered_rmat(hb, oracle, variant):
     """R-MAT leaves many counters unchanged, so standard iterations merge only

@@ -282,6 +282,10 @@ struct hb_handle {
     uint32_t* d_medium_list = nullptr;          // systolic: medium nodes to check or copy
     uint32_t* d_heavy = nullptr;
     uint64_t n_heavy = 0;
+    uint4* d_heavy_items = nullptr;     // heavy-kernel items (whole nodes or segments)
+    uint64_t n_heavy_items = 0;
+    uint8_t* d_heavy_part = nullptr;    // partial counters of split nodes' segments
+    uint32_t* d_heavy_arrive = nullptr; // arrival counts of split nodes
     hbk::TilePartial* d_partials = nullptr;  // one per tile, then one per heavy block
     uint64_t n_partials = 0;
     double* d_nf_items = nullptr;     // neighbourhood-function part per work item / heavy node
@@ -489,6 +493,43 @@ int device_partition(hb_handle* h, const uint64_t* off0, uint32_t win_nodes, uin
         if ((r = dalloc(h, &h->d_heavy, h->n_heavy))) return r;
         HB_CUDA(h, cudaMemcpyAsync(h->d_heavy, heavy.data(), h->n_heavy * 4, cudaMemcpyHostToDevice,
                                    h->stream));
+        // heavy-kernel items: a node of more than HEAVY_SPLIT arcs becomes
+        // segments of HEAVY_SEG arcs; items by decreasing arcs (ties in list
+        // order), so the longest start first. The key holds 2^32 - 1 - degree.
+        struct Item {
+            uint64_t arcs;
+            uint32_t hi, seg, nseg, slot;
+        };
+        std::vector<Item> items;
+        uint32_t slots = 0;
+        for (uint64_t i = 0; i < h->n_heavy; i++) {
+            const uint64_t d = 0xffffffffull - (keys[i] >> 32);
+            if (d > hbk::HEAVY_SPLIT) {
+                const uint32_t nseg = (uint32_t)((d + hbk::HEAVY_SEG - 1) / hbk::HEAVY_SEG);
+                for (uint32_t k = 0; k < nseg; k++)
+                    items.push_back({std::min<uint64_t>(hbk::HEAVY_SEG, d - (uint64_t)k * hbk::HEAVY_SEG),
+                                     (uint32_t)i, k, nseg, slots});
+                slots += nseg;
+            } else {
+                items.push_back({d, (uint32_t)i, 0, 1, 0});
+            }
+        }
+        std::stable_sort(items.begin(), items.end(),
+                         [](const Item& x, const Item& y) { return x.arcs > y.arcs; });
+        std::vector<uint4> table(items.size());
+        for (size_t k = 0; k < items.size(); k++)
+            table[k] = make_uint4(items[k].hi, items[k].seg, items[k].nseg, items[k].slot);
+        h->n_heavy_items = table.size();
+        if ((r = dalloc(h, &h->d_heavy_items, table.size()))) return r;
+        HB_CUDA(h, cudaMemcpyAsync(h->d_heavy_items, table.data(), table.size() * sizeof(uint4),
+                                   cudaMemcpyHostToDevice, h->stream));
+        if (slots) {
+            if ((r = dalloc(h, &h->d_heavy_part, (size_t)slots * h->stride))) return r;
+            if ((r = dalloc(h, &h->d_heavy_arrive, slots))) return r;
+            HB_CUDA(h, cudaMemsetAsync(h->d_heavy_arrive, 0, (size_t)slots * 4, h->stream));
+        }
+        // host copies are read by the copies above before they return
+        HB_CUDA(h, cudaStreamSynchronize(h->stream));
     }
     HB_CUDA(h, cudaStreamSynchronize(h->stream));
     for (void* p : {(void*)seg_chunks, (void*)seg_heavy, (void*)chunk_at, (void*)heavy_at,
@@ -886,6 +927,10 @@ int enqueue_union(hb_handle* h, const hbk::UnionArgs& a, cudaStream_t s, bool wi
         hbk::UnionArgs ah = a;
         ah.list = h->d_heavy;
         ah.list_len = h->n_heavy;
+        ah.heavy_items = h->d_heavy_items;
+        ah.heavy_len = h->n_heavy_items;
+        ah.heavy_part = h->d_heavy_part;
+        ah.heavy_arrive = h->d_heavy_arrive;
         HB_CUDA(h, cudaEventRecord(h->fork, s));
         HB_CUDA(h, cudaStreamWaitEvent(h->side, h->fork, 0));
         HB_LAUNCH(h, hbk::launch_union_heavy(h->log2m, ah, h->grid_heavy, h->side));
@@ -2257,7 +2302,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
             for (int c = 0; c < kTunedClasses; c++) h->tuner.chosen[c] = it->second[c];
     }
     h->grid_heavy = hbk::heavy_grid(h->log2m, h->device);
-    if ((uint64_t)h->grid_heavy > h->n_heavy + 1) h->grid_heavy = (int)(h->n_heavy + 1);
+    if ((uint64_t)h->grid_heavy > h->n_heavy_items + 1) h->grid_heavy = (int)(h->n_heavy_items + 1);
     h->grid_mark = 8 * hbk::num_sms(h->device);
     // integer totals of the union kernels (atomics) and the summed
     // neighbourhood function

@@ -22,6 +22,10 @@ int load_bvgraph(const std::string& basename, Csr& g, std::string& err, uint64_t
 namespace hbk {
 
 constexpr int MAX_DISCOUNT = 8;
+// heavy nodes with more arcs than HEAVY_SPLIT run as segments of HEAVY_SEG
+// arcs, one CTA each (k_union_heavy)
+constexpr uint64_t HEAVY_SPLIT = 32768;
+constexpr uint64_t HEAVY_SEG = 16384;
 
 // What one tile (or one block of the heavy-node kernel) contributes to an
 // iteration; summed in a fixed order after the union kernels.
@@ -72,6 +76,13 @@ struct UnionArgs {
     const double* ln_table;   // m * ln(m / z), z = 0..m
     const uint32_t* list;     // heavy node list
     uint64_t list_len;
+    // heavy-kernel work items {heavy index, segment, segments, first partial
+    // slot}, and for split nodes the partial counters of their segments and
+    // one arrival count per node (at its first slot; zero between launches)
+    const uint4* heavy_items;
+    uint64_t heavy_len;
+    uint8_t* heavy_part;
+    uint32_t* heavy_arrive;
     const uint32_t* tiles;    // window k = nodes [tiles[k], tiles[k+1])
     uint32_t n_tiles;         // number of windows
     // systolic iterations: the light and medium nodes to check or to copy, in

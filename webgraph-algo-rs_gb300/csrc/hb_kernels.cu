@@ -1249,31 +1249,60 @@ __global__ void k_chunk_items(const uint2* __restrict__ chunks, uint64_t n_chunk
 }
 
 // ---------------------------------------------------------------------------
-// heavy nodes: one CTA per node. Lanes split the successors (G lanes per
-// counter), the per-lane partial counters are merged by a butterfly of
-// shuffles and then across warps through shared memory.
+// heavy nodes: one CTA per work item. An item is a whole heavy node, or, for
+// a node of more than HEAVY_SPLIT arcs, one segment of HEAVY_SEG of its arcs
+// (a single CTA on the largest R-MAT node, 240 K arcs at 2^24, took the whole
+// heavy kernel's time). Lanes split the item's successors (G lanes per
+// counter); the per-lane partial counters are merged by a butterfly of
+// shuffles and then across warps through shared memory. A segment stores its
+// partial counter in the node's slot and counts itself in; the last segment
+// to arrive merges the node's partials (and the node's own counter) and ends
+// the node as a whole node does. The maximum is order independent, so the
+// result is the same whichever segment arrives last.
 // ---------------------------------------------------------------------------
+// chunk c of a partial counter written by another block of this launch (L2,
+// not the non-coherent path)
+template <int LOG2M>
+__device__ __forceinline__ void load_chunk_cg(const uint8_t* base, uint64_t slot, int c,
+                                              uint32_t (&w)[Geo<LOG2M>::NW]) {
+    using Gm = Geo<LOG2M>;
+    const uint4* p = reinterpret_cast<const uint4*>(base + slot * (uint64_t)Gm::COUNTER_BYTES +
+                                                    (uint64_t)c * Gm::CHUNK_BYTES);
+#pragma unroll
+    for (int q = 0; q < Gm::NW / 4; q++) {
+        const uint4 t = __ldcg(p + q);
+        w[4 * q] = t.x;
+        w[4 * q + 1] = t.y;
+        w[4 * q + 2] = t.z;
+        w[4 * q + 3] = t.w;
+    }
+}
+
 template <int LOG2M>
 __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
     using Gm = Geo<LOG2M>;
     constexpr int G = Gm::CHUNKS, NW = Gm::NW, REGS = Gm::CHUNK_REGS;
     constexpr int TEAM = 256, P = TEAM / G, WARPS = TEAM / 32;
     __shared__ uint32_t red[WARPS][G][NW];
+    __shared__ uint32_t s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int tid = threadIdx.x;
     const int p = tid / G, c = tid % G;
     const unsigned leader_mask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
     uint32_t modc = 0, scanned = 0, sarcs = 0, vis = 0;
-    for (uint64_t idx = blockIdx.x; idx < a.list_len; idx += gridDim.x) {
+    for (uint64_t idx = blockIdx.x; idx < a.heavy_len; idx += gridDim.x) {
         double nf = 0.0;
-        const uint64_t v = __ldg(a.list + idx);
+        // {heavy index, segment, segments of the node, the node's first partial slot}
+        const uint4 it = __ldg(a.heavy_items + idx);
+        const uint32_t hi = it.x, seg = it.y, nseg = it.z, slot = it.w;
+        const uint64_t v = __ldg(a.list + hi);
         const uint64_t s0 = __ldg(a.off + v), s1 = __ldg(a.off + v + 1);
+        const uint64_t e0 = s0 + (uint64_t)seg * HEAVY_SEG;
+        const uint64_t e1 = nseg == 1 ? s1 : min(s1, e0 + (uint64_t)HEAVY_SEG);
         const bool scan = !a.systolic || test_bit(a.mbc, v);
         if (scan) {
-            NodeSums ns{};
-            if (tid == 0) ns = load_sums(a, (uint32_t)v);
             uint32_t prev[NW], acc[NW];
-            if (p == 0) {
+            if (p == 0 && seg == 0) {
                 load_chunk<LOG2M>(a.curr, v, c, prev);
 #pragma unroll
                 for (int i = 0; i < NW; i++) acc[i] = prev[i];
@@ -1281,7 +1310,7 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
 #pragma unroll
                 for (int i = 0; i < NW; i++) acc[i] = prev[i] = 0u;
             }
-            gather_rolling<LOG2M>(a, (uint32_t)v, c, s0 + p, s1, P, !a.gather_all, acc, 0);
+            gather_rolling<LOG2M>(a, (uint32_t)v, c, e0 + p, e1, P, !a.gather_all, acc, 0);
             __syncwarp();
 #pragma unroll
             for (int off = G; off < 32; off <<= 1) {
@@ -1302,6 +1331,38 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                     for (int i = 0; i < NW; i++) y[i] = red[w][c][i];
                     merge_chunk<REGS>(acc, y);
                 }
+            }
+            bool last = true;
+            if (nseg > 1) {
+                // this segment's partial into its slot, then count it in
+                if (warp == 0 && lane < G) {
+                    store_chunk<LOG2M>(a.heavy_part, (uint64_t)slot + seg, c, acc);
+                    __threadfence();
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    const uint32_t before = atomicAdd(a.heavy_arrive + slot, 1u);
+                    s_last = before == nseg - 1;
+                    __threadfence();
+                }
+                __syncthreads();
+                last = s_last != 0;
+                if (last && warp == 0 && lane < G) {
+                    // the node's own counter and every segment's partial
+                    load_chunk<LOG2M>(a.curr, v, c, prev);
+#pragma unroll
+                    for (int i = 0; i < NW; i++) acc[i] = prev[i];
+                    for (uint32_t k = 0; k < nseg; k++) {
+                        uint32_t y[NW];
+                        load_chunk_cg<LOG2M>(a.heavy_part, (uint64_t)slot + k, c, y);
+                        merge_chunk<REGS>(acc, y);
+                    }
+                    if (lane == 0) a.heavy_arrive[slot] = 0u;  // ready for the next launch
+                }
+            }
+            if (last && warp == 0 && lane < G) {
+                NodeSums ns{};
+                if (c == 0) ns = load_sums(a, (uint32_t)v);
                 const bool changed = commit_node<LOG2M>(a, v, c, leader_mask, prev, acc);
                 if (c == 0) {
                     scanned++;
@@ -1312,9 +1373,9 @@ __global__ void __launch_bounds__(256) k_union_heavy(UnionArgs a) {
                     }
                 }
                 finish_node<LOG2M>(a, (uint32_t)v, c, leader_mask, acc, changed, ns, nf, vis);
-                if (c == 0) a.nf_items[a.heavy_item_base + idx] = nf;
+                if (c == 0) a.nf_items[a.heavy_item_base + hi] = nf;
             }
-        } else if (test_bit(a.curr_mod, v)) {
+        } else if (seg == 0 && test_bit(a.curr_mod, v)) {
             if (tid < G) {
                 uint32_t prev[NW];
                 load_chunk<LOG2M>(a.curr, v, c, prev);
@@ -1459,22 +1520,40 @@ __global__ void k_sum_f64(const double* __restrict__ in, uint64_t count, double*
 // and the neighbourhood function (sum of the cached estimates) of the
 // iteration just run; one block per running instance, fixed order
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_inst_stats(const uint32_t* __restrict__ next_mod,
-                                                    const double* __restrict__ est,
-                                                    const uint64_t* __restrict__ starts, uint32_t count,
-                                                    unsigned long long* __restrict__ mods,
-                                                    double* __restrict__ nfs) {
-    // one block per instance, a fixed order: thread t sums nodes b + t,
-    // b + t + 256, ..., then a fixed tree. An instance whose previous
-    // iteration modified nothing has stopped: its values stay.
-    __shared__ double s_nf[256];
-    __shared__ unsigned long long s_mc[256];
+constexpr int INST_THREADS = 512;
+__global__ void __launch_bounds__(INST_THREADS) k_inst_stats(const uint32_t* __restrict__ next_mod,
+                                                             const double* __restrict__ est,
+                                                             const uint64_t* __restrict__ starts,
+                                                             uint32_t count,
+                                                             unsigned long long* __restrict__ mods,
+                                                             double* __restrict__ nfs) {
+    // One block per instance, a fixed order: thread t keeps four running
+    // sums (nodes b + t + 512 (4j + k) go to sum k, so four loads are in
+    // flight), adds them as (s0 + s1) + (s2 + s3), then a fixed tree. (With
+    // one sum, 256 threads, the largest instance's block took most of the
+    // kernel's time.) An instance whose previous iteration modified nothing
+    // has stopped: its values stay.
+    constexpr int T = INST_THREADS;
+    __shared__ double s_nf[T];
+    __shared__ unsigned long long s_mc[T];
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
         if (mods[i] == 0) continue;  // uniform over the block
         __syncthreads();
         const uint64_t b = __ldg(starts + i), e = __ldg(starts + i + 1);
-        double sum = 0.0;
-        for (uint64_t v = b + threadIdx.x; v < e; v += blockDim.x) sum = __dadd_rn(sum, est[v]);
+        double s4[4] = {0.0, 0.0, 0.0, 0.0};
+        uint64_t v = b + threadIdx.x;
+        for (; v + 3 * T < e; v += 4 * T) {
+            double x[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) x[k] = __ldg(est + v + k * T);
+#pragma unroll
+            for (int k = 0; k < 4; k++) s4[k] = __dadd_rn(s4[k], x[k]);
+        }
+        // at most three nodes left for this thread
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if (v + k * T < e) s4[k] = __dadd_rn(s4[k], __ldg(est + v + k * T));
+        const double sum = __dadd_rn(__dadd_rn(s4[0], s4[1]), __dadd_rn(s4[2], s4[3]));
         unsigned long long mc = 0;
         if (e > b) {
             const uint64_t w0 = b >> 5, w1 = (e - 1) >> 5;
@@ -2206,7 +2285,8 @@ int launch_inst_stats(const uint32_t* next_mod, const double* est, const uint64_
                       uint32_t count, unsigned long long* mods, double* nfs, void* stream) {
     const int grid = (int)std::min<uint64_t>((uint64_t)count, 16384);
     ++t_launches;
-    if (grid) k_inst_stats<<<grid, 256, 0, (cudaStream_t)stream>>>(next_mod, est, starts, count, mods, nfs);
+    if (grid)
+        k_inst_stats<<<grid, INST_THREADS, 0, (cudaStream_t)stream>>>(next_mod, est, starts, count, mods, nfs);
     return (int)cudaGetLastError();
 }
 
