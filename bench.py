@@ -330,9 +330,13 @@ def cpu_bounded_run(offsets, successors, t_offsets, t_successors, budget_s=30.0)
                             t_successors=t_successors, sod=True, harm=True, threads=cores)
     t = time.perf_counter()
     o.init()
-    visited, iters = 0, 0
-    while time.perf_counter() - t < budget_s:
+    visited, iters, last = 0, 0, 0.0
+    # at least one iteration; another only if one more like the last still
+    # ends within the budget
+    while iters == 0 or time.perf_counter() - t + last < budget_s:
+        t_it = time.perf_counter()
         st = o.iterate()
+        last = time.perf_counter() - t_it
         visited += st["visited_arcs"]
         iters += 1
         if st["modified"] == 0:
@@ -843,7 +847,9 @@ def run_served(args):
     wall, infos, late = served_stream(server, graphs, jobs)
     main_run = summary(wall, infos, late, jobs)
     st1 = server.stats()
-    main_run["stepping"] = {k: st1[k] - st0[k] for k in st1}
+    main_run["stepping"] = {k: st1[k] - st0[k] for k in st1 if k != "device_ms"}
+    main_run["stepping"]["device_ms"] = {k: st1["device_ms"][k] - st0["device_ms"][k]
+                                         for k in st1["device_ms"]}
     # a lower arrival rate, one the device can keep up with
     sustained = None
     if args.sustained_rate > 0:

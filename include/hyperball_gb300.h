@@ -363,6 +363,14 @@ const char* hb_server_last_error(void);
  * diagnostic of the continuous batching. */
 int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* union_ms,
                     uint64_t* job_steps, double* launch_ms);
+/* Where the steps' time went, summed over the steps: device time from a
+ * step's first launch to its union part (the jobs' pre-union kernels), of
+ * the union part (the shared launch and the jobs' heavy-node kernels), and
+ * from its end to the step's last launch (the post-union kernels and the
+ * totals' copies); host time planning and launching, and waiting for the
+ * steps to end. No reference counterpart: a diagnostic. */
+int hb_server_step_times(hb_server* s, double* pre_ms, double* union_ms, double* post_ms,
+                         double* host_ms, double* wait_ms);
 
 /* ---- breadth-first visits ------------------------------------------------------ */
 /* The fair parallel breadth-first visit of the reference (ParFair,

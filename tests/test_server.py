@@ -52,6 +52,12 @@ def test_served_jobs_equal_jobs_alone(max_active, borrow):
         np.testing.assert_allclose(s.sum_of_distances(j), want["sod"], rtol=RTOL)
         np.testing.assert_allclose(s.harmonic_centralities(j), want["harm"], rtol=RTOL)
         s.release(j)
+    st = s.stats()
+    assert st["steps"] > 0 and st["job_steps"] >= st["steps"]
+    dev = st["device_ms"]
+    assert dev["union"] == pytest.approx(st["union_ms"]) and dev["union"] > 0
+    assert dev["pre"] >= 0 and dev["post"] >= 0 and st["wait_ms"] > 0
+    assert dev["pre"] + dev["union"] + dev["post"] <= st["step_ms"] * 1.05
     s.close()
 
 

@@ -86,6 +86,16 @@ cudaError_t lib_pool(int device, cudaMemPool_t* out) {
     return cudaSuccess;
 }
 
+// A non-blocking stream at the device's highest priority: its blocks are
+// scheduled ahead of pending blocks of default-priority streams (the job
+// server's creation work runs at the default priority beside the steps).
+cudaError_t high_priority_stream(cudaStream_t* s) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return e;
+    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, greatest);
+}
+
 cudaError_t pool_alloc(int device, void** p, size_t bytes, cudaStream_t s) {
     cudaMemPool_t pool = nullptr;
     cudaError_t e = lib_pool(device, &pool);
@@ -564,13 +574,27 @@ bool check_view(const hb_graph_view* g, std::string& why) {
 
 int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t** d_succ) {
     int r;
+    // HB_TRACE: the allocations' host time and the copies' device time
+    const bool trace = std::getenv("HB_TRACE") != nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
     if ((r = dalloc(h, d_off, g->num_nodes + 1))) return r;
     if ((r = dalloc(h, d_succ, g->num_arcs))) return r;
+    const auto t1 = std::chrono::steady_clock::now();
+    if (trace) cudaEventRecord(h->ev[0], h->stream);
     HB_CUDA(h, cudaMemcpyAsync(*d_off, g->offsets, (g->num_nodes + 1) * 8, cudaMemcpyHostToDevice,
                                h->stream));
     if (g->num_arcs)
         HB_CUDA(h, cudaMemcpyAsync(*d_succ, g->successors, g->num_arcs * 4, cudaMemcpyHostToDevice,
                                    h->stream));
+    if (trace) {
+        cudaEventRecord(h->ev[1], h->stream);
+        cudaEventSynchronize(h->ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+        std::fprintf(stderr, "hb_create   allocations %.2f ms (host), copies %.2f ms (device), %.2f ms (host)\n",
+                     std::chrono::duration<double, std::milli>(t1 - t0).count(), ms,
+                     std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count());
+    }
     // reject decreasing offsets before any kernel sizes work by them (the
     // successors are checked where they are renumbered)
     int* d_bad = nullptr;
@@ -892,7 +916,12 @@ int enqueue_pre(hb_handle* h, hbk::UnionArgs& a, bool first_systolic, cudaStream
     HB_CUDA(h, cudaMemsetAsync(h->d_partials, 0, h->n_partials * sizeof(hbk::TilePartial), s));
     HB_CUDA(h, cudaMemsetAsync(h->d_nf_items, 0, (h->n_chunks + h->n_heavy) * sizeof(double), s));
     HB_CUDA(h, cudaMemsetAsync(h->d_cursor, 0, sizeof(unsigned long long), s));
-    HB_CUDA(h, cudaMemcpyAsync(h->d_ic, h->h_ic, sizeof(hbk::IterConsts), cudaMemcpyHostToDevice, s));
+    // the per-iteration constants and, after the union, the totals move
+    // between the pinned host blocks and the device by a small kernel, not by
+    // the copy engines: a served job's step would otherwise queue behind the
+    // other jobs' CSR uploads and result downloads
+    HB_LAUNCH(h, hbk::launch_copy_u64(reinterpret_cast<const uint64_t*>(h->h_ic),
+                                      reinterpret_cast<uint64_t*>(h->d_ic), sizeof(hbk::IterConsts) / 8, s));
     if (h->systolic && h->n_tiles) {
         // the light and medium nodes to check or to copy
         HB_LAUNCH(h, hbk::launch_work_lists(a.mbc, a.curr_mod, h->d_medium_bits, h->d_light_bits, n,
@@ -967,10 +996,13 @@ int enqueue_post(hb_handle* h, const hbk::UnionArgs& a, cudaStream_t s, bool ext
     if (n_inst) {
         HB_LAUNCH(h, hbk::launch_inst_stats(h->d_bits[h->mod_cur ^ 1], h->d_est, h->d_inst_start,
                                             (uint32_t)n_inst, h->d_inst_mod, h->d_inst_nf, s));
-        HB_CUDA(h, cudaMemcpyAsync(h->h_inst_mod, h->d_inst_mod, n_inst * 8, cudaMemcpyDeviceToHost, s));
-        HB_CUDA(h, cudaMemcpyAsync(h->h_inst_sum, h->d_inst_nf, n_inst * 8, cudaMemcpyDeviceToHost, s));
+        HB_LAUNCH(h, hbk::launch_copy_u64(reinterpret_cast<const uint64_t*>(h->d_inst_mod),
+                                          reinterpret_cast<uint64_t*>(h->h_inst_mod), n_inst, s));
+        HB_LAUNCH(h, hbk::launch_copy_u64(reinterpret_cast<const uint64_t*>(h->d_inst_nf),
+                                          reinterpret_cast<uint64_t*>(h->h_inst_sum), n_inst, s));
     }
-    HB_CUDA(h, cudaMemcpyAsync(h->h_tot, h->d_partials, sizeof(hbk::TilePartial), cudaMemcpyDeviceToHost, s));
+    HB_LAUNCH(h, hbk::launch_copy_u64(reinterpret_cast<const uint64_t*>(h->d_partials),
+                                      reinterpret_cast<uint64_t*>(h->h_tot), sizeof(hbk::TilePartial) / 8, s));
     HB_CUDA(h, rec(h->ev[3]));
     return HB_OK;
 }
@@ -1191,7 +1223,8 @@ struct MultiCtx {
     // the shared launch's job table (its kernel parameters)
     std::unique_ptr<hbk::JobsArgs> jobs;
     int grid = 1;
-    cudaEvent_t u0 = nullptr, u1 = nullptr;
+    cudaEvent_t u0 = nullptr, u1 = nullptr;  // around the union part (shared launch, heavy kernels)
+    cudaEvent_t b0 = nullptr, b1 = nullptr;  // around the whole step
     // a handle with a stream of its own runs its pre and post parts there, so
     // that the small kernels of different handles overlap (steps launched
     // directly, not captured)
@@ -1211,6 +1244,7 @@ struct MultiCtx {
     std::vector<Shape> seen;
     uint64_t steps = 0, replays = 0;
     double union_ms = 0.0;
+    double pre_ms = 0.0, post_ms = 0.0;   // device time before and after the union part
     double host_ms = 0.0, wait_ms = 0.0;  // planning and launches; waiting for the step's end
     std::string err;
 };
@@ -1231,6 +1265,8 @@ static void multi_free(MultiCtx& mc) {
     mc.jobs.reset();
     if (mc.u0) cudaEventDestroy(mc.u0);
     if (mc.u1) cudaEventDestroy(mc.u1);
+    if (mc.b0) cudaEventDestroy(mc.b0);
+    if (mc.b1) cudaEventDestroy(mc.b1);
     for (int j = 0; j < 64; j++) {
         if (mc.fork_ev[j]) cudaEventDestroy(mc.fork_ev[j]);
         if (mc.join_ev[j]) cudaEventDestroy(mc.join_ev[j]);
@@ -1238,7 +1274,7 @@ static void multi_free(MultiCtx& mc) {
     }
     if (mc.cap) cudaStreamDestroy(mc.cap);
     mc.d_cursor = nullptr;
-    mc.u0 = mc.u1 = nullptr;
+    mc.u0 = mc.u1 = mc.b0 = mc.b1 = nullptr;
     mc.cap = nullptr;
 }
 
@@ -1250,6 +1286,8 @@ static int multi_init(MultiCtx& mc, int device, cudaStream_t s) {
     mc.jobs.reset(new hbk::JobsArgs());
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u0);
     if (e == cudaSuccess) e = cudaEventCreate(&mc.u1);
+    if (e == cudaSuccess) e = cudaEventCreate(&mc.b0);
+    if (e == cudaSuccess) e = cudaEventCreate(&mc.b1);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mc.cap, cudaStreamNonBlocking);
     for (int j = 0; j < 64 && e == cudaSuccess; j++) {
         e = cudaEventCreateWithFlags(&mc.fork_ev[j], cudaEventDisableTiming);
@@ -1286,6 +1324,7 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
         mc.err = std::string("multi-instance step: ") + cudaGetErrorString(e);
         return HB_ERR_CUDA;
     };
+    if (cudaError_t e = rec(mc.b0); e != cudaSuccess) return fail(e);
     for (size_t j = 0; j < hs.size(); j++) {
         const cudaStream_t y = own(j) ? hs[j]->stream : x;
         if (y != x)
@@ -1344,6 +1383,7 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
         if (y != x)
             if (cudaError_t e = join(j); e != cudaSuccess) return fail(e);
     }
+    if (cudaError_t e = rec(mc.b1); e != cudaSuccess) return fail(e);
     return HB_OK;
 }
 
@@ -1428,9 +1468,13 @@ static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
     const auto t_done = std::chrono::steady_clock::now();
     mc.host_ms += std::chrono::duration<double, std::milli>(t_launched - t_start).count();
     mc.wait_ms += std::chrono::duration<double, std::milli>(t_done - t_launched).count();
-    float ms = 0.f;
+    float ms = 0.f, pre = 0.f, post = 0.f;
     cudaEventElapsedTime(&ms, mc.u0, mc.u1);
+    cudaEventElapsedTime(&pre, mc.b0, mc.u0);
+    cudaEventElapsedTime(&post, mc.u1, mc.b1);
     mc.union_ms += ms;
+    mc.pre_ms += pre;
+    mc.post_ms += post;
     mc.steps++;
     for (size_t j = 0; j < hs.size(); j++) {
         int r = iter_finish(hs[j], plans[j], exec != nullptr, ms, nullptr);
@@ -1545,6 +1589,13 @@ int hb_multi_start(hb_handle* h) {
     return do_init(h);
 }
 
+int hb_multi_set_stream(hb_handle* h, void* stream) {
+    HB_CUDA(h, cudaSetDevice(h->device));
+    HB_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->stream = (cudaStream_t)stream;
+    return HB_OK;
+}
+
 int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err) {
     std::vector<hb_handle*> v(hs, hs + count);
     int r = multi_iterate(v, m->mc);
@@ -1557,9 +1608,11 @@ bool hb_multi_done(const hb_handle* h) {
 }
 
 uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms, double* host_ms,
-                        double* wait_ms) {
+                        double* wait_ms, double* pre_ms, double* post_ms) {
     if (replays) *replays = m->mc.replays;
     if (union_ms) *union_ms = m->mc.union_ms;
+    if (pre_ms) *pre_ms = m->mc.pre_ms;
+    if (post_ms) *post_ms = m->mc.post_ms;
     if (host_ms) *host_ms = m->mc.host_ms;
     if (wait_ms) *wait_ms = m->mc.wait_ms;
     return m->mc.steps;
@@ -2016,12 +2069,20 @@ const char* hb_last_error(const hb_handle* h) { return h ? h->err.c_str() : g_gl
 // to stderr (the reference's progress-logger role for building).
 struct PhaseTrace {
     bool on = std::getenv("HB_TRACE") != nullptr;
+    int device = -1;  // once known: the library pool's reserved and used bytes too
     std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
     void mark(const char* phase) {
         if (!on) return;
         const auto now = std::chrono::steady_clock::now();
-        std::fprintf(stderr, "hb_create %-28s %8.2f ms\n", phase,
-                     std::chrono::duration<double, std::milli>(now - t).count());
+        uint64_t reserved = 0, used = 0;
+        cudaMemPool_t pool = nullptr;
+        if (device >= 0 && lib_pool(device, &pool) == cudaSuccess) {
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+        }
+        std::fprintf(stderr, "hb_create %-28s %8.2f ms   pool %.2f GB reserved, %.2f GB used\n", phase,
+                     std::chrono::duration<double, std::milli>(now - t).count(), reserved / 1e9,
+                     used / 1e9);
         t = now;
     }
 };
@@ -2120,7 +2181,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         }
     if ((r = cuda_err(hp, cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming), "cudaEventCreate")) ||
         (r = cuda_err(hp, cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming), "cudaEventCreate")) ||
-        (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking), "cudaStreamCreate")) ||
+        (r = cuda_err(hp, high_priority_stream(&h->side), "cudaStreamCreate")) ||
         (r = cuda_err(hp, cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking), "cudaStreamCreate")) ||
         (r = cuda_err(hp, pinned_alloc((void**)&h->h_ic, sizeof(hbk::IterConsts)), "cudaMallocHost")) ||
         (r = cuda_err(hp, pinned_alloc((void**)&h->h_tot, sizeof(hbk::TilePartial)), "cudaMallocHost"))) {
@@ -2158,6 +2219,7 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         hbk::chunk_nodes(h->log2m, &per_light, &per_medium);
         uint64_t* off0 = nullptr;
         uint32_t* succ0 = nullptr;
+        trace.device = h->device;
         trace.mark("setup");
         if ((r = upload_csr(hp, graph, &off0, &succ0))) return fail(r);
         trace.mark("CSR upload + check");
@@ -2257,16 +2319,25 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         std::vector<double> lnt(mm + 1, 0.0);
         const double mf = (double)mm;
         for (uint64_t z = 1; z <= mm; z++) lnt[z] = mf * std::log(mf / (double)z);
+        // Host-to-device copies of the handle go on its own stream, and are
+        // waited for: a plain cudaMemcpy from pageable memory may return
+        // before its DMA lands and orders nothing on the handle's
+        // non-blocking streams (the init kernel once read a table that was
+        // still on its way: every initial estimate 0 in a served job).
         if ((r = dalloc(hp, &h->d_lnt, mm + 1))) return fail(r);
-        if ((r = cuda_err(hp, cudaMemcpy(h->d_lnt, lnt.data(), (mm + 1) * 8, cudaMemcpyHostToDevice),
-                          "cudaMemcpy")))
+        if ((r = cuda_err(hp, cudaMemcpyAsync(h->d_lnt, lnt.data(), (mm + 1) * 8, cudaMemcpyHostToDevice,
+                                              h->stream),
+                          "cudaMemcpyAsync")))
             return fail(r);
+        if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     }
     if (o.weights) {
         if ((r = dalloc(hp, &h->d_weights, n))) return fail(r);
-        if ((r = cuda_err(hp, cudaMemcpy(h->d_weights, o.weights, n * 8, cudaMemcpyHostToDevice),
-                          "cudaMemcpy")))
+        if ((r = cuda_err(hp, cudaMemcpyAsync(h->d_weights, o.weights, n * 8, cudaMemcpyHostToDevice,
+                                              h->stream),
+                          "cudaMemcpyAsync")))
             return fail(r);
+        if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     }
     trace.mark("state arrays");
     h->grid_tile = hbk::tile_grid(h->log2m, h->device, 0);

@@ -129,7 +129,12 @@ struct InitArgs {
     int* any31;               // set to 1 when an initial register holds 31
 };
 
+static_assert(sizeof(IterConsts) % 8 == 0 && sizeof(TilePartial) % 8 == 0, "copied as 64-bit words");
+
 // Launchers (hb_kernels.cu). All return cudaError_t as int.
+// dst[i] = src[i], i < n, by a kernel (either side may be page-locked host
+// memory, which the device reads and writes through unified addressing)
+int launch_copy_u64(const uint64_t* src, uint64_t* dst, uint64_t n, void* stream);
 int launch_init(int log2m, const InitArgs& a, void* stream);
 // device counters (one byte per register) -> the reference's packed layout,
 // in caller node order (inv: caller node -> device node)
@@ -267,12 +272,15 @@ void hb_multi_destroy(hb_multi* m);
 // hb_init of a handle that will be stepped (its own stream, synchronous)
 int hb_multi_start(hb_handle* h);
 // one iteration of each of the count handles (count <= MAX_JOBS)
+// moves the handle's later work to `stream` (its earlier work is waited for)
+int hb_multi_set_stream(hb_handle* h, void* stream);
 int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err);
 // the handle's run is over: its last iteration modified no counter, or it
 // ran num_nodes iterations (the stop rules of run_until_done, HB:541, HB:559-570)
 bool hb_multi_done(const hb_handle* h);
-// steps run so far, of them replayed from graphs, device time of the shared
-// launches, host time planning and launching, host time waiting for the steps
+// steps run so far, of them replayed from graphs, device time of the union
+// parts (shared launch and heavy kernels), host time planning and launching,
+// host time waiting for the steps, device time before and after the union parts
 uint64_t hb_multi_steps(const hb_multi* m, uint64_t* replays, double* union_ms, double* host_ms,
-                        double* wait_ms);
+                        double* wait_ms, double* pre_ms, double* post_ms);
 

@@ -2273,6 +2273,19 @@ int launch_pack_counters(int log2m, const uint8_t* src, const uint32_t* inv, uin
 #undef CALL
 }
 
+__global__ void k_copy_u64(const uint64_t* src, uint64_t* dst, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+int launch_copy_u64(const uint64_t* src, uint64_t* dst, uint64_t n, void* stream) {
+    if (n == 0) return 0;
+    const int grid = (int)std::min<uint64_t>((n + 255) / 256, 1024);
+    ++t_launches;
+    k_copy_u64<<<grid, 256, 0, (cudaStream_t)stream>>>(src, dst, n);
+    return (int)cudaGetLastError();
+}
+
 int launch_add_indeg(unsigned long long* rows, const uint32_t* indeg, uint64_t n, void* stream) {
     if (n == 0) return 0;
     const int grid = (int)std::min<uint64_t>((n + 255) / 256, 8192);

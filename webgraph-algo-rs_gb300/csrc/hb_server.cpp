@@ -6,14 +6,16 @@
 // slot is free (at most max_active jobs past admission) and its estimated
 // device footprint fits the budget next to the admitted jobs. Admitted jobs
 // go through three stages, each with its own host thread(s):
-//   creation  (up to 8 threads) hb_create on the job's own stream: CSR upload,
-//                            partition, renumbering, transpose;
+//   creation  (setup_threads, default 2) hb_create on the job's own stream:
+//                            CSR upload, partition, renumbering, transpose;
+//                            its steps and results then run on a stream of
+//                            the highest priority;
 //   stepping  (one thread)   every running job advances one iteration per
 //                            step, and the union work of all of them runs as
 //                            one kernel launch (hb_multi_step); a job created
 //                            meanwhile joins at the next step, a finished one
 //                            leaves after the step that stopped it;
-//   results   (up to 8 threads) neighbourhood function, sums and registers to
+//   results   (as many threads) neighbourhood function, sums and registers to
 //                            the host, handle destroyed, budget released.
 // So requests that arrive while others run are admitted as slots and memory
 // free up, and their iterations interleave in the shared kernel. Latency is
@@ -42,7 +44,8 @@ using Clock = std::chrono::steady_clock;
 struct Job {
     uint64_t id = 0;
     hb_handle* h = nullptr;           // from creation to the results stage
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;    // creation, at the default priority
+    cudaStream_t run_stream = nullptr; // steps and results, at the highest priority
     Csr graph;                // the copied graph (hb_server_submit)
     hb_graph_view borrowed{}; // the caller's graph (hb_server_submit_borrowed), else empty
     bool is_borrowed = false;
@@ -154,11 +157,27 @@ static void creator(hb_server* s) {
             r = hb_multi_start(job->h);
             if (r) msg = hb_last_error(job->h);
         }
+        if (!r) {
+            // the job's pre- and post-union kernels then go ahead of other
+            // jobs' creation work waiting for the SMs
+            int least = 0, greatest = 0;
+            if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+                cudaStreamCreateWithPriority(&job->run_stream, cudaStreamNonBlocking, greatest) !=
+                    cudaSuccess) {
+                cudaGetLastError();
+                r = HB_ERR_CUDA;
+                msg = "cudaStreamCreate failed";
+            } else if ((r = hb_multi_set_stream(job->h, job->run_stream))) {
+                msg = hb_last_error(job->h);
+            }
+        }
         if (r) {
             if (job->h) hb_destroy(job->h);
             job->h = nullptr;
             if (job->stream) cudaStreamDestroy(job->stream);
             job->stream = nullptr;
+            if (job->run_stream) cudaStreamDestroy(job->run_stream);
+            job->run_stream = nullptr;
             job_done(s, job, r, msg);
             continue;
         }
@@ -269,6 +288,8 @@ static void finisher(hb_server* s) {
         job->h = nullptr;
         if (job->stream) cudaStreamDestroy(job->stream);
         job->stream = nullptr;
+        if (job->run_stream) cudaStreamDestroy(job->run_stream);
+        job->run_stream = nullptr;
         job_done(s, job, r, msg);
     }
 }
@@ -324,7 +345,12 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0 && cudaSetDevice(o.device) == cudaSuccess) {
         std::string err;
-        cudaError_t ce = cudaStreamCreateWithFlags(&s->step_stream, cudaStreamNonBlocking);
+        // the steps run at the device's highest stream priority, the jobs'
+        // creation at the default one
+        int least = 0, greatest = 0;
+        cudaError_t ce = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (ce == cudaSuccess)
+            ce = cudaStreamCreateWithPriority(&s->step_stream, cudaStreamNonBlocking, greatest);
         int r = ce == cudaSuccess ? hb_multi_create(o.device, s->step_stream, &s->multi, err) : HB_ERR_CUDA;
         if (r) {
             cudaGetLastError();
@@ -549,8 +575,22 @@ int hb_server_stats(hb_server* s, uint64_t* steps, double* step_ms, double* unio
     if (step_ms) *step_ms = s->step_ms;
     if (job_steps) *job_steps = s->job_steps;
     double ums = 0.0, hms = 0.0;
-    if (s->multi) hb_multi_steps(s->multi, nullptr, &ums, &hms, nullptr);
+    if (s->multi) hb_multi_steps(s->multi, nullptr, &ums, &hms, nullptr, nullptr, nullptr);
     if (union_ms) *union_ms = ums;
     if (launch_ms) *launch_ms = hms;
+    return HB_OK;
+}
+
+int hb_server_step_times(hb_server* s, double* pre_ms, double* union_ms, double* post_ms,
+                         double* host_ms, double* wait_ms) {
+    if (!s) return server_err(HB_ERR_INVALID, "server is NULL");
+    std::lock_guard<std::mutex> lock(s->mu);
+    double pre = 0.0, uni = 0.0, post = 0.0, host = 0.0, wait = 0.0;
+    if (s->multi) hb_multi_steps(s->multi, nullptr, &uni, &host, &wait, &pre, &post);
+    if (pre_ms) *pre_ms = pre;
+    if (union_ms) *union_ms = uni;
+    if (post_ms) *post_ms = post;
+    if (host_ms) *host_ms = host;
+    if (wait_ms) *wait_ms = wait;
     return HB_OK;
 }

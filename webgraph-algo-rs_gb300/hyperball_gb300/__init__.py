@@ -268,6 +268,7 @@ EXPORTS = [
                                        ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.POINTER(ctypes.c_double)]),
+    ("hb_server_step_times", ctypes.c_int, [_H] + [ctypes.POINTER(ctypes.c_double)] * 5),
     ("hb_device_transpose", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
@@ -956,15 +957,23 @@ class HyperBallServer:
         self._borrowed = {}
 
     def stats(self):
-        """Stepping statistics (hb_server_stats): steps, their wall time on
-        the stepping thread, the device time of the shared union launches,
-        and the job-steps (jobs per step, summed)."""
+        """Stepping statistics (hb_server_stats, hb_server_step_times):
+        steps, their wall time on the stepping thread, the device time of the
+        union parts, the job-steps (jobs per step, summed), and where the
+        steps' time went (device time before, in and after the union parts;
+        host time launching and waiting)."""
         st, sm, um, js = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
         lm = ctypes.c_double()
         _scheck(self._lib.hb_server_stats(self._h, ctypes.byref(st), ctypes.byref(sm),
                                           ctypes.byref(um), ctypes.byref(js), ctypes.byref(lm)))
+        pre, uni, post, host, wait = (ctypes.c_double() for _ in range(5))
+        _scheck(self._lib.hb_server_step_times(self._h, ctypes.byref(pre), ctypes.byref(uni),
+                                               ctypes.byref(post), ctypes.byref(host),
+                                               ctypes.byref(wait)))
         return {"steps": st.value, "step_ms": sm.value, "union_ms": um.value,
-                "job_steps": js.value, "launch_ms": lm.value}
+                "job_steps": js.value, "launch_ms": lm.value,
+                "device_ms": {"pre": pre.value, "union": uni.value, "post": post.value},
+                "host_ms": host.value, "wait_ms": wait.value}
 
     def submit(self, graph, log2m, hasher=None, sum_of_distances=False,
                sum_of_inverse_distances=False, transpose_on_device=True, borrow=False):
