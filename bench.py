@@ -517,7 +517,8 @@ def run_gb300(args):
                            f"workload ({os.path.relpath(PROFILES[args.workload], ROOT)}) times "
                            f"the model bytes of the average launch") if ratio else
                           "no ncu capture of this workload",
-        "kernel": "union (k_union_window + k_union_heavy), one launch each per iteration",
+        "kernel": ("union (k_union_window or k_union_staged, and k_union_heavy), one launch "
+                   "each per iteration"),
         "model": "compulsory bytes: 8(S+1) + 4A + W U + 2 W S + n/4 per iteration",
         "model_bytes_per_launch": per_launch_model,
         "with_sums": {"achieved": model_sums / (union_ms / 1e3) / 1e9,
