@@ -62,7 +62,7 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-rmat", action="store_true",
                    help="web-like workload: skip the R-MAT 2^24 run reported beside it (rmat24)")
-    p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served", "visit"],
+    p.add_argument("--workload", choices=["weblike", "rmat", "batched", "served", "visit", "sumsweep"],
                    default="weblike",
                    help="weblike: the 2^26 web-like graph (default); rmat: R-MAT 2^24 x 16, "
                         "log2m 8; batched: many small graphs; served: a Poisson stream of jobs "
@@ -90,6 +90,8 @@ def set_workload(args):
         LOG2M = 8
         if args.log2n is None:
             args.log2n = 24
+    elif args.workload == "sumsweep" and args.log2n is None:
+        args.log2n = 20
     elif args.log2n is None:
         args.log2n = 26
     COUNTER_BYTES = (1 << LOG2M) * 5 // 8
@@ -964,6 +966,64 @@ def run_visit(args):
     return 0
 
 
+def run_sumsweep(args):
+    """One step = ExactSumSweep RadiusDiameter (the radius, the diameter and
+    their vertices) of the web-like graph with 2^log2n nodes (default 2^20)
+    through the public call, graph and transpose from host memory."""
+    import torch
+    import hyperball_gb300 as hb
+
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    torch.cuda.set_device(0)
+    g = hb.Graph.weblike(1 << args.log2n)
+    t = g.transpose()
+    level = "radius_diameter"
+    for _ in range(args.warmup):
+        r = hb.exact_sum_sweep(g, t, level=level)
+    secs, dev = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = hb.exact_sum_sweep(g, t, level=level)
+        secs.append(time.perf_counter() - t0)
+        dev.append(r["device_ms"])
+    ms = 1e3 * sum(secs) / len(secs)
+    fields = ("diameter", "radius", "diametral_vertex", "radial_vertex", "radius_iterations",
+              "diameter_iterations")
+    cpu, parity = None, None
+    if not args.no_cpu_baseline:
+        from oracle import hbo
+        t0 = time.perf_counter()
+        o = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+        dt = time.perf_counter() - t0
+        if any(o[f] != r[f] for f in fields):
+            raise RuntimeError("ExactSumSweep differs from the oracle")
+        parity = {"oracle": "oracle/sum_sweep_oracle.cpp", "result": "match",
+                  "checked": ", ".join(fields)}
+        cpu = {"value": 1.0 / dt, "unit": "runs/s", "cores": 1, "kind": "port",
+               "sample": f"ExactSumSweep restated (computer.rs), sequential visits, one run, {dt:.1f} s"}
+    line = {
+        "metric": "ExactSumSweep RadiusDiameter runs/s", "value": 1e3 / ms,
+        "unit": "runs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"weblike-2^{args.log2n} ExactSumSweep RadiusDiameter (directed)",
+                   "nodes": g.num_nodes, "arcs": g.num_arcs, "diameter": r["diameter"],
+                   "radius": r["radius"], "visits": r["sweeps"],
+                   "diameter_iterations": r["diameter_iterations"],
+                   "note": "value and e2e: the whole call from host CSR arrays (components on "
+                           "the host, visits and bounds on the device); device_ms: the device part"},
+        "device_ms": sum(dev) / len(dev),
+        "e2e": {"value": 1e3 / ms, "unit": "runs/s",
+                "h2d_bytes_per_step": 2 * (8 * (g.num_nodes + 1) + 4 * g.num_arcs),
+                "d2h_bytes_per_step": 64, "ms_per_step": ms},
+        "cpu_baseline": cpu, "parity": parity,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -974,6 +1034,8 @@ def main():
         return run_served(args)
     if args.workload == "visit":
         return run_visit(args)
+    if args.workload == "sumsweep":
+        return run_sumsweep(args)
     return run_gb300(args)
 
 

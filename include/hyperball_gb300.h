@@ -417,6 +417,51 @@ int hb_visit_each(hb_visit* v, const uint64_t* roots, size_t nroots, uint32_t* d
                   size_t len);
 const char* hb_visit_last_error(const hb_visit* v);
 
+/* ---- ExactSumSweep ------------------------------------------------------------- */
+/* The reference's ExactSumSweep (src/algo/exact_sum_sweep/: the OutputLevel
+ * types All, AllForward, RadiusDiameter, Diameter, Radius of
+ * output_level.rs, compute_directed and compute_undirected) on the device:
+ * exact eccentricities, radius and diameter from a few breadth-first visits
+ * with per-node bounds. */
+enum {
+    HB_SWEEP_ALL = 0,             /* forward and backward eccentricities, radius, diameter */
+    HB_SWEEP_ALL_FORWARD = 1,     /* forward eccentricities, radius, diameter */
+    HB_SWEEP_RADIUS_DIAMETER = 2,
+    HB_SWEEP_DIAMETER = 3,
+    HB_SWEEP_RADIUS = 4
+};
+/* a radius without radial vertices (usize::MAX in the reference) and an
+ * iteration count the level did not compute */
+#define HB_SWEEP_NONE UINT64_MAX
+typedef struct hb_sweep_result {
+    uint64_t diameter, radius;                 /* dir_outputs.rs / undir_outputs.rs */
+    uint64_t diametral_vertex, radial_vertex;
+    uint64_t radius_iterations, diameter_iterations;
+    uint64_t forward_iterations, all_iterations;
+    uint64_t sweeps;                           /* breadth-first visits run (no reference counterpart) */
+    double device_ms;                          /* device time of the computation (no reference counterpart) */
+} hb_sweep_result;
+/* OutputLevel::compute_directed(graph, transpose, radial_vertices) when
+ * `transpose` is given (output_level.rs:27-36), compute_undirected(graph)
+ * for a symmetric graph when it is NULL (a symmetric graph's All is
+ * AllForward, computer.rs:109-114). radial_vertices: num_nodes bytes
+ * (nonzero: radial) or NULL, which takes the nodes that reach the largest
+ * strongly connected component (computer.rs:487-542). Eccentricities (each
+ * num_nodes words, or NULL) are written when the level computes them: All
+ * gives forward and backward ones, AllForward the forward ones. Where the
+ * reference's parallel visits leave the radial vertex open among several
+ * nodes, the smallest is reported. An empty graph returns HB_ERR_INVALID with
+ * the reference's assertion message. The strongly connected components and
+ * the arcs between them are computed on the host, sequentially, as in the
+ * reference (sccs/tarjan.rs, scc_graph.rs). stream NULL: a stream of its
+ * own. Returns when the results are on the host. */
+int hb_exact_sum_sweep(const hb_graph_view* graph, const hb_graph_view* transpose, int level,
+                       const uint8_t* radial_vertices, int device, void* stream,
+                       uint64_t* forward_eccentricities, uint64_t* backward_eccentricities,
+                       hb_sweep_result* out);
+/* The message of the calling thread's last failed hb_exact_sum_sweep. */
+const char* hb_sweep_last_error(void);
+
 /* ---- device CSR utilities ----------------------------------------------------- */
 
 /* Transpose of a device-resident CSR graph: d_offsets[num_nodes + 1] and

@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/hyperball_oracle.cpp (HyperBall) and oracle/visits_oracle.cpp
-(breadth-first visits) into oracle/_build/libhb_oracle.so with g++. The reference crate itself is Rust and cannot be built in this image (no
+Compiles oracle/hyperball_oracle.cpp (HyperBall), oracle/visits_oracle.cpp
+(breadth-first visits) and oracle/sum_sweep_oracle.cpp (ExactSumSweep) into oracle/_build/libhb_oracle.so with g++. The reference crate itself is Rust and cannot be built in this image (no
 cargo/rustc), so there is no oracle/_ref: the oracle is this C++ restatement.
 The seeded graph generators (webgraph-algo-rs_gb300/csrc/graph_gen.cpp, plain
 C++) are compiled in too, so a process that only runs the oracle can build the
@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libhb_oracle.so")
 GEN_DIR = os.path.join(os.path.dirname(HERE), "webgraph-algo-rs_gb300", "csrc")
 SOURCES = [os.path.join(HERE, "hyperball_oracle.cpp"), os.path.join(HERE, "visits_oracle.cpp"),
-           os.path.join(GEN_DIR, "graph_gen.cpp")]
+           os.path.join(HERE, "sum_sweep_oracle.cpp"), os.path.join(GEN_DIR, "graph_gen.cpp")]
 HEADERS = [os.path.join(HERE, "hll_oracle.hpp"), os.path.join(GEN_DIR, "graph_gen.h")]
 
 

@@ -101,6 +101,12 @@ def lib():
             "hbo_visit_create": (V, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32)]),
             "hbo_visit_destroy": (None, [V]),
             "hbo_visit_reset": (None, [V]),
+            "hbo_sum_sweep": (ctypes.c_int, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                             _P(ctypes.c_uint64), _P(ctypes.c_uint32), ctypes.c_int,
+                                             V, _P(ctypes.c_uint64), _P(ctypes.c_uint64),
+                                             _P(ctypes.c_uint64)]),
+            "hbo_eccentricities": (None, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                          _P(ctypes.c_uint64)]),
             "hbo_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, _P(ctypes.c_uint64)]),
             "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
@@ -353,3 +359,57 @@ class OracleVisit:
                              d.ctypes.data_as(_P(ctypes.c_uint64)))
         return d
 
+
+
+SWEEP_LEVELS = {"all": 0, "all_forward": 1, "radius_diameter": 2, "diameter": 3, "radius": 4}
+NOT_COMPUTED = 2**64 - 1
+
+
+def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all", radial=None):
+    """ExactSumSweep restated (src/algo/exact_sum_sweep/computer.rs): a
+    directed graph with its transpose, or a symmetric graph without one.
+    Returns the output level's fields (eccentricities as uint64 arrays;
+    iterations and the radius of a graph without radial vertices as
+    NOT_COMPUTED = 2^64 - 1), or None when the level's outputs were not all
+    computed (an empty graph: the reference's output builders panic)."""
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    suc = np.ascontiguousarray(successors, dtype=np.uint32)
+    n = len(off) - 1
+    P64 = lambda a: a.ctypes.data_as(_P(ctypes.c_uint64))
+    P32 = lambda a: a.ctypes.data_as(_P(ctypes.c_uint32))
+    undirected = t_offsets is None
+    if not undirected:
+        toff = np.ascontiguousarray(t_offsets, dtype=np.uint64)
+        tsuc = np.ascontiguousarray(t_successors, dtype=np.uint32)
+    rad = None if radial is None else np.ascontiguousarray(radial, dtype=np.uint8)
+    fe = np.zeros(max(n, 1), dtype=np.uint64)
+    be = np.zeros(max(n, 1), dtype=np.uint64)
+    res = np.zeros(8, dtype=np.uint64)
+    lv = SWEEP_LEVELS[level]
+    r = lib().hbo_sum_sweep(n, P64(off), P32(suc), None if undirected else P64(toff),
+                            None if undirected else P32(tsuc), lv,
+                            None if rad is None else rad.ctypes.data, P64(fe), P64(be), P64(res))
+    if r != 0:
+        return None
+    out = {"diameter": int(res[0]), "radius": int(res[1]), "diametral_vertex": int(res[2]),
+           "radial_vertex": int(res[3]), "radius_iterations": int(res[4]),
+           "diameter_iterations": int(res[5]), "forward_iterations": int(res[6]),
+           "all_iterations": int(res[7])}
+    eff = 1 if undirected and lv == 0 else lv
+    if eff in (0, 1):
+        out["forward_eccentricities"] = fe[:n].copy()
+    if eff == 0:
+        out["backward_eccentricities"] = be[:n].copy()
+    return out
+
+
+def eccentricities(offsets, successors):
+    """Forward eccentricity of every node, one breadth-first visit each."""
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    suc = np.ascontiguousarray(successors, dtype=np.uint32)
+    n = len(off) - 1
+    e = np.zeros(max(n, 1), dtype=np.uint64)
+    lib().hbo_eccentricities(n, off.ctypes.data_as(_P(ctypes.c_uint64)),
+                             suc.ctypes.data_as(_P(ctypes.c_uint32)),
+                             e.ctypes.data_as(_P(ctypes.c_uint64)))
+    return e[:n]

@@ -39,7 +39,7 @@ def _units():
     cuda = _cuda_home()
     inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC]
     units = []
-    for name in ("hb_kernels.cu", "visits.cu"):
+    for name in ("hb_kernels.cu", "visits.cu", "sum_sweep.cu"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OBJ, name + ".o")
         cmd = [os.path.join(cuda, "bin", "nvcc"), *ARCH, "-O3", "-lineinfo", "-std=c++17",

@@ -373,9 +373,13 @@ int dalloc(hb_handle* h, T** out, size_t count) {
     size_t bytes = std::max<size_t>(count * sizeof(T), 256);
     void* p = nullptr;
     // stream-ordered: freeing never synchronises the whole device, so other
-    // work (other handles, other jobs of a server) keeps running
+    // work (other handles, other jobs of a server) keeps running. The block
+    // is valid in the handle's stream order; creation and hb_init end with a
+    // synchronisation before any other stream uses it. (A synchronisation
+    // after every allocation cost a served job's creation up to one step of
+    // the other jobs per allocation: its stream waits for SMs the shared
+    // union launch holds.)
     cudaError_t e = pool_alloc(h->device, &p, bytes, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return cuda_err(h, e, "cudaMallocFromPoolAsync");
@@ -613,8 +617,9 @@ int upload_csr(hb_handle* h, const hb_graph_view* g, uint64_t** d_off, uint32_t*
 void dfree(hb_handle* h, void* p) {
     for (auto it = h->bufs.begin(); it != h->bufs.end(); ++it)
         if (it->p == p) {
+            // stream-ordered: later allocations reuse the block after the
+            // work before this point (no synchronisation)
             cudaFreeAsync(p, h->stream);
-            cudaStreamSynchronize(h->stream);
             h->bufs.erase(it);
             return;
         }
@@ -2319,17 +2324,17 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
         std::vector<double> lnt(mm + 1, 0.0);
         const double mf = (double)mm;
         for (uint64_t z = 1; z <= mm; z++) lnt[z] = mf * std::log(mf / (double)z);
-        // Host-to-device copies of the handle go on its own stream, and are
-        // waited for: a plain cudaMemcpy from pageable memory may return
-        // before its DMA lands and orders nothing on the handle's
-        // non-blocking streams (the init kernel once read a table that was
-        // still on its way: every initial estimate 0 in a served job).
+        // Host-to-device copies of the handle go on its own stream: a plain
+        // cudaMemcpy from pageable memory may return before its DMA lands and
+        // orders nothing on the handle's non-blocking streams (the init
+        // kernel once read a table that was still on its way: every initial
+        // estimate 0 in a served job). A pageable source is staged before
+        // cudaMemcpyAsync returns, so it may go out of scope right after.
         if ((r = dalloc(hp, &h->d_lnt, mm + 1))) return fail(r);
         if ((r = cuda_err(hp, cudaMemcpyAsync(h->d_lnt, lnt.data(), (mm + 1) * 8, cudaMemcpyHostToDevice,
                                               h->stream),
                           "cudaMemcpyAsync")))
             return fail(r);
-        if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     }
     if (o.weights) {
         if ((r = dalloc(hp, &h->d_weights, n))) return fail(r);
@@ -2337,7 +2342,6 @@ static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpos
                                               h->stream),
                           "cudaMemcpyAsync")))
             return fail(r);
-        if ((r = cuda_err(hp, cudaStreamSynchronize(h->stream), "cudaStreamSynchronize"))) return fail(r);
     }
     trace.mark("state arrays");
     h->grid_tile = hbk::tile_grid(h->log2m, h->device, 0);

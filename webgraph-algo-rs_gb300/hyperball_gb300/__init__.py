@@ -155,6 +155,14 @@ class VisitStats(ctypes.Structure):
                 ("known_arcs", ctypes.c_uint64), ("device_ms", ctypes.c_double)]
 
 
+class SweepResult(ctypes.Structure):
+    _fields_ = [("diameter", ctypes.c_uint64), ("radius", ctypes.c_uint64),
+                ("diametral_vertex", ctypes.c_uint64), ("radial_vertex", ctypes.c_uint64),
+                ("radius_iterations", ctypes.c_uint64), ("diameter_iterations", ctypes.c_uint64),
+                ("forward_iterations", ctypes.c_uint64), ("all_iterations", ctypes.c_uint64),
+                ("sweeps", ctypes.c_uint64), ("device_ms", ctypes.c_double)]
+
+
 class IterStats(ctypes.Structure):
     _fields_ = [
         ("iteration", ctypes.c_uint64),
@@ -286,6 +294,11 @@ EXPORTS = [
     ("hb_visit_each", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     ("hb_visit_last_error", ctypes.c_char_p, [_H]),
+    ("hb_exact_sum_sweep", ctypes.c_int, [ctypes.POINTER(GraphView), ctypes.POINTER(GraphView),
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.POINTER(SweepResult)]),
+    ("hb_sweep_last_error", ctypes.c_char_p, []),
 ]
 
 _lib = None
@@ -1060,6 +1073,49 @@ def release_cached_memory(device=0):
 # ---------------------------------------------------------------------------
 # breadth-first visits (src/algo/visits/breadth_first/par_fair.rs)
 # ---------------------------------------------------------------------------
+SWEEP_LEVELS = {"all": 0, "all_forward": 1, "radius_diameter": 2, "diameter": 3, "radius": 4}
+SWEEP_NONE = 2**64 - 1
+
+
+def exact_sum_sweep(graph, transpose=None, level="all", radial_vertices=None, device=0,
+                    stream=None):
+    """ExactSumSweep (src/algo/exact_sum_sweep/) on the device:
+    OutputLevel::compute_directed(graph, transpose, radial_vertices) with a
+    transpose, compute_undirected(graph) of a symmetric graph without one.
+    `level`: "all", "all_forward", "radius_diameter", "diameter", "radius".
+    Returns the output's fields as a dict (forward / backward eccentricities
+    as uint64 arrays where the level computes them; a radius without radial
+    vertices and iteration counts the level does not compute are
+    SWEEP_NONE = 2^64 - 1), plus "sweeps" (visits run) and "device_ms"."""
+    lib = load_library()
+    lv = SWEEP_LEVELS[level]
+    g = graph.view()
+    t = transpose.view() if transpose is not None else None
+    n = graph.num_nodes
+    rad = None
+    if radial_vertices is not None:
+        rad = np.ascontiguousarray(radial_vertices, dtype=np.uint8)
+        if rad.shape != (n,):
+            raise ValueError("radial_vertices must have one entry per node")
+    eff = 1 if (transpose is None and lv == 0) else lv
+    fe = np.zeros(max(n, 1), dtype=np.uint64) if eff in (0, 1) else None
+    be = np.zeros(max(n, 1), dtype=np.uint64) if eff == 0 else None
+    res = SweepResult()
+    code = lib.hb_exact_sum_sweep(ctypes.byref(g), ctypes.byref(t) if t is not None else None, lv,
+                                  rad.ctypes.data if rad is not None else None, int(device), stream,
+                                  fe.ctypes.data if fe is not None else None,
+                                  be.ctypes.data if be is not None else None, ctypes.byref(res))
+    if code:
+        msg = (lib.hb_sweep_last_error() or b"").decode(errors="replace")
+        raise _ERRORS.get(code, HyperBallError)(code, msg)
+    out = {f: getattr(res, f) for f, _ in SweepResult._fields_}
+    if fe is not None:
+        out["forward_eccentricities"] = fe[:n]
+    if be is not None:
+        out["backward_eccentricities"] = be[:n]
+    return out
+
+
 class ParFair:
     """The fair parallel breadth-first visit of the reference (ParFairPred /
     ParFairNoPred, par_fair.rs:92-124) on the device. The reference reports
