@@ -42,7 +42,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -70,11 +73,21 @@ __device__ __forceinline__ void sw_append(bool c, uint32_t s, uint32_t* queue, u
     if (c) queue[base + __popc(mask & ((1u << lane) - 1u))] = s;
 }
 
+// The level state of a visit in device memory, so that the host enqueues
+// several levels before it looks: queue slots [b, e) are the frontier (at
+// distance d - 1), d the distance its successors get, last the largest
+// distance that reached a node.
+struct Level {
+    unsigned long long b, e, d, last;
+};
+
 // level [b, e) of the queue (distance d - 1) -> distance d, appended at *tail
 __global__ void k_sw_expand(const uint64_t* __restrict__ off, const uint32_t* __restrict__ succ,
                             const uint32_t* __restrict__ comp, uint32_t* dist, uint32_t* queue,
-                            uint64_t b, uint64_t e, uint32_t d, unsigned long long* tail, uint32_t* heavy,
+                            const Level* lev, unsigned long long* tail, uint32_t* heavy,
                             unsigned long long* heavy_n) {
+    const uint64_t b = lev->b, e = lev->e;
+    const uint32_t d = (uint32_t)lev->d;
     const int lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -101,9 +114,10 @@ __global__ void k_sw_expand(const uint64_t* __restrict__ off, const uint32_t* __
 
 // the deferred nodes of a level, one block each
 __global__ void k_sw_heavy(const uint64_t* __restrict__ off, const uint32_t* __restrict__ succ,
-                           const uint32_t* __restrict__ comp, uint32_t* dist, uint32_t* queue, uint32_t d,
+                           const uint32_t* __restrict__ comp, uint32_t* dist, uint32_t* queue, const Level* lev,
                            unsigned long long* tail, const uint32_t* heavy, const unsigned long long* heavy_n) {
     const uint64_t count = *heavy_n;
+    const uint32_t d = (uint32_t)lev->d;
     for (uint64_t h = blockIdx.x; h < count; h += gridDim.x) {
         const uint32_t v = heavy[h];
         const uint64_t s0 = off[v], s1 = off[v + 1];
@@ -119,6 +133,16 @@ __global__ void k_sw_heavy(const uint64_t* __restrict__ off, const uint32_t* __r
             sw_append(c, s, queue, tail);
         }
     }
+}
+
+// the next level: the nodes just appended become the frontier
+__global__ void k_sw_advance(Level* lev, const unsigned long long* tail, unsigned long long* heavy_n) {
+    const unsigned long long t = *tail;
+    if (t > lev->e) lev->last = lev->d;
+    lev->b = lev->e;
+    lev->e = t;
+    lev->d++;
+    *heavy_n = 0;
 }
 
 // the start nodes of a visit at distance 0 (each start is distinct)
@@ -439,7 +463,8 @@ struct Sweeper {
     uint32_t *d_roots = nullptr, *d_df = nullptr, *d_db = nullptr;
     u64 *d_fl = nullptr, *d_fh = nullptr, *d_bl = nullptr, *d_bh = nullptr, *d_ft = nullptr, *d_bt = nullptr;
     uint8_t* d_radial = nullptr;
-    unsigned long long* d_cnt = nullptr;  // [0] tail [1] heavy [2] radius key [3..7] missing counts
+    unsigned long long* d_cnt = nullptr;  // [2] radius key [3..7] missing counts
+    hbs::Level* d_lev = nullptr;          // a visit's level, then its tail and deferred-node count
     unsigned long long *d_ecc_f = nullptr, *d_ecc_b = nullptr, *d_best_score = nullptr, *d_best_tot = nullptr;
     uint32_t* d_pivot = nullptr;
     u64 *d_ef = nullptr, *d_eb = nullptr;
@@ -466,7 +491,7 @@ struct Sweeper {
         // a symmetric graph is its own transpose: each block once
         std::vector<void*> ps = {d_off, d_toff, d_succ, d_tsucc, d_dist, d_queue, d_heavy, d_comp,
                                  d_roots, d_df, d_db, d_fl, d_fh, d_bl, d_bh, d_ft, d_bt, d_radial,
-                                 d_cnt, d_ecc_f, d_ecc_b, d_best_score, d_best_tot, d_pivot, d_ef,
+                                 d_cnt, d_lev, d_ecc_f, d_ecc_b, d_best_score, d_best_tot, d_pivot, d_ef,
                                  d_eb, d_cstart, d_cend, d_gather, d_gather64, d_best};
         std::sort(ps.begin(), ps.end());
         ps.erase(std::unique(ps.begin(), ps.end()), ps.end());
@@ -488,37 +513,39 @@ struct Sweeper {
     // One visit from the `count` start nodes in d_roots on the graph or its
     // transpose (inside components when `in_comp`); returns the number of
     // visited nodes (d_queue[0, visited), distances in d_dist) and the
-    // largest distance in *ecc.
+    // largest distance in *ecc. Levels are enqueued LEVELS_AHEAD at a time
+    // with their bounds in device memory (a level past the last is empty);
+    // the host looks only between groups.
     u64 visit(u64 count, bool backward, bool in_comp, u64* ecc) {
+        constexpr int LEVELS_AHEAD = 8;
         const u64* off = backward ? d_toff : d_off;
         const uint32_t* succ = backward ? d_tsucc : d_succ;
         const uint32_t* cp = in_comp ? d_comp : nullptr;
         ck(cudaMemsetAsync(d_dist, 0xff, n * 4, s), "cudaMemsetAsync");
         hbs::k_sw_roots<<<blocks(count), hbs::SW_THREADS, 0, s>>>(d_roots, count, d_dist, d_queue);
         ck(cudaGetLastError(), "k_sw_roots");
-        u64 b = 0, e = count;
-        uint32_t d = 0;
-        h_cnt[0] = e;
-        while (e > b) {
-            d++;
-            ck(cudaMemcpyAsync(d_cnt, h_cnt, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-            ck(cudaMemsetAsync(d_cnt + 1, 0, 8, s), "cudaMemsetAsync");
-            const u64 warps = e - b;
-            const int g = (int)std::min<u64>((warps * 32 + hbs::SW_THREADS - 1) / hbs::SW_THREADS, (u64)grid);
-            hbs::k_sw_expand<<<g, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, b, e, d, d_cnt, d_heavy,
-                                                          d_cnt + 1);
+        hbs::Level* h = reinterpret_cast<hbs::Level*>(h_cnt);
+        *h = hbs::Level{0, count, 1, 0};
+        h_cnt[4] = count;  // tail
+        h_cnt[5] = 0;      // deferred nodes
+        ck(cudaMemcpyAsync(d_lev, h_cnt, 6 * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        unsigned long long* tail = reinterpret_cast<unsigned long long*>(d_lev) + 4;
+        unsigned long long* heavy_n = tail + 1;
+        for (;;) {
+            for (int k = 0; k < LEVELS_AHEAD; k++) {
+                hbs::k_sw_expand<<<grid, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
+                                                                 d_heavy, heavy_n);
+                hbs::k_sw_heavy<<<sms * 4, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
+                                                                  d_heavy, heavy_n);
+                hbs::k_sw_advance<<<1, 1, 0, s>>>(d_lev, tail, heavy_n);
+            }
             ck(cudaGetLastError(), "k_sw_expand");
-            hbs::k_sw_heavy<<<sms * 4, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, d, d_cnt, d_heavy,
-                                                              d_cnt + 1);
-            ck(cudaGetLastError(), "k_sw_heavy");
-            ck(cudaMemcpyAsync(h_cnt, d_cnt, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+            ck(cudaMemcpyAsync(h_cnt, d_lev, 6 * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
             sync();
-            b = e;
-            e = h_cnt[0];
+            if (h->b == h->e) break;
         }
-        // the last level that added nodes is d - 1
-        if (ecc) *ecc = d - 1;
-        return e;
+        if (ecc) *ecc = h->last;
+        return h_cnt[4];
     }
 
     void set_root(u64 r) {
@@ -809,20 +836,39 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     w.grid = w.sms * 8;
     ck(cudaEventCreate(&w.ev0), "cudaEventCreate");
     ck(cudaEventCreate(&w.ev1), "cudaEventCreate");
+    // HB_TRACE=1: the phases' host time on stderr
+    const bool trace = std::getenv("HB_TRACE") != nullptr;
+    auto t_mark = std::chrono::steady_clock::now();
+    auto mark = [&](const char* what) {
+        if (!trace) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "hb_exact_sum_sweep %-22s %9.2f ms\n", what,
+                     std::chrono::duration<double, std::milli>(now - t_mark).count());
+        t_mark = now;
+    };
     // components and the arcs between them (host, as the reference)
     HostCsr hg{n, g->offsets, g->successors};
     HostCsr ht = t ? HostCsr{n, t->offsets, t->successors} : hg;
     w.comp = w.undirected ? symm_components(hg, w.ncomp) : tarjan(hg, w.ncomp);
     w.seg.assign(w.ncomp, 0);
+    mark("components");
     if (!w.undirected) {
-        // scc_graph.rs:118-227
-        std::vector<std::vector<uint32_t>> members(w.ncomp);
-        for (u64 v = 0; v < n; v++) members[w.comp[v]].push_back((uint32_t)v);
+        // scc_graph.rs:118-227; the nodes of each component in increasing
+        // order by a counting sort
+        std::vector<u64> first(w.ncomp + 1, 0);
+        for (u64 v = 0; v < n; v++) first[w.comp[v] + 1]++;
+        for (u64 c = 0; c < w.ncomp; c++) first[c + 1] += first[c];
+        std::vector<uint32_t> members(n);
+        {
+            std::vector<u64> at(first.begin(), first.end() - 1);
+            for (u64 v = 0; v < n; v++) members[at[w.comp[v]]++] = (uint32_t)v;
+        }
         std::vector<uint32_t> bs(w.ncomp, 0xffffffffu), be(w.ncomp, 0);
         std::vector<uint32_t> children;
         auto value = [&](u64 a, u64 b) { return ht.deg(a) + hg.deg(b); };
         for (u64 c = 0; c < w.ncomp; c++) {
-            for (uint32_t v : members[c])
+            for (u64 k = first[c]; k < first[c + 1]; k++) {
+                const uint32_t v = members[k];
                 for (u64 e = hg.off[v]; e < hg.off[v + 1]; e++) {
                     const uint32_t x = hg.succ[e];
                     const uint32_t xc = w.comp[x];
@@ -837,6 +883,7 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
                         be[xc] = x;
                     }
                 }
+            }
             w.seg[c] = w.ctarget.size();
             for (uint32_t ch : children) {
                 w.ctarget.push_back(ch);
@@ -847,6 +894,7 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
             children.clear();
         }
     }
+    mark("component arcs");
     // device state
     const u64 nc = w.ncomp, nconn = w.ctarget.size();
     w.alloc(&w.d_off, n + 1);
@@ -862,6 +910,7 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     for (u64** p : {&w.d_fl, &w.d_fh, &w.d_bl, &w.d_bh, &w.d_ft, &w.d_bt}) w.alloc(p, n);
     w.alloc(&w.d_radial, n);
     w.alloc(&w.d_cnt, 8);
+    ck(cudaMalloc((void**)&w.d_lev, 6 * 8), "cudaMalloc");
     w.alloc(&w.d_ecc_f, nc);
     w.alloc(&w.d_ecc_b, nc);
     w.alloc(&w.d_best_score, nc);
@@ -913,10 +962,13 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     } else {
         ck(cudaMemsetAsync(w.d_radial, 0, n, s), "cudaMemsetAsync");
     }
+    w.sync();
+    mark("device state");
     ck(cudaEventRecord(w.ev0, s), "cudaEventRecord");
     w.compute();
     ck(cudaEventRecord(w.ev1, s), "cudaEventRecord");
     w.sync();
+    mark("visits and bounds");
     cudaEventElapsedTime(&w.device_ms, w.ev0, w.ev1);
     // output_level.rs: what each level reports, and its asserts
     out->diameter = w.diameter_low;
