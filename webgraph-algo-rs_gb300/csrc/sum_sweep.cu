@@ -331,6 +331,12 @@ __global__ void k_sw_refine(uint64_t n, const uint32_t* __restrict__ comp, const
     }
 }
 
+// a[i] = b[i] = value (the start node's bounds after its own visit)
+__global__ void k_sw_set2(uint64_t* a, uint64_t* b, uint64_t i, uint64_t value) {
+    a[i] = value;
+    b[i] = value;
+}
+
 __global__ void k_sw_fill64(uint64_t* p, uint64_t count, uint64_t value) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
         p[i] = value;
@@ -471,7 +477,8 @@ struct Sweeper {
     uint32_t *d_cstart = nullptr, *d_cend = nullptr, *d_gather = nullptr;
     u64* d_gather64 = nullptr;
     hbs::Best* d_best = nullptr;
-    unsigned long long* h_cnt = nullptr;
+    unsigned long long* h_cnt = nullptr;  // page-locked: [0, 6) a visit's level, 6 root, 7 key, [8, 13) counts
+    hbs::Best* h_best = nullptr;          // page-locked copy of the selection's block results
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     float device_ms = 0.f;
     u64 sweeps = 0;
@@ -483,6 +490,7 @@ struct Sweeper {
     u64 diameter_low = 0, radius_high = NONE, diameter_vertex = 0, radius_vertex = 0, iterations = 0;
     u64 radius_it = NONE, diameter_it = NONE, forward_it = NONE, all_it = NONE;
     bool compute_radial = true;
+    std::vector<uint8_t> radial_host;  // the radial vertices (read on the host by forward steps)
     int grid = 1;
 
     ~Sweeper() {
@@ -498,6 +506,7 @@ struct Sweeper {
         for (void* p : ps)
             if (p) cudaFree(p);
         if (h_cnt) cudaFreeHost(h_cnt);
+        if (h_best) cudaFreeHost(h_best);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (own_stream && s) cudaStreamDestroy(s);
@@ -548,21 +557,20 @@ struct Sweeper {
         return h_cnt[4];
     }
 
+    // small transfers go through page-locked words (a pageable copy would
+    // wait for the stream each time): h_cnt[6] the start node, h_cnt[7]
+    // the radius key
     void set_root(u64 r) {
-        const uint32_t v = (uint32_t)r;
-        ck(cudaMemcpyAsync(d_roots, &v, 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        reinterpret_cast<uint32_t*>(h_cnt + 6)[0] = (uint32_t)r;
+        ck(cudaMemcpyAsync(d_roots, h_cnt + 6, 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
     }
 
     unsigned long long read_key() {
-        unsigned long long k = 0;
-        ck(cudaMemcpyAsync(&k, d_cnt + 2, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        ck(cudaMemcpyAsync(h_cnt + 7, d_cnt + 2, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
         sync();
-        return k;
+        return h_cnt[7];
     }
-    void reset_key() {
-        const unsigned long long none = ~0ull;
-        ck(cudaMemcpyAsync(d_cnt + 2, &none, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-    }
+    void reset_key() { ck(cudaMemsetAsync(d_cnt + 2, 0xff, 8, s), "cudaMemsetAsync"); }
 
     // argmax / argmin over nodes (filter 0: bounds fa, fb not met; 1 radial)
     u64 select(const u64* val, const u64* tie, bool maximize, int filter, const u64* fa, const u64* fb) {
@@ -570,12 +578,11 @@ struct Sweeper {
         hbs::k_sw_select<<<g, hbs::SW_THREADS, 0, s>>>(n, val, tie, d_off, maximize ? 1 : 0, filter, fa, fb,
                                                        d_radial, d_best);
         ck(cudaGetLastError(), "k_sw_select");
-        std::vector<hbs::Best> h(g);
-        ck(cudaMemcpyAsync(h.data(), d_best, g * sizeof(hbs::Best), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        ck(cudaMemcpyAsync(h_best, d_best, g * sizeof(hbs::Best), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
         sync();
         hbs::Best b{0, 0, NONE};
-        for (const hbs::Best& c : h)
-            if (hbs::better(c, b, maximize)) b = c;
+        for (int k = 0; k < g; k++)
+            if (hbs::better(h_best[k], b, maximize)) b = h_best[k];
         return b.idx;
     }
 
@@ -605,12 +612,9 @@ struct Sweeper {
         const u64 cnt = visit(1, false, false, &ecc);
         sweeps++;
         hbs::k_sw_fwd_update<<<blocks(cnt), hbs::SW_THREADS, 0, s>>>(d_queue, cnt, d_dist, d_bt, d_bl, d_bh);
+        hbs::k_sw_set2<<<1, 1, 0, s>>>(d_fl, d_fh, start, ecc);
         ck(cudaGetLastError(), "k_sw_fwd_update");
-        ck(cudaMemcpyAsync(d_fl + start, &ecc, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-        ck(cudaMemcpyAsync(d_fh + start, &ecc, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-        uint8_t rad = 0;
-        ck(cudaMemcpyAsync(&rad, d_radial + start, 1, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
-        sync();
+        const bool rad = radial_host[start] != 0;
         if (diameter_low < ecc) {
             diameter_low = ecc;
             diameter_vertex = start;
@@ -630,9 +634,8 @@ struct Sweeper {
         reset_key();
         hbs::k_sw_bwd_update<<<blocks(cnt), hbs::SW_THREADS, 0, s>>>(d_queue, cnt, d_dist, d_ft, d_fl, d_fh,
                                                                     d_radial, d_cnt + 2);
+        hbs::k_sw_set2<<<1, 1, 0, s>>>(d_bl, d_bh, start, ecc);
         ck(cudaGetLastError(), "k_sw_bwd_update");
-        ck(cudaMemcpyAsync(d_bl + start, &ecc, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-        ck(cudaMemcpyAsync(d_bh + start, &ecc, 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
         const unsigned long long key = read_key();
         if (key != ~0ull && (key >> 32) < radius_high) {
             radius_high = key >> 32;
@@ -736,8 +739,8 @@ struct Sweeper {
         hbs::k_sw_missing<<<blocks(n), hbs::SW_THREADS, 0, s>>>(n, d_fl, d_fh, d_bl, d_bh, d_radial, diameter_low,
                                                                radius_high, d_cnt + 3);
         ck(cudaGetLastError(), "k_sw_missing");
-        unsigned long long c[5];
-        ck(cudaMemcpyAsync(c, d_cnt + 3, sizeof c, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        unsigned long long* c = h_cnt + 8;
+        ck(cudaMemcpyAsync(c, d_cnt + 3, 5 * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
         sync();
         const u64 mr = c[0], mdf = c[1], mdb = c[2], maf = c[3], mab = c[4];
         if (mr == 0 && radius_it == NONE) radius_it = iterations;
@@ -756,6 +759,9 @@ struct Sweeper {
     // computer.rs:282-409
     void compute() {
         if (compute_radial) compute_radial_vertices();
+        radial_host.resize(n);
+        ck(cudaMemcpyAsync(radial_host.data(), d_radial, n, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        sync();
         step(select(nullptr, nullptr, true, 2, nullptr, nullptr), true);
         for (int i = 2; i <= 6; i++) {
             if (i % 2 == 0)
@@ -923,7 +929,8 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     w.alloc(&w.d_cend, nconn);
     w.alloc(&w.d_gather, nconn);
     w.alloc(&w.d_best, (u64)w.grid);
-    ck(cudaMallocHost((void**)&w.h_cnt, 8 * 8), "cudaMallocHost");
+    ck(cudaMallocHost((void**)&w.h_cnt, 16 * 8), "cudaMallocHost");
+    ck(cudaMallocHost((void**)&w.h_best, (size_t)w.grid * sizeof(hbs::Best)), "cudaMallocHost");
     cudaStream_t s = w.s;
     ck(cudaMemcpyAsync(w.d_off, g->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
     if (m) ck(cudaMemcpyAsync(w.d_succ, g->successors, m * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
