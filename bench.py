@@ -78,6 +78,8 @@ def parse_args():
                    help="served: a second, lower arrival rate (0: none)")
     p.add_argument("--setup-threads", type=int, default=0,
                    help="served: job creation / results threads (0: the server's default)")
+    p.add_argument("--union-sm-reserve", type=int, default=None,
+                   help="served: SMs the shared union launch leaves to job creation (default: the server's)")
     args = p.parse_args()
     set_workload(args)
     return args
@@ -828,7 +830,8 @@ def run_served(args):
 
     with ThreadPoolExecutor(max_workers=host_cores()) as ex:
         graphs = list(ex.map(make, gspecs))
-    server = hb.HyperBallServer(max_active=args.max_active, setup_threads=args.setup_threads)
+    server = hb.HyperBallServer(max_active=args.max_active, setup_threads=args.setup_threads,
+                                union_sm_reserve=args.union_sm_reserve)
     # warm-up: one job of each log2m
     for l2m in (4, 6, 8):
         j = server.submit(graphs[0], l2m, sum_of_distances=True, sum_of_inverse_distances=True)

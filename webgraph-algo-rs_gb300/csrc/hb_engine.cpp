@@ -1594,6 +1594,13 @@ int hb_multi_start(hb_handle* h) {
     return do_init(h);
 }
 
+void hb_multi_reserve_sms(hb_multi* m, uint32_t sms) {
+    const int all = hbk::num_sms(m->mc.device);
+    const int per_sm = std::max(1, hbk::jobs_grid(m->mc.device) / std::max(all, 1));
+    const int used = std::max(1, all - (int)std::min<uint32_t>(sms, (uint32_t)all - 1));
+    m->mc.grid = per_sm * used;
+}
+
 int hb_multi_set_stream(hb_handle* h, void* stream) {
     HB_CUDA(h, cudaSetDevice(h->device));
     HB_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -275,6 +275,8 @@ int hb_multi_start(hb_handle* h);
 // moves the handle's later work to `stream` (its earlier work is waited for)
 int hb_multi_set_stream(hb_handle* h, void* stream);
 int hb_multi_step(hb_multi* m, hb_handle* const* hs, uint32_t count, std::string& err);
+// the shared union launch leaves `sms` SMs free (its grid is that much smaller)
+void hb_multi_reserve_sms(hb_multi* m, uint32_t sms);
 // the handle's run is over: its last iteration modified no counter, or it
 // ran num_nodes iterations (the stop rules of run_until_done, HB:541, HB:559-570)
 bool hb_multi_done(const hb_handle* h);

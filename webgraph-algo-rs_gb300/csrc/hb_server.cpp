@@ -358,6 +358,7 @@ int hb_server_create(const hb_server_options* opts, hb_server** out) {
             delete s;
             return server_err(r, "server setup: " + (err.empty() ? std::string("cudaStreamCreate failed") : err));
         }
+        if (o.union_sm_reserve) hb_multi_reserve_sms(s->multi, o.union_sm_reserve);
     } else {
         // no device: every job fails at creation with HB_ERR_NO_DEVICE
         cudaGetLastError();

@@ -129,7 +129,7 @@ class ServerOptions(ctypes.Structure):
         ("max_active", ctypes.c_uint32),
         ("keep_registers", ctypes.c_uint32),
         ("setup_threads", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("union_sm_reserve", ctypes.c_uint32),
     ]
 
 
@@ -953,7 +953,7 @@ class HyperBallServer:
     returns for its graph alone."""
 
     def __init__(self, hbm_budget_bytes=150 * 10**9, max_active=16, keep_registers=False,
-                 device=0, setup_threads=0):
+                 device=0, setup_threads=0, union_sm_reserve=None):
         lib = load_library()
         self._lib = lib
         o = ServerOptions()
@@ -963,6 +963,8 @@ class HyperBallServer:
         o.keep_registers = 1 if keep_registers else 0
         o.device = int(device)
         o.setup_threads = int(setup_threads)
+        if union_sm_reserve is not None:
+            o.union_sm_reserve = int(union_sm_reserve)
         h = ctypes.c_void_p()
         _scheck(lib.hb_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h
