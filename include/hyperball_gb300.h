@@ -304,7 +304,7 @@ typedef struct hb_server_options {
     uint32_t max_active;       /* jobs past admission at once, 1 to 48; default 16 */
     uint32_t keep_registers;   /* 1: keep each finished job's counters for hb_server_get_registers */
     uint32_t setup_threads;    /* threads that create jobs, and as many that fetch results; 0 = min(max_active, 2) */
-    uint32_t union_sm_reserve; /* SMs the shared union launch leaves to the jobs' creation kernels; 0: none */
+    uint32_t union_sm_reserve; /* SMs the shared union launch leaves to the jobs' creation kernels; default 16 */
 } hb_server_options;
 
 typedef struct hb_job_info {

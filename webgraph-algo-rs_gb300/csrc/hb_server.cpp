@@ -326,6 +326,9 @@ void hb_server_options_default(hb_server_options* o) {
     o->hbm_budget_bytes = 150ull * 1000 * 1000 * 1000;
     o->max_active = 16;
     o->keep_registers = 0;
+    // measured on the 600-job served workload, two runs each: 0, 16 and 38
+    // SMs left free gave 1.66/1.49, 1.67/1.84 and 1.41/1.68 e12 updates/s
+    o->union_sm_reserve = 16;
 }
 
 int hb_server_create(const hb_server_options* opts, hb_server** out) {
