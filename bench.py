@@ -366,6 +366,13 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    if args.workload == "sumsweep":
+        return run_reference_sumsweep(args)
+    if args.workload not in ("weblike", "rmat"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the CPU arm times the single-graph workloads (weblike, rmat) and sumsweep"}),
+              flush=True)
+        return 0
     g = make_oracle_graph(args)
     t = g.transpose()
     # warm-up: the first iterations of an earlier run (at most 3: each is
@@ -384,6 +391,36 @@ def run_reference(args):
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": ("one step = one complete run (minutes on the host cores), so one step is timed; "
                  "the warm-up is the first iterations of an earlier run"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_sumsweep(args):
+    """The oracle's ExactSumSweep (sequential visits) on the graph of
+    --workload sumsweep; each step is one complete call."""
+    from oracle import hbo
+    g = hbo.OracleGraph.weblike(1 << args.log2n)
+    t = g.transpose()
+    level = "radius_diameter"
+    for _ in range(min(args.warmup, 1)):
+        hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+    steps = max(1, min(args.steps, 2))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+    dt = (time.perf_counter() - t0) / steps
+    line = {
+        "impl": "reference", "metric": "ExactSumSweep RadiusDiameter runs/s", "value": 1.0 / dt,
+        "unit": "runs/s", "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1),
+        "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"weblike-2^{args.log2n} ExactSumSweep RadiusDiameter (directed)",
+                   "nodes": g.num_nodes, "arcs": g.num_arcs, "diameter": r["diameter"],
+                   "radius": r["radius"], "diameter_iterations": r["diameter_iterations"]},
+        "cpu_baseline": {"value": 1.0 / dt, "unit": "runs/s", "cores": 1, "kind": "port",
+                         "sample": "ExactSumSweep restated (computer.rs), sequential visits"},
+        "e2e": {"value": 1.0 / dt, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
