@@ -28,12 +28,12 @@
 //   k_sw_pivot_*              the best pivot of every component
 //                             (computer.rs:418-475) by three atomicMin passes;
 //   k_sw_refine               the node pass of all_cc_upper_bound.
-// The host keeps what the reference computes sequentially as well: the
-// strongly connected components (Tarjan, sccs/tarjan.rs; connected
-// components of a symmetric graph, sccs/symm_seq.rs), the arcs between
-// components (scc_graph.rs) and the two passes over the component DAG of
-// all_cc_upper_bound (computer.rs:829-873), which touch one value per
-// component and per DAG arc.
+// The strongly connected component of the largest out-degree node comes from
+// two device visits; the host runs Tarjan's algorithm on the nodes outside it
+// (see directed_components), the connected components of a symmetric graph
+// (sccs/symm_seq.rs), the arcs between components (scc_graph.rs) and the two
+// passes over the component DAG of all_cc_upper_bound (computer.rs:829-873),
+// which touch one value per component and per DAG arc.
 //
 // Where the reference's parallel visits leave a choice open (which of the
 // nodes reaching a new minimal radius in one step becomes the radial vertex)
@@ -384,16 +384,20 @@ struct HostCsr {
 
 // sccs/tarjan.rs: components numbered as they are emitted (reverse
 // topological order), roots in node order, successors in arc order
-std::vector<uint32_t> tarjan(const HostCsr& g, u64& ncomp) {
+// With `group` given, only the nodes v with group[v] == want and the arcs
+// between them take part (the other entries of comp are left as they are),
+// and the components are numbered from ncomp on.
+void tarjan_into(const HostCsr& g, std::vector<uint32_t>& comp, u64& ncomp, const uint8_t* group = nullptr,
+                 uint8_t want = 0) {
     const u64 n = g.n;
-    std::vector<uint32_t> index(n, 0xffffffffu), low(n, 0), comp(n, 0);
+    auto in = [&](u64 v) { return !group || group[v] == want; };
+    std::vector<uint32_t> index(n, 0xffffffffu), low(n, 0);
     std::vector<uint8_t> on_stack(n, 0);
     std::vector<uint32_t> stack;
     std::vector<std::pair<uint32_t, u64>> call;
     uint32_t counter = 0;
-    ncomp = 0;
     for (u64 r = 0; r < n; r++) {
-        if (index[r] != 0xffffffffu) continue;
+        if (index[r] != 0xffffffffu || !in(r)) continue;
         index[r] = low[r] = counter++;
         stack.push_back((uint32_t)r);
         on_stack[r] = 1;
@@ -403,6 +407,7 @@ std::vector<uint32_t> tarjan(const HostCsr& g, u64& ncomp) {
             u64& e = call.back().second;
             if (e < g.off[v + 1]) {
                 const uint32_t w = g.succ[e++];
+                if (!in(w)) continue;
                 if (index[w] == 0xffffffffu) {
                     index[w] = low[w] = counter++;
                     stack.push_back(w);
@@ -427,6 +432,12 @@ std::vector<uint32_t> tarjan(const HostCsr& g, u64& ncomp) {
             if (!call.empty() && low[v] < low[call.back().first]) low[call.back().first] = low[v];
         }
     }
+}
+
+std::vector<uint32_t> tarjan(const HostCsr& g, u64& ncomp) {
+    std::vector<uint32_t> comp(g.n, 0);
+    ncomp = 0;
+    tarjan_into(g, comp, ncomp);
     return comp;
 }
 
@@ -584,6 +595,50 @@ struct Sweeper {
         for (int k = 0; k < g; k++)
             if (hbs::better(h_best[k], b, maximize)) b = h_best[k];
         return b.idx;
+    }
+
+    // The strongly connected components of a directed graph, numbered in a
+    // reverse topological order (sccs/tarjan.rs numbers them as Tarjan's
+    // algorithm emits them). The component of the largest out-degree node
+    // is found on the device, as the nodes that both reach it and are reached
+    // from it (two visits). The other nodes are split into those reached from it
+    // (their components can only lead to components reached from it) and the
+    // rest (whose components can lead to everything). Tarjan's algorithm runs
+    // on each part alone, on the host, the first part numbered first, then the
+    // pivot's component, then the rest: every arc between components goes
+    // from a higher number to a lower one, as in Tarjan's numbering. The
+    // numbering of the reference matters only when two components share the
+    // largest size (computer.rs:498-506 takes the first); then the whole
+    // graph goes through Tarjan's algorithm in node order instead.
+    std::vector<uint32_t> directed_components(const HostCsr& hg) {
+        const u64 p = select(nullptr, nullptr, true, 2, nullptr, nullptr);
+        std::vector<uint32_t> fw(n), bw(n);
+        set_root(p);
+        visit(1, false, false, nullptr);
+        ck(cudaMemcpyAsync(fw.data(), d_dist, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        set_root(p);
+        visit(1, true, false, nullptr);
+        ck(cudaMemcpyAsync(bw.data(), d_dist, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        sync();
+        // group 0: reached from p only; 1: the component of p; 2: the rest
+        std::vector<uint8_t> group(n);
+        for (u64 v = 0; v < n; v++) {
+            const bool f = fw[v] != hbs::INF, b = bw[v] != hbs::INF;
+            group[v] = f && b ? 1 : f ? 0 : 2;
+        }
+        std::vector<uint32_t> comp(n, 0);
+        u64 nc = 0;
+        tarjan_into(hg, comp, nc, group.data(), 0);
+        const uint32_t pc = (uint32_t)nc++;
+        for (u64 v = 0; v < n; v++)
+            if (group[v] == 1) comp[v] = pc;
+        tarjan_into(hg, comp, nc, group.data(), 2);
+        std::vector<u64> sizes(nc, 0);
+        for (u64 v = 0; v < n; v++) sizes[comp[v]]++;
+        const u64 big = *std::max_element(sizes.begin(), sizes.end());
+        if (std::count(sizes.begin(), sizes.end(), big) > 1) return tarjan(hg, ncomp);
+        ncomp = nc;
+        return comp;
     }
 
     // computer.rs:487-542
@@ -852,10 +907,49 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
                      std::chrono::duration<double, std::milli>(now - t_mark).count());
         t_mark = now;
     };
-    // components and the arcs between them (host, as the reference)
     HostCsr hg{n, g->offsets, g->successors};
     HostCsr ht = t ? HostCsr{n, t->offsets, t->successors} : hg;
-    w.comp = w.undirected ? symm_components(hg, w.ncomp) : tarjan(hg, w.ncomp);
+    // the graph on the device first: the components use its visits
+    w.alloc(&w.d_off, n + 1);
+    w.alloc(&w.d_succ, m);
+    if (t) {
+        w.alloc(&w.d_toff, n + 1);
+        w.alloc(&w.d_tsucc, m);
+    } else {
+        w.d_toff = w.d_off;
+        w.d_tsucc = w.d_succ;
+    }
+    for (uint32_t** p : {&w.d_dist, &w.d_queue, &w.d_heavy, &w.d_comp, &w.d_roots, &w.d_df, &w.d_db}) w.alloc(p, n);
+    for (u64** p : {&w.d_fl, &w.d_fh, &w.d_bl, &w.d_bh, &w.d_ft, &w.d_bt}) w.alloc(p, n);
+    w.alloc(&w.d_radial, n);
+    w.alloc(&w.d_cnt, 8);
+    ck(cudaMalloc((void**)&w.d_lev, 6 * 8), "cudaMalloc");
+    w.alloc(&w.d_best, (u64)w.grid);
+    ck(cudaMallocHost((void**)&w.h_cnt, 16 * 8), "cudaMallocHost");
+    ck(cudaMallocHost((void**)&w.h_best, (size_t)w.grid * sizeof(hbs::Best)), "cudaMallocHost");
+    cudaStream_t s = w.s;
+    ck(cudaMemcpyAsync(w.d_off, g->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    if (m) ck(cudaMemcpyAsync(w.d_succ, g->successors, m * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    if (t) {
+        ck(cudaMemcpyAsync(w.d_toff, t->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+        if (m) ck(cudaMemcpyAsync(w.d_tsucc, t->successors, m * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    }
+    // the CSR is checked before any kernel indexes with it
+    {
+        int bad = 0;
+        int* d_bad = (int*)(w.d_cnt + 7);
+        ck(cudaMemsetAsync(d_bad, 0, 4, s), "cudaMemsetAsync");
+        hbs::k_sw_validate<<<w.blocks(std::max(n, m)), hbs::SW_THREADS, 0, s>>>(w.d_off, w.d_succ, n, m, d_bad);
+        if (t) hbs::k_sw_validate<<<w.blocks(std::max(n, m)), hbs::SW_THREADS, 0, s>>>(w.d_toff, w.d_tsucc, n, m, d_bad);
+        ck(cudaGetLastError(), "k_sw_validate");
+        ck(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        w.sync();
+        if (bad) fail(HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
+    }
+    mark("device graph");
+    // components and the arcs between them
+    if (w.undirected) w.comp = symm_components(hg, w.ncomp);
+    else w.comp = w.directed_components(hg);
     w.seg.assign(w.ncomp, 0);
     mark("components");
     if (!w.undirected) {
@@ -901,22 +995,7 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
         }
     }
     mark("component arcs");
-    // device state
     const u64 nc = w.ncomp, nconn = w.ctarget.size();
-    w.alloc(&w.d_off, n + 1);
-    w.alloc(&w.d_succ, m);
-    if (t) {
-        w.alloc(&w.d_toff, n + 1);
-        w.alloc(&w.d_tsucc, m);
-    } else {
-        w.d_toff = w.d_off;
-        w.d_tsucc = w.d_succ;
-    }
-    for (uint32_t** p : {&w.d_dist, &w.d_queue, &w.d_heavy, &w.d_comp, &w.d_roots, &w.d_df, &w.d_db}) w.alloc(p, n);
-    for (u64** p : {&w.d_fl, &w.d_fh, &w.d_bl, &w.d_bh, &w.d_ft, &w.d_bt}) w.alloc(p, n);
-    w.alloc(&w.d_radial, n);
-    w.alloc(&w.d_cnt, 8);
-    ck(cudaMalloc((void**)&w.d_lev, 6 * 8), "cudaMalloc");
     w.alloc(&w.d_ecc_f, nc);
     w.alloc(&w.d_ecc_b, nc);
     w.alloc(&w.d_best_score, nc);
@@ -928,32 +1007,10 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     w.alloc(&w.d_cstart, nconn);
     w.alloc(&w.d_cend, nconn);
     w.alloc(&w.d_gather, nconn);
-    w.alloc(&w.d_best, (u64)w.grid);
-    ck(cudaMallocHost((void**)&w.h_cnt, 16 * 8), "cudaMallocHost");
-    ck(cudaMallocHost((void**)&w.h_best, (size_t)w.grid * sizeof(hbs::Best)), "cudaMallocHost");
-    cudaStream_t s = w.s;
-    ck(cudaMemcpyAsync(w.d_off, g->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-    if (m) ck(cudaMemcpyAsync(w.d_succ, g->successors, m * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-    if (t) {
-        ck(cudaMemcpyAsync(w.d_toff, t->offsets, (n + 1) * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-        if (m) ck(cudaMemcpyAsync(w.d_tsucc, t->successors, m * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-    }
     ck(cudaMemcpyAsync(w.d_comp, w.comp.data(), n * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
     if (nconn) {
         ck(cudaMemcpyAsync(w.d_cstart, w.cstart.data(), nconn * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
         ck(cudaMemcpyAsync(w.d_cend, w.cend.data(), nconn * 4, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
-    }
-    // the CSR is checked before any kernel indexes with it
-    {
-        int bad = 0;
-        int* d_bad = (int*)(w.d_cnt + 7);
-        ck(cudaMemsetAsync(d_bad, 0, 4, s), "cudaMemsetAsync");
-        hbs::k_sw_validate<<<w.blocks(std::max(n, m)), hbs::SW_THREADS, 0, s>>>(w.d_off, w.d_succ, n, m, d_bad);
-        if (t) hbs::k_sw_validate<<<w.blocks(std::max(n, m)), hbs::SW_THREADS, 0, s>>>(w.d_toff, w.d_tsucc, n, m, d_bad);
-        ck(cudaGetLastError(), "k_sw_validate");
-        ck(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
-        w.sync();
-        if (bad) fail(HB_ERR_INVALID, "graph has decreasing offsets or successors >= num_nodes");
     }
     // computer.rs:213-240: lower bounds 0, upper bounds n, totals 0
     ck(cudaMemsetAsync(w.d_fl, 0, n * 8, s), "cudaMemsetAsync");
