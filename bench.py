@@ -1052,8 +1052,10 @@ def run_sumsweep(args):
                    "nodes": g.num_nodes, "arcs": g.num_arcs, "diameter": r["diameter"],
                    "radius": r["radius"], "visits": r["sweeps"],
                    "diameter_iterations": r["diameter_iterations"],
-                   "note": "value and e2e: the whole call from host CSR arrays (components on "
-                           "the host, visits and bounds on the device); device_ms: the device part"},
+                   "note": "value and e2e: the whole call from host CSR arrays (the largest "
+                           "component from two device visits, the other components and the "
+                           "component arcs on the host, visits and bounds on the device); "
+                           "device_ms: the visits and bounds"},
         "device_ms": sum(dev) / len(dev),
         "e2e": {"value": 1e3 / ms, "unit": "runs/s",
                 "h2d_bytes_per_step": 2 * (8 * (g.num_nodes + 1) + 4 * g.num_arcs),

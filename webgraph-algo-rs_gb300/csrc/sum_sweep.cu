@@ -491,6 +491,9 @@ struct Sweeper {
     unsigned long long* h_cnt = nullptr;  // page-locked: [0, 6) a visit's level, 6 root, 7 key, [8, 13) counts
     hbs::Best* h_best = nullptr;          // page-locked copy of the selection's block results
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    static constexpr int LEVELS_AHEAD = 8;
+    cudaGraphExec_t group_graph[2][2] = {};  // [backward][inside components]: LEVELS_AHEAD levels
+    cudaStream_t cap = nullptr;              // capture stream of the groups
     float device_ms = 0.f;
     u64 sweeps = 0;
     // host state (computer.rs:38-89)
@@ -520,6 +523,10 @@ struct Sweeper {
         if (h_best) cudaFreeHost(h_best);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (auto& row : group_graph)
+            for (cudaGraphExec_t g : row)
+                if (g) cudaGraphExecDestroy(g);
+        if (cap) cudaStreamDestroy(cap);
         if (own_stream && s) cudaStreamDestroy(s);
     }
 
@@ -535,9 +542,10 @@ struct Sweeper {
     // visited nodes (d_queue[0, visited), distances in d_dist) and the
     // largest distance in *ecc. Levels are enqueued LEVELS_AHEAD at a time
     // with their bounds in device memory (a level past the last is empty);
-    // the host looks only between groups.
+    // the host looks only between groups. A group is one CUDA graph per kind
+    // of visit (forward or backward, inside components or not), captured
+    // the first time on a private stream and launched on the call's stream.
     u64 visit(u64 count, bool backward, bool in_comp, u64* ecc) {
-        constexpr int LEVELS_AHEAD = 8;
         const u64* off = backward ? d_toff : d_off;
         const uint32_t* succ = backward ? d_tsucc : d_succ;
         const uint32_t* cp = in_comp ? d_comp : nullptr;
@@ -551,15 +559,28 @@ struct Sweeper {
         ck(cudaMemcpyAsync(d_lev, h_cnt, 6 * 8, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
         unsigned long long* tail = reinterpret_cast<unsigned long long*>(d_lev) + 4;
         unsigned long long* heavy_n = tail + 1;
-        for (;;) {
+        auto enqueue = [&](cudaStream_t x) {
             for (int k = 0; k < LEVELS_AHEAD; k++) {
-                hbs::k_sw_expand<<<grid, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
+                hbs::k_sw_expand<<<grid, hbs::SW_THREADS, 0, x>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
                                                                  d_heavy, heavy_n);
-                hbs::k_sw_heavy<<<sms * 4, hbs::SW_THREADS, 0, s>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
+                hbs::k_sw_heavy<<<sms * 4, hbs::SW_THREADS, 0, x>>>(off, succ, cp, d_dist, d_queue, d_lev, tail,
                                                                   d_heavy, heavy_n);
-                hbs::k_sw_advance<<<1, 1, 0, s>>>(d_lev, tail, heavy_n);
+                hbs::k_sw_advance<<<1, 1, 0, x>>>(d_lev, tail, heavy_n);
             }
-            ck(cudaGetLastError(), "k_sw_expand");
+        };
+        cudaGraphExec_t& ge = group_graph[backward ? 1 : 0][in_comp ? 1 : 0];
+        if (!ge) {
+            if (!cap) ck(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+            enqueue(cap);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(cap, &graph);
+            if (e == cudaSuccess) ck(cudaGraphInstantiate(&ge, graph, 0), "cudaGraphInstantiate");
+            if (graph) cudaGraphDestroy(graph);
+            ck(e, "cudaStreamEndCapture");
+        }
+        for (;;) {
+            ck(cudaGraphLaunch(ge, s), "cudaGraphLaunch");
             ck(cudaMemcpyAsync(h_cnt, d_lev, 6 * 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
             sync();
             if (h->b == h->e) break;
