@@ -442,7 +442,7 @@ typedef struct hb_sweep_result {
     double device_ms;                          /* device time of the computation (no reference counterpart) */
 } hb_sweep_result;
 /* OutputLevel::compute_directed(graph, transpose, radial_vertices) when
- * `transpose` is given (output_level.rs:27-36), compute_undirected(graph)
+ * `transpose` is given (output_level.rs:47-53), compute_undirected(graph)
  * for a symmetric graph when it is NULL (a symmetric graph's All is
  * AllForward, computer.rs:109-114). radial_vertices: num_nodes bytes
  * (nonzero: radial) or NULL, which takes the nodes that reach the largest
