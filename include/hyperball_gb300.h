@@ -452,9 +452,9 @@ typedef struct hb_sweep_result {
  * reference's parallel visits leave the radial vertex open among several
  * nodes, the smallest is reported. An empty graph returns HB_ERR_INVALID with
  * the reference's assertion message. The component of the largest
- * out-degree node is found by two device visits; the other strongly
- * connected components and the arcs between components are computed on the
- * host, sequentially, as in the reference (sccs/tarjan.rs, scc_graph.rs).
+ * out-degree node is found by device visits; the other components and the
+ * arcs between components are computed on the host, sequentially, as in the
+ * reference (sccs/tarjan.rs, sccs/symm_seq.rs, scc_graph.rs).
  * stream NULL: a stream of its own. Returns when the results are on the
  * host. */
 int hb_exact_sum_sweep(const hb_graph_view* graph, const hb_graph_view* transpose, int level,

@@ -29,11 +29,12 @@
 //                             (computer.rs:418-475) by three atomicMin passes;
 //   k_sw_refine               the node pass of all_cc_upper_bound.
 // The strongly connected component of the largest out-degree node comes from
-// two device visits; the host runs Tarjan's algorithm on the nodes outside it
-// (see directed_components), the connected components of a symmetric graph
-// (sccs/symm_seq.rs), the arcs between components (scc_graph.rs) and the two
-// passes over the component DAG of all_cc_upper_bound (computer.rs:829-873),
-// which touch one value per component and per DAG arc.
+// two device visits (one for a symmetric graph); the host runs Tarjan's
+// algorithm (sccs/tarjan.rs) or the symmetric labelling (sccs/symm_seq.rs) on
+// the nodes outside it (see directed_components, symmetric_components), and
+// finds the arcs between components (scc_graph.rs) and the two passes over
+// the component DAG of all_cc_upper_bound (computer.rs:829-873), which touch
+// one value per component and per DAG arc.
 //
 // Where the reference's parallel visits leave a choice open (which of the
 // nodes reaching a new minimal radius in one step becomes the radial vertex)
@@ -442,11 +443,10 @@ std::vector<uint32_t> tarjan(const HostCsr& g, u64& ncomp) {
 }
 
 // sccs/symm_seq.rs: components of a symmetric graph in order of their
-// smallest node
-std::vector<uint32_t> symm_components(const HostCsr& g, u64& ncomp) {
-    std::vector<uint32_t> comp(g.n, 0xffffffffu);
+// smallest node (nodes already labelled are skipped, the others numbered
+// from ncomp on)
+void symm_into(const HostCsr& g, std::vector<uint32_t>& comp, u64& ncomp) {
     std::vector<uint32_t> st;
-    ncomp = 0;
     for (u64 r = 0; r < g.n; r++) {
         if (comp[r] != 0xffffffffu) continue;
         comp[r] = (uint32_t)ncomp;
@@ -462,6 +462,12 @@ std::vector<uint32_t> symm_components(const HostCsr& g, u64& ncomp) {
         }
         ncomp++;
     }
+}
+
+std::vector<uint32_t> symm_components(const HostCsr& g, u64& ncomp) {
+    std::vector<uint32_t> comp(g.n, 0xffffffffu);
+    ncomp = 0;
+    symm_into(g, comp, ncomp);
     return comp;
 }
 
@@ -658,6 +664,32 @@ struct Sweeper {
         for (u64 v = 0; v < n; v++) sizes[comp[v]]++;
         const u64 big = *std::max_element(sizes.begin(), sizes.end());
         if (std::count(sizes.begin(), sizes.end(), big) > 1) return tarjan(hg, ncomp);
+        ncomp = nc;
+        return comp;
+    }
+
+    // The components of a symmetric graph: the one of the largest-degree
+    // node from one device visit, the others on the host (symm_seq.rs). The
+    // numbering (symm_seq.rs numbers by smallest node) matters only when two
+    // components share the largest size; then all of them come from the host
+    // in the reference's order.
+    std::vector<uint32_t> symmetric_components(const HostCsr& hg) {
+        const u64 p = select(nullptr, nullptr, true, 2, nullptr, nullptr);
+        std::vector<uint32_t> d(n);
+        set_root(p);
+        visit(1, false, false, nullptr);
+        ck(cudaMemcpyAsync(d.data(), d_dist, n * 4, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+        sync();
+        std::vector<uint32_t> comp(n, 0xffffffffu);
+        u64 nc = 0;
+        for (u64 v = 0; v < n; v++)
+            if (d[v] != hbs::INF) comp[v] = 0;
+        nc = 1;
+        symm_into(hg, comp, nc);
+        std::vector<u64> sizes(nc, 0);
+        for (u64 v = 0; v < n; v++) sizes[comp[v]]++;
+        const u64 big = *std::max_element(sizes.begin(), sizes.end());
+        if (std::count(sizes.begin(), sizes.end(), big) > 1) return symm_components(hg, ncomp);
         ncomp = nc;
         return comp;
     }
@@ -969,7 +1001,7 @@ int run(const hb_graph_view* g, const hb_graph_view* t, int level, const uint8_t
     }
     mark("device graph");
     // components and the arcs between them
-    if (w.undirected) w.comp = symm_components(hg, w.ncomp);
+    if (w.undirected) w.comp = w.symmetric_components(hg);
     else w.comp = w.directed_components(hg);
     w.seg.assign(w.ncomp, 0);
     mark("components");
