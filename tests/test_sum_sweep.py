@@ -306,3 +306,25 @@ def test_device_errors():
     h = hb.Graph.erdos_renyi(60, 3, 1)
     with pytest.raises(hb.HyperBallError, match="transpose"):
         hb.exact_sum_sweep(g, h)
+
+
+REFERENCE_UNDIRECTED = [
+    (3, [(0, 1), (1, 2), (2, 1), (1, 0)], "all"),
+    (9, sym([(0, 1), (1, 2), (0, 3), (3, 4), (0, 5), (5, 6), (0, 7), (7, 8)]), "all"),
+    (4, sym([(0, 1), (0, 2), (1, 3), (2, 3)]), "radius"),
+    (7, sym([(i, (i + 1) % 7) for i in range(7)]), "radius_diameter"),
+    (10, [(i, j) for i in range(10) for j in range(10) if i != j], "all"),
+    (100, [], "all"),
+    (66, sym([(10, 32), (10, 65), (21, 44)]), "radius"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(len(REFERENCE_UNDIRECTED)))
+def test_device_reference_undirected_cases(case):
+    """The reference's undirected cases (tests/test_undir_sum_sweep.rs):
+    one component, several of distinct sizes, and only singletons (a tie
+    for the largest component)."""
+    n, arcs, level = REFERENCE_UNDIRECTED[case]
+    off, suc = csr(n, arcs)
+    device_vs_oracle(off, suc, level=level)
