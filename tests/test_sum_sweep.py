@@ -328,3 +328,28 @@ def test_device_reference_undirected_cases(case):
     n, arcs, level = REFERENCE_UNDIRECTED[case]
     off, suc = csr(n, arcs)
     device_vs_oracle(off, suc, level=level)
+
+
+def test_sweep_argument_errors_need_no_device():
+    """Argument errors are reported before any device work (the reference's
+    assertion message for an empty graph, a transpose of another size); with
+    no device, a valid call fails loudly instead of computing on the host."""
+    import hyperball_gb300 as hb
+    g0 = hb.Graph.from_csr(np.zeros(1, dtype=np.uint64), np.zeros(0, dtype=np.uint32))
+    with pytest.raises(hb.HyperBallError, match="Trying to build All without all eccentricities computed"):
+        hb.exact_sum_sweep(g0, g0)
+    with pytest.raises(hb.HyperBallError, match="Trying to build Radius without the radius computed"):
+        hb.exact_sum_sweep(g0, level="radius")
+    g = hb.Graph.erdos_renyi(50, 3, 1)
+    with pytest.raises(hb.HyperBallError, match="transpose"):
+        hb.exact_sum_sweep(g, hb.Graph.erdos_renyi(60, 3, 1))
+    with pytest.raises(ValueError):
+        hb.exact_sum_sweep(g, g.transpose(), radial_vertices=np.zeros(3, dtype=np.uint8))
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except ImportError:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(hb.NoDeviceError):
+            hb.exact_sum_sweep(g, g.transpose())
