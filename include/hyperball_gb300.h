@@ -509,6 +509,11 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
  * returns HB_ERR_TIMEOUT. hb_init then starts a clean run. Pass (0, 0) to
  * restore the defaults. No reference counterpart. */
 int hb_debug_far_wait(hb_handle* h, uint32_t polls, uint32_t extra_tx_bytes);
+/* Test hook (process-wide): the device allocation of a handle (creation,
+ * discount arrays) that is the (after + 1)-th from now fails once with
+ * HB_ERR_OOM, as a cudaMalloc failure would; after < 0 turns it off. The
+ * failing call releases what it had allocated. No reference counterpart. */
+int hb_debug_fail_allocations(int64_t after);
 
 /* ---- introspection ---------------------------------------------------------- */
 /* Library build string, e.g. "hyperball_gb300 sm_103a". */

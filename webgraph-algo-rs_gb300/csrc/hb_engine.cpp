@@ -16,8 +16,11 @@
 // n-bit bitmaps (modified current/next, must-be-checked current/next).
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -367,9 +370,23 @@ int cuda_err(hb_handle* h, cudaError_t e, const char* what) {
         if (_e != 0) return cuda_err((h), (cudaError_t)_e, #call);            \
     } while (0)
 
+// NVTX range for the scope (iterations, steps, creation): visible in a
+// profiler's timeline, free without one
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+// hb_debug_fail_allocations: the device allocation of a handle that brings
+// this count to zero fails (once); -1: none
+std::atomic<long long> g_fail_alloc_after{-1};
+
 template <class T>
 int dalloc(hb_handle* h, T** out, size_t count) {
     *out = nullptr;
+    if (g_fail_alloc_after.load(std::memory_order_relaxed) >= 0 &&
+        g_fail_alloc_after.fetch_sub(1) == 0)
+        return set_err(h, HB_ERR_OOM, "device allocation failed (injected by hb_debug_fail_allocations)");
     size_t bytes = std::max<size_t>(count * sizeof(T), 256);
     void* p = nullptr;
     // stream-ordered: freeing never synchronises the whole device, so other
@@ -1196,6 +1213,7 @@ int iter_finish(hb_handle* h, IterPlan& p, bool from_graph, double union_ms, hb_
 }
 
 int do_iterate(hb_handle* h, hb_iter_stats* out) {
+    NvtxRange range("hb_iterate");
     IterPlan p;
     iter_plan(h, p);
     cudaStream_t s = h->stream;
@@ -1396,6 +1414,7 @@ static int multi_enqueue(std::vector<hb_handle*>& hs, std::vector<IterPlan>& pla
 // mc.device).
 static int multi_iterate(std::vector<hb_handle*>& hs, MultiCtx& mc) {
     if (hs.empty()) return HB_OK;
+    NvtxRange range("hb_multi_step");
     if (hs.size() > kMaxJobs) {
         mc.err = "more than 48 instances in one step";
         return HB_ERR_INVALID;
@@ -2031,6 +2050,11 @@ int hb_device_transpose_noalloc(const uint64_t* d_offsets, const uint32_t* d_suc
     return HB_OK;
 }
 
+int hb_debug_fail_allocations(int64_t after) {
+    g_fail_alloc_after.store(after < 0 ? -1 : after);
+    return HB_OK;
+}
+
 int hb_debug_far_wait(hb_handle* h, uint32_t polls, uint32_t extra_tx_bytes) {
     if (!h) return set_err(nullptr, HB_ERR_INVALID, "null handle");
     if (extra_tx_bytes > (1u << 19))
@@ -2101,6 +2125,7 @@ struct PhaseTrace {
 
 static int create_impl(const hb_graph_view* graph, const hb_graph_view* transpose,
                        const hb_options* opts, const std::vector<uint64_t>* inst, hb_handle** out) {
+    NvtxRange range("hb_create");
     if (!out) return set_err(nullptr, HB_ERR_INVALID, "out is NULL");
     PhaseTrace trace;
     *out = nullptr;

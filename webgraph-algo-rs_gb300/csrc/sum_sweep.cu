@@ -41,6 +41,7 @@
 // this takes the smallest node; everything else follows the reference's
 // sequence of steps exactly, so the iteration counts match too.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -1121,6 +1122,10 @@ extern "C" {
 int hb_exact_sum_sweep(const hb_graph_view* graph, const hb_graph_view* transpose, int level,
                        const uint8_t* radial_vertices, int device, void* stream, uint64_t* forward_eccentricities,
                        uint64_t* backward_eccentricities, hb_sweep_result* out) {
+    nvtxRangePushA("hb_exact_sum_sweep");
+    struct Pop {
+        ~Pop() { nvtxRangePop(); }
+    } pop;
     try {
         return run(graph, transpose, level, radial_vertices, device, stream, forward_eccentricities,
                    backward_eccentricities, out);

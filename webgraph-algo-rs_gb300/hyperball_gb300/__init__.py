@@ -284,6 +284,7 @@ EXPORTS = [
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p,
       ctypes.c_void_p, ctypes.c_void_p]),
     ("hb_debug_far_wait", ctypes.c_int, [_H, ctypes.c_uint32, ctypes.c_uint32]),
+    ("hb_debug_fail_allocations", ctypes.c_int, [ctypes.c_int64]),
     ("hb_visit_create", ctypes.c_int, [ctypes.POINTER(GraphView), ctypes.c_int, ctypes.c_void_p,
                                        ctypes.POINTER(ctypes.c_void_p)]),
     ("hb_visit_destroy", None, [_H]),
@@ -1075,6 +1076,13 @@ def release_cached_memory(device=0):
 # ---------------------------------------------------------------------------
 # breadth-first visits (src/algo/visits/breadth_first/par_fair.rs)
 # ---------------------------------------------------------------------------
+def debug_fail_allocations(after):
+    """Test hook (hb_debug_fail_allocations): the (after + 1)-th device
+    allocation of a handle from now fails once with HB_ERR_OOM; -1 turns
+    it off."""
+    load_library().hb_debug_fail_allocations(int(after))
+
+
 SWEEP_LEVELS = {"all": 0, "all_forward": 1, "radius_diameter": 2, "diameter": 3, "radius": 4}
 SWEEP_NONE = 2**64 - 1
 
