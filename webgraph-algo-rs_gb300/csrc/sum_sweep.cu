@@ -11,7 +11,8 @@
 //                             node (a block for nodes above SW_HEAVY arcs);
 //                             a successor is claimed by an atomicCAS on its
 //                             distance word and appended to the next level
-//                             with one atomicAdd per warp; an optional
+//                             through a per-warp run in shared memory (one
+//                             atomicAdd per run of up to 128 nodes); an optional
 //                             component array keeps a visit inside each
 //                             start node's strongly connected component
 //                             (computer.rs:745-800: all pivots at once);
@@ -75,6 +76,42 @@ __device__ __forceinline__ void sw_append(bool c, uint32_t s, uint32_t* queue, u
     if (c) queue[base + __popc(mask & ((1u << lane) - 1u))] = s;
 }
 
+// A warp's claimed nodes wait in shared memory and go to the queue in runs
+// of up to SW_RUN slots, one atomicAdd on the tail per run: on a level of
+// many small-degree nodes a per-chunk append puts one same-address atomic
+// in the chain of almost every frontier node.
+constexpr int SW_RUN = 128;
+
+// adds the lanes' claimed nodes to the warp's run, writing the run out when
+// another chunk might not fit (every lane of the warp calls it)
+__device__ __forceinline__ void sw_stage(bool c, uint32_t s, uint32_t* run, int& fill, uint32_t* queue,
+                                         unsigned long long* tail) {
+    const unsigned mask = __ballot_sync(0xffffffffu, c);
+    const int lane = threadIdx.x & 31;
+    if (c) run[fill + __popc(mask & ((1u << lane) - 1u))] = s;
+    fill += __popc(mask);
+    if (fill > SW_RUN - 32) {
+        __syncwarp();
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(tail, (unsigned long long)fill);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (int k = lane; k < fill; k += 32) queue[base + k] = run[k];
+        __syncwarp();
+        fill = 0;
+    }
+}
+
+// writes out what is left of the warp's run
+__device__ __forceinline__ void sw_flush(const uint32_t* run, int fill, uint32_t* queue, unsigned long long* tail) {
+    if (fill == 0) return;
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(tail, (unsigned long long)fill);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int k = lane; k < fill; k += 32) queue[base + k] = run[k];
+}
+
 // The level state of a visit in device memory, so that the host enqueues
 // several levels before it looks: queue slots [b, e) are the frontier (at
 // distance d - 1), d the distance its successors get, last the largest
@@ -88,6 +125,9 @@ __global__ void k_sw_expand(const uint64_t* __restrict__ off, const uint32_t* __
                             const uint32_t* __restrict__ comp, uint32_t* dist, uint32_t* queue,
                             const Level* lev, unsigned long long* tail, uint32_t* heavy,
                             unsigned long long* heavy_n) {
+    __shared__ uint32_t runs[SW_THREADS / 32][SW_RUN];
+    uint32_t* run = runs[threadIdx.x >> 5];
+    int fill = 0;  // the same in every lane of the warp
     const uint64_t b = lev->b, e = lev->e;
     const uint32_t d = (uint32_t)lev->d;
     const int lane = threadIdx.x & 31;
@@ -109,9 +149,10 @@ __global__ void k_sw_expand(const uint64_t* __restrict__ off, const uint32_t* __
                 s = __ldg(succ + x);
                 c = (!comp || __ldg(comp + s) == cv) && sw_claim(dist, s, d);
             }
-            sw_append(c, s, queue, tail);
+            sw_stage(c, s, run, fill, queue, tail);
         }
     }
+    sw_flush(run, fill, queue, tail);
 }
 
 // the deferred nodes of a level, one block each
