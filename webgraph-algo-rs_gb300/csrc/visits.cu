@@ -12,9 +12,11 @@
 //   k_visit_expand  one warp per frontier node walks its successors 32 at a
 //                   time; a successor whose visited bit a lane sets first
 //                   (atomicOr, after a plain read that skips the common
-//                   already-visited case) is appended to the next level
-//                   with one atomicAdd per warp; nodes with more than
-//                   HEAVY_MIN successors are deferred to
+//                   already-visited case) is staged with its predecessor
+//                   in the warp's run in shared memory, and a run goes to
+//                   the next level with one atomicAdd on the tail per up to
+//                   RUN nodes; nodes with more than HEAVY_MIN successors
+//                   are deferred to
 //   k_visit_heavy   one block per node.
 // The Unknown events of the reference (node, pred, distance) are the queue
 // slots of the visit with the level of each slot; Known events are counted.
@@ -57,6 +59,45 @@ __device__ __forceinline__ void append(bool c, uint32_t s, uint32_t p, uint32_t*
     }
 }
 
+// A warp's claimed nodes and their predecessors wait in shared memory and
+// go to the queue in runs of up to RUN slots: a per-chunk append puts one
+// same-address atomic on the tail in the chain of almost every frontier
+// node of a level of many small-degree nodes.
+constexpr int RUN = 128;
+constexpr int EXPAND_THREADS = 256;
+
+// writes the warp's run [0, fill) to the queue (every lane of the warp)
+__device__ __forceinline__ void write_run(const uint32_t* rn, const uint32_t* rp, int fill, uint32_t* queue,
+                                          uint32_t* pred, unsigned long long* tail) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(tail, (unsigned long long)fill);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (int k = lane; k < fill; k += 32) {
+        queue[base + k] = rn[k];
+        pred[base + k] = rp[k];
+    }
+    __syncwarp();
+}
+
+// adds the lanes' claimed nodes (predecessor p) to the warp's run, writing
+// the run out when another chunk might not fit (every lane of the warp)
+__device__ __forceinline__ void stage(bool c, uint32_t s, uint32_t p, uint32_t* rn, uint32_t* rp, int& fill,
+                                      uint32_t* queue, uint32_t* pred, unsigned long long* tail) {
+    const unsigned mask = __ballot_sync(0xffffffffu, c);
+    if (c) {
+        const int k = fill + __popc(mask & ((1u << (threadIdx.x & 31)) - 1u));
+        rn[k] = s;
+        rp[k] = p;
+    }
+    fill += __popc(mask);
+    if (fill > RUN - 32) {
+        write_run(rn, rp, fill, queue, pred, tail);
+        fill = 0;
+    }
+}
+
 __global__ void k_visit_roots(const uint32_t* __restrict__ roots, uint64_t nroots, uint32_t* visited,
                               uint32_t* queue, uint32_t* pred, unsigned long long* tail) {
     // whole warps iterate together (the limit is a multiple of 32) so that
@@ -76,6 +117,10 @@ __global__ void k_visit_expand(const uint64_t* __restrict__ off, const uint32_t*
                                uint32_t* visited, uint32_t* queue, uint32_t* pred, uint64_t b,
                                uint64_t e, unsigned long long* tail, uint32_t* heavy,
                                unsigned long long* heavy_n, unsigned long long* known) {
+    __shared__ uint32_t run_node[EXPAND_THREADS / 32][RUN], run_pred[EXPAND_THREADS / 32][RUN];
+    uint32_t* rn = run_node[threadIdx.x >> 5];
+    uint32_t* rp = run_pred[threadIdx.x >> 5];
+    int fill = 0;  // the same in every lane of the warp
     const int lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -96,9 +141,10 @@ __global__ void k_visit_expand(const uint64_t* __restrict__ off, const uint32_t*
                 c = claim(visited, s);
                 kn += !c;
             }
-            append(c, s, v, queue, pred, tail);
+            stage(c, s, v, rn, rp, fill, queue, pred, tail);
         }
     }
+    if (fill) write_run(rn, rp, fill, queue, pred, tail);
     if (kn) atomicAdd(known, kn);
 }
 
@@ -332,8 +378,9 @@ int hb_visit_run(hb_visit* v, const uint64_t* roots, size_t nroots, uint64_t max
         uint64_t d = 0;
         while (e > b && d < max_distance) {
             VC(v, cudaMemsetAsync(v->d_cnt + 1, 0, 8, s), "cudaMemsetAsync");
-            const int g1 = (int)std::min<uint64_t>(((e - b) * 32 + 255) / 256, (uint64_t)egrid);
-            hbv::k_visit_expand<<<g1, 256, 0, s>>>(v->d_off, v->d_succ, v->d_visited, v->d_queue, v->d_pred,
+            const int g1 = (int)std::min<uint64_t>(((e - b) * 32 + hbv::EXPAND_THREADS - 1) / hbv::EXPAND_THREADS,
+                                                   (uint64_t)egrid);
+            hbv::k_visit_expand<<<g1, hbv::EXPAND_THREADS, 0, s>>>(v->d_off, v->d_succ, v->d_visited, v->d_queue, v->d_pred,
                                                    b, e, v->d_cnt, v->d_heavy, v->d_cnt + 1, v->d_cnt + 2);
             VC(v, cudaGetLastError(), "k_visit_expand");
             hbv::k_visit_heavy<<<hgrid, 256, 0, s>>>(v->d_off, v->d_succ, v->d_visited, v->d_queue, v->d_pred,
