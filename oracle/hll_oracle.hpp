@@ -13,10 +13,13 @@
 // checker. Nothing in the product path includes this file.
 //
 // Parity status: the HLL arithmetic and the Jenkins hasher are pinned by the
-// reference's Java-produced cnr-2000 goldens (tests/hyperball_results/*); the
-// SipHash round function is pinned by the SipHash-2-4 test vector of the paper,
-// but the SipHash-1-3 node hash itself (Rust's DefaultHasher) is parity-unpinned
-// because no reference test fixes a DefaultHasher output.
+// reference's Java-produced cnr-2000 goldens (tests/hyperball_results/*). No
+// reference test fixes a DefaultHasher output; the SipHash round function is
+// pinned by the SipHash-2-4 test vector of the paper, and the SipHash-1-3 node
+// hash by an independent SipHash-1-3: CPython's bytes hash, whose key is zero
+// under PYTHONHASHSEED=0 as Rust's DefaultHasher::new() key is (1,012 values,
+// tests/test_oracle.py). What stays assumed is Rust std's DefaultHasher itself
+// (SipHash-1-3, zero keys, a usize written as its 8 little-endian bytes).
 #pragma once
 
 #include <algorithm>

@@ -7,6 +7,8 @@
 * HyperLogLog arithmetic: merge is the register-wise max, count quirk,
   register size, SipHash round function (paper vector), statistical accuracy
   (tests/test_hyperloglog_counter.rs).
+* The default node hash (Rust's DefaultHasher, SipHash-1-3 with zero keys)
+  against CPython's SipHash-1-3 bytes hash under PYTHONHASHSEED=0.
 """
 import hashlib
 import json
@@ -225,6 +227,39 @@ def test_sip13_is_siphash13_of_le_bytes(oracle):
     L = oracle.lib()
     for x in (0, 1, 12345, 2**63 + 7):
         assert L.hbo_hash(0, 0, x) == L.hbo_siphash(1, 3, 0, 0, x.to_bytes(8, "little"), 8)
+
+
+def test_sip13_matches_cpython_siphash13(oracle):
+    """The node hash against an independent SipHash-1-3. CPython hashes bytes
+    with SipHash-1-3 (sys.hash_info.algorithm 'siphash13', no small-input
+    cutoff), and with PYTHONHASHSEED=0 its 128-bit key is all zero bits: the
+    key of Rust's DefaultHasher::new(), which the reference's HyperBall uses
+    (hyperball_impl.rs:69, hyper_log_log_logic.rs:241-246). So in such an
+    interpreter hash(x.to_bytes(8, 'little')) is the node hash of x, as a
+    signed 64-bit value (CPython maps -1 to -2)."""
+    import subprocess
+    import sys
+    rng = np.random.default_rng(11)
+    xs = [0, 1, 2, 3, 255, 256, 65535, 1 << 20, (1 << 26) - 1, (1 << 32) + 1, 2**63, 2**64 - 1]
+    xs += [int(v) for v in rng.integers(0, 1 << 26, size=500, dtype=np.uint64)]
+    xs += [int(v) for v in rng.integers(0, 2**63, size=500, dtype=np.uint64) * 2 + 1]
+    code = ("import sys; h = sys.hash_info; print(h.algorithm, h.cutoff); "
+            "[print(hash(int(t).to_bytes(8, 'little'))) for t in sys.stdin.read().split()]")
+    env = dict(os.environ, PYTHONHASHSEED="0")
+    out = subprocess.run([sys.executable, "-c", code], input=" ".join(map(str, xs)), env=env,
+                         capture_output=True, text=True, check=True).stdout.split("\n")
+    algorithm, cutoff = out[0].split()
+    if algorithm != "siphash13" or cutoff != "0":
+        pytest.skip(f"this interpreter hashes bytes with {algorithm} (cutoff {cutoff})")
+    L = oracle.lib()
+    checked = 0
+    for x, line in zip(xs, out[1:]):
+        py = int(line)
+        if py == -2:
+            continue  # SipHash output -1 or -2: CPython returns -2 for both
+        assert L.hbo_hash(0, 0, x) == py & (2**64 - 1), x
+        checked += 1
+    assert checked == len(xs)
 
 
 def _splitmix(seed, xs):
