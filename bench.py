@@ -368,9 +368,12 @@ def run_reference(args):
         return 0
     if args.workload == "sumsweep":
         return run_reference_sumsweep(args)
+    if args.workload == "visit":
+        return run_reference_visit(args)
     if args.workload not in ("weblike", "rmat"):
         print(json.dumps({"impl": "reference", "unavailable":
-                          "the CPU arm times the single-graph workloads (weblike, rmat) and sumsweep"}),
+                          "the CPU arm times the single-graph workloads (weblike, rmat, visit) "
+                          "and sumsweep"}),
               flush=True)
         return 0
     g = make_oracle_graph(args)
@@ -396,6 +399,46 @@ def run_reference(args):
     return 0
 
 
+def run_reference_visit(args):
+    """The oracle's fair parallel visit (par_fair.rs restated, all host
+    threads) of the graph of --workload visit from node 0; each step is one
+    complete visit after a reset."""
+    import numpy as np
+    from oracle import hbo
+    g = make_oracle_graph(args)
+    o = hbo.OracleVisit(g.offsets, g.successors)
+    threads = os.cpu_count() or 1
+    for _ in range(min(args.warmup, 1)):
+        o.reset()
+        nodes = o.par_visit([0], threads=threads)[0]
+    off = np.asarray(g.offsets)
+    idx = nodes.astype(np.int64)
+    arcs = int(np.sum(off[idx + 1] - off[idx]))
+    steps = max(1, min(args.steps, 3))
+    secs = []
+    for _ in range(steps):
+        o.reset()
+        t0 = time.perf_counter()
+        nodes, _, dists = o.par_visit([0], threads=threads)
+        secs.append(time.perf_counter() - t0)
+    dt = sum(secs) / steps
+    line = {
+        "impl": "reference", "metric": "breadth-first visit arcs examined/s", "value": arcs / dt,
+        "unit": "arcs/s", "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1),
+        "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic",
+        "config": {"workload": f"weblike-2^{args.log2n} breadth-first visit from node 0",
+                   "nodes": g.num_nodes, "arcs": g.num_arcs, "visited": len(nodes),
+                   "levels": int(dists.max()) + 1 if len(dists) else 0, "arcs_examined": arcs},
+        "cpu_baseline": {"value": arcs / dt, "unit": "arcs/s", "cores": threads, "kind": "port",
+                         "sample": f"fair parallel breadth-first visit (par_fair.rs restated) on "
+                                   f"{threads} threads, complete visits"},
+        "e2e": {"value": arcs / dt, "unit": "arcs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference_sumsweep(args):
     """The oracle's ExactSumSweep (sequential visits) on the graph of
     --workload sumsweep; each step is one complete call."""
@@ -403,12 +446,13 @@ def run_reference_sumsweep(args):
     g = hbo.OracleGraph.weblike(1 << args.log2n)
     t = g.transpose()
     level = "radius_diameter"
+    threads = os.cpu_count() or 1
     for _ in range(min(args.warmup, 1)):
-        hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+        hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level, threads=threads)
     steps = max(1, min(args.steps, 2))
     t0 = time.perf_counter()
     for _ in range(steps):
-        r = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+        r = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level, threads=threads)
     dt = (time.perf_counter() - t0) / steps
     line = {
         "impl": "reference", "metric": "ExactSumSweep RadiusDiameter runs/s", "value": 1.0 / dt,
@@ -418,8 +462,9 @@ def run_reference_sumsweep(args):
         "config": {"workload": f"weblike-2^{args.log2n} ExactSumSweep RadiusDiameter (directed)",
                    "nodes": g.num_nodes, "arcs": g.num_arcs, "diameter": r["diameter"],
                    "radius": r["radius"], "diameter_iterations": r["diameter_iterations"]},
-        "cpu_baseline": {"value": 1.0 / dt, "unit": "runs/s", "cores": 1, "kind": "port",
-                         "sample": "ExactSumSweep restated (computer.rs), sequential visits"},
+        "cpu_baseline": {"value": 1.0 / dt, "unit": "runs/s", "cores": threads, "kind": "port",
+                         "sample": f"ExactSumSweep restated (computer.rs), fair parallel visits on "
+                                   f"{threads} threads"},
         "e2e": {"value": 1.0 / dt, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -981,13 +1026,15 @@ def run_visit(args):
     if not args.no_cpu_baseline:
         from oracle import hbo
         o = hbo.OracleVisit(g.offsets, g.successors)
+        threads = os.cpu_count() or 1
         t = time.perf_counter()
-        on = o.visit([0])[0]
+        on = o.par_visit([0], threads=threads)[0]
         dt = time.perf_counter() - t
         if len(on) != st["visited"]:
             raise RuntimeError("the oracle's visit reached another number of nodes")
-        cpu = {"value": arcs / dt, "unit": "arcs/s", "cores": 1, "kind": "port",
-               "sample": f"sequential breadth-first visit (seq.rs restated), the same visit, {dt:.1f} s"}
+        cpu = {"value": arcs / dt, "unit": "arcs/s", "cores": threads, "kind": "port",
+               "sample": f"fair parallel breadth-first visit (par_fair.rs restated) on {threads} threads, "
+                         f"the same visit, {dt:.2f} s"}
     line = {
         "metric": "breadth-first visit arcs examined/s", "value": arcs / (device_ms / 1e3),
         "unit": "arcs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -1034,15 +1081,17 @@ def run_sumsweep(args):
     cpu, parity = None, None
     if not args.no_cpu_baseline:
         from oracle import hbo
+        threads = os.cpu_count() or 1
         t0 = time.perf_counter()
-        o = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level)
+        o = hbo.sum_sweep(g.offsets, g.successors, t.offsets, t.successors, level=level, threads=threads)
         dt = time.perf_counter() - t0
         if any(o[f] != r[f] for f in fields):
             raise RuntimeError("ExactSumSweep differs from the oracle")
         parity = {"oracle": "oracle/sum_sweep_oracle.cpp", "result": "match",
                   "checked": ", ".join(fields)}
-        cpu = {"value": 1.0 / dt, "unit": "runs/s", "cores": 1, "kind": "port",
-               "sample": f"ExactSumSweep restated (computer.rs), sequential visits, one run, {dt:.1f} s"}
+        cpu = {"value": 1.0 / dt, "unit": "runs/s", "cores": threads, "kind": "port",
+               "sample": f"ExactSumSweep restated (computer.rs), fair parallel visits on {threads} "
+                         f"threads, one run, {dt:.1f} s"}
     line = {
         "metric": "ExactSumSweep RadiusDiameter runs/s", "value": 1e3 / ms,
         "unit": "runs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

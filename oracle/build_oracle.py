@@ -20,7 +20,8 @@ LIB = os.path.join(OUT_DIR, "libhb_oracle.so")
 GEN_DIR = os.path.join(os.path.dirname(HERE), "webgraph-algo-rs_gb300", "csrc")
 SOURCES = [os.path.join(HERE, "hyperball_oracle.cpp"), os.path.join(HERE, "visits_oracle.cpp"),
            os.path.join(HERE, "sum_sweep_oracle.cpp"), os.path.join(GEN_DIR, "graph_gen.cpp")]
-HEADERS = [os.path.join(HERE, "hll_oracle.hpp"), os.path.join(GEN_DIR, "graph_gen.h")]
+HEADERS = [os.path.join(HERE, "hll_oracle.hpp"), os.path.join(HERE, "par_fair.hpp"),
+           os.path.join(GEN_DIR, "graph_gen.h")]
 
 
 def _stale():

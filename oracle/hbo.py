@@ -112,6 +112,15 @@ def lib():
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
                                                 _P(ctypes.c_uint64), _P(ctypes.c_uint64),
                                                 ctypes.c_uint64, _P(ctypes.c_uint64)]),
+            "hbo_par_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
+                                                    ctypes.c_uint64, ctypes.c_uint32,
+                                                    _P(ctypes.c_uint64), _P(ctypes.c_uint64),
+                                                    _P(ctypes.c_uint64), ctypes.c_uint64,
+                                                    _P(ctypes.c_uint64)]),
+            "hbo_sum_sweep_par": (ctypes.c_int, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                                 _P(ctypes.c_uint64), _P(ctypes.c_uint32), ctypes.c_int,
+                                                 V, _P(ctypes.c_uint64), _P(ctypes.c_uint64),
+                                                 _P(ctypes.c_uint64), ctypes.c_uint32]),
         }
         for k, (r, a) in sig.items():
             f = getattr(L, k)
@@ -322,7 +331,10 @@ class SeqHyperBall:
 class OracleVisit:
     """The reference's sequential breadth-first visit (seq.rs:113-224)
     restated: visit(roots) returns the Unknown events (node, pred, distance)
-    in event order; the visited set persists until reset()."""
+    in event order; the visited set persists until reset(). par_visit is the
+    fair parallel visit with predecessors (par_fair.rs:226-323) on host
+    threads, on the same visited set. Both leave the number of Known events
+    in `known`."""
 
     def __init__(self, offsets, successors):
         self._off = np.ascontiguousarray(offsets, dtype=np.uint64)
@@ -350,6 +362,22 @@ class OracleVisit:
         P = lambda a: a.ctypes.data_as(_P(ctypes.c_uint64))
         k = lib().hbo_visit_run(self._h, P(r), len(r), md, P(nodes), P(preds), P(dists), cap,
                                 ctypes.byref(known))
+        self.known = known.value
+        return nodes[:k], preds[:k], dists[:k]
+
+    def par_visit(self, roots, max_distance=None, threads=None):
+        r = np.ascontiguousarray(roots, dtype=np.uint64)
+        cap = self.n
+        nodes = np.zeros(cap, dtype=np.uint64)
+        preds = np.zeros(cap, dtype=np.uint64)
+        dists = np.zeros(cap, dtype=np.uint64)
+        known = ctypes.c_uint64()
+        md = 2**64 - 1 if max_distance is None else int(max_distance)
+        th = (os.cpu_count() or 1) if threads is None else max(1, int(threads))
+        P = lambda a: a.ctypes.data_as(_P(ctypes.c_uint64))
+        k = lib().hbo_par_visit_run(self._h, P(r), len(r), md, th, P(nodes), P(preds), P(dists), cap,
+                                    ctypes.byref(known))
+        self.known = known.value
         return nodes[:k], preds[:k], dists[:k]
 
     def visit_each(self, roots):
@@ -365,9 +393,12 @@ SWEEP_LEVELS = {"all": 0, "all_forward": 1, "radius_diameter": 2, "diameter": 3,
 NOT_COMPUTED = 2**64 - 1
 
 
-def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all", radial=None):
+def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all", radial=None,
+              threads=1):
     """ExactSumSweep restated (src/algo/exact_sum_sweep/computer.rs): a
     directed graph with its transpose, or a symmetric graph without one.
+    threads > 1 runs its visits as fair parallel visits on that many host
+    threads (the results are the same).
     Returns the output level's fields (eccentricities as uint64 arrays;
     iterations and the radius of a graph without radial vertices as
     NOT_COMPUTED = 2^64 - 1), or None when the level's outputs were not all
@@ -386,9 +417,10 @@ def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all
     be = np.zeros(max(n, 1), dtype=np.uint64)
     res = np.zeros(8, dtype=np.uint64)
     lv = SWEEP_LEVELS[level]
-    r = lib().hbo_sum_sweep(n, P64(off), P32(suc), None if undirected else P64(toff),
-                            None if undirected else P32(tsuc), lv,
-                            None if rad is None else rad.ctypes.data, P64(fe), P64(be), P64(res))
+    r = lib().hbo_sum_sweep_par(n, P64(off), P32(suc), None if undirected else P64(toff),
+                                None if undirected else P32(tsuc), lv,
+                                None if rad is None else rad.ctypes.data, P64(fe), P64(be), P64(res),
+                                max(1, int(threads)))
     if r != 0:
         return None
     out = {"diameter": int(res[0]), "radius": int(res[1]), "diametral_vertex": int(res[2]),

@@ -17,6 +17,8 @@
 #include <deque>
 #include <vector>
 
+#include "par_fair.hpp"
+
 namespace {
 
 using u64 = uint64_t;
@@ -44,6 +46,22 @@ void bfs(const Csr& g, u64 root, std::vector<u64>& dist) {
             dist[s] = dist[v] + 1;
             q.push_back(s);
         }
+    }
+}
+
+// The same distances from the reference's fair parallel visit on `threads`
+// threads (par_fair.rs:274-322, one level at a time; see par_fair.hpp), the
+// visit the reference's ExactSumSweep runs.
+void par_bfs(const Csr& g, u64 root, std::vector<u64>& dist, unsigned threads) {
+    std::vector<uint8_t> visited(g.n, 0);
+    std::vector<hbo_par::Item> cur{{(uint32_t)root, (uint32_t)root}}, next;
+    visited[root] = 1;
+    for (u64 d = 0; !cur.empty(); d++) {
+        hbo_par::parallel_ranges(threads, cur.size(), [&](unsigned, u64 b, u64 e) {
+            for (u64 i = b; i < e; i++) dist[cur[i].first] = d;
+        });
+        hbo_par::expand_level(g.off, g.succ, cur, visited.data(), threads, next);
+        std::swap(cur, next);
     }
 }
 
@@ -180,6 +198,12 @@ struct Computer {
     u64 ncomp = 0;
     std::vector<u64> seg;
     std::vector<Conn> conns;
+    unsigned threads = 1;  // > 1: the visits run level by level on this many threads
+
+    void visit(const Csr& h, u64 root, std::vector<u64>& d) const {
+        if (threads > 1) par_bfs(h, root, d, threads);
+        else bfs(h, root, d);
+    }
 
     bool inc_f(u64 i) const { return forward_low[i] != forward_high[i]; }
     bool inc_b(u64 i) const { return backward_low[i] != backward_high[i]; }
@@ -218,7 +242,7 @@ struct Computer {
             if (comp[v] == big) break;
         }
         std::vector<u64> d(n, NONE);
-        bfs(t, v, d);
+        visit(t, v, d);
         for (u64 i = 0; i < n; i++)
             if (d[i] != NONE) radial[i] = 1;
     }
@@ -226,7 +250,7 @@ struct Computer {
     // computer.rs:644-693
     void forward_step(u64 start) {
         std::vector<u64> d(n, NONE);
-        bfs(g, start, d);
+        visit(g, start, d);
         u64 ecc = 0;
         for (u64 v = 0; v < n; v++) {
             if (d[v] == NONE) continue;
@@ -248,7 +272,7 @@ struct Computer {
     // computer.rs:572-642 (a new minimal radius: the smallest such node)
     void backward_step(u64 start) {
         std::vector<u64> d(n, NONE);
-        bfs(t, start, d);
+        visit(t, start, d);
         u64 ecc = 0, r = radius_high, rv = radius_vertex;
         for (u64 v = 0; v < n; v++) {
             if (d[v] == NONE) continue;
@@ -447,6 +471,8 @@ struct Computer {
 
 extern "C" {
 
+// hbo_sum_sweep_par (visits on `threads` threads) and hbo_sum_sweep (on the
+// calling thread; the results do not depend on it):
 // ExactSumSweep of a directed graph (toff/tsucc: its transpose) or, with
 // toff == NULL, of a symmetric graph. level: 0 All, 1 AllForward,
 // 2 RadiusDiameter, 3 Diameter, 4 Radius (output_level.rs). radial: n bytes
@@ -456,10 +482,11 @@ extern "C" {
 // to fecc / becc when given (All: forward_low and backward_high; AllForward
 // and symmetric All: forward_low). Returns 0, or -1 when the level's outputs
 // were not all computed (output_level.rs asserts; an empty graph).
-int hbo_sum_sweep(uint64_t n, const uint64_t* off, const uint32_t* succ, const uint64_t* toff,
-                  const uint32_t* tsucc, int level, const uint8_t* radial, uint64_t* fecc,
-                  uint64_t* becc, uint64_t* res) {
+int hbo_sum_sweep_par(uint64_t n, const uint64_t* off, const uint32_t* succ, const uint64_t* toff,
+                      const uint32_t* tsucc, int level, const uint8_t* radial, uint64_t* fecc,
+                      uint64_t* becc, uint64_t* res, uint32_t threads) {
     Computer c;
+    c.threads = threads;
     c.n = n;
     c.g = Csr{n, off, succ};
     const bool undirected = toff == nullptr;
@@ -507,6 +534,12 @@ int hbo_sum_sweep(uint64_t n, const uint64_t* off, const uint32_t* succ, const u
     if (becc && c.out == ALL)
         for (u64 i = 0; i < n; i++) becc[i] = c.backward_high[i];
     return 0;
+}
+
+int hbo_sum_sweep(uint64_t n, const uint64_t* off, const uint32_t* succ, const uint64_t* toff,
+                  const uint32_t* tsucc, int level, const uint8_t* radial, uint64_t* fecc,
+                  uint64_t* becc, uint64_t* res) {
+    return hbo_sum_sweep_par(n, off, succ, toff, tsucc, level, radial, fecc, becc, res, 1);
 }
 
 // Forward eccentricity of every node by one breadth-first visit each (the

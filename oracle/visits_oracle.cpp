@@ -5,11 +5,17 @@
 // already visited are skipped, each root is an Unknown event at distance 0,
 // a FIFO queue with a level separator gives the distances) with the
 // distance filter of its documentation example (seq.rs:78-80: nodes farther
-// than max_distance are neither reported nor marked). Only tests/ and
-// bench.py's CPU-baseline leg load it; the product never does.
+// than max_distance are neither reported nor marked), and of the fair
+// parallel visit with predecessors (par_fair.rs:226-323, hbo_par_visit_run)
+// on host threads. Only tests/ and bench.py's CPU-baseline leg load it; the
+// product never does.
+#include <algorithm>
 #include <cstdint>
 #include <deque>
+#include <utility>
 #include <vector>
+
+#include "par_fair.hpp"
 
 struct hbo_visit {
     uint64_t n;
@@ -83,6 +89,46 @@ uint64_t hbo_visit_run(void* vv, const uint64_t* roots, uint64_t nroots, uint64_
             distance++;
             queue.push_back(UINT64_MAX);
         }
+    }
+    if (known) *known = kn;
+    return cnt;
+}
+
+// One fair parallel visit with predecessors (ParFairPred, par_fair.rs:226-323)
+// on `threads` threads, sharing the handle's visited set with hbo_visit_run.
+// Roots not yet visited form level 0 (par_fair.rs:243-258); every frontier
+// node is an Unknown event (node, pred, distance), level by level, in the
+// order of the frontier (free within a level, as in the reference); the next
+// level comes from hbo_par::expand_level. The distance filter (nodes farther
+// than max_distance are neither reported nor marked) rejects every successor
+// of the level at max_distance, so those arcs are not Known events either
+// (par_fair.rs:295-309: Known only for arcs the filter passes). Returns the
+// number of Unknown events (at most `capacity` stored).
+uint64_t hbo_par_visit_run(void* vv, const uint64_t* roots, uint64_t nroots, uint64_t max_distance,
+                           uint32_t threads, uint64_t* nodes, uint64_t* preds, uint64_t* dists,
+                           uint64_t capacity, uint64_t* known) {
+    hbo_visit* v = (hbo_visit*)vv;
+    std::vector<hbo_par::Item> cur, next;
+    for (uint64_t i = 0; i < nroots; i++) {
+        const uint64_t r = roots[i];
+        if (v->visited[r]) continue;
+        v->visited[r] = 1;
+        cur.push_back({(uint32_t)r, (uint32_t)r});
+    }
+    uint64_t cnt = 0, kn = 0;
+    for (uint64_t d = 0; !cur.empty(); d++) {
+        const uint64_t base = cnt, stored = cnt < capacity ? std::min<uint64_t>(cur.size(), capacity - cnt) : 0;
+        hbo_par::parallel_ranges(threads, stored, [&](unsigned, uint64_t b, uint64_t e) {
+            for (uint64_t i = b; i < e; i++) {
+                nodes[base + i] = cur[i].first;
+                preds[base + i] = cur[i].second;
+                dists[base + i] = d;
+            }
+        });
+        cnt += cur.size();
+        if (d >= max_distance) break;
+        kn += hbo_par::expand_level(v->off, v->succ, cur, v->visited.data(), threads, next);
+        std::swap(cur, next);
     }
     if (known) *known = kn;
     return cnt;

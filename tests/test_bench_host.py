@@ -106,6 +106,35 @@ def test_reference_arm_loads_only_oracle_libraries():
     assert "MAPS False True" in r.stdout
 
 
+@pytest.mark.parametrize("workload,metric,config_keys", [
+    ("visit", "breadth-first visit arcs examined/s",
+     {"workload", "nodes", "arcs", "visited", "levels", "arcs_examined"}),
+    ("sumsweep", "ExactSumSweep RadiusDiameter runs/s",
+     {"workload", "nodes", "arcs", "diameter", "radius", "diameter_iterations"}),
+])
+def test_reference_arm_of_the_visit_and_sumsweep_workloads(workload, metric, config_keys):
+    """The CPU arm of the breadth-first visit and ExactSumSweep workloads: the
+    oracle's fair parallel visits on every host thread, the GPU arm's metric
+    and config keys, and no library of the product in the process."""
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--workload', "
+            f"'{workload}', '--log2n', '15', '--steps', '1', '--warmup', '1']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\n"
+            "except SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('MAPS', 'libhyperball_gb300' in maps, 'libhb_oracle' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600,
+                       cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout.strip().splitlines()
+    assert out[-1] == "MAPS False True"
+    line = json.loads(out[-2])
+    assert line["impl"] == "reference" and line["metric"] == metric and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["cpu_baseline"]["cores"] == (os.cpu_count() or 1)
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert set(line["config"]) == config_keys
+
+
 def test_reference_arm_other_ranks_exit_quietly():
     env = dict(os.environ, RANK="1", WORLD_SIZE="2")
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",

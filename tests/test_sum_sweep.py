@@ -206,6 +206,38 @@ def test_levels_agree_with_the_definition(level):
             np.testing.assert_array_equal(r["backward_eccentricities"], be)
 
 
+@pytest.mark.parametrize("kind", ["weblike", "rmat", "undirected"])
+def test_parallel_visits_give_the_same_result(kind):
+    """The oracle with its visits as fair parallel visits on host threads
+    (par_fair.rs, the visit the reference's ExactSumSweep runs; levels of
+    4,096 nodes and more split among the threads) gives every field of the
+    sequential run."""
+    if kind == "weblike":
+        g = hbo.OracleGraph.weblike(1 << 16)
+    elif kind == "rmat":
+        g = hbo.OracleGraph.rmat(15, 8, 0.57, 0.19, 0.19, seed=3)
+    else:
+        # an R-MAT graph with each arc also reversed
+        e = hbo.OracleGraph.rmat(15, 8, 0.57, 0.19, 0.19, seed=5)
+        n = e.num_nodes
+        src = np.repeat(np.arange(n, dtype=np.uint64), np.diff(e.offsets.astype(np.int64)))
+        dst = e.successors.astype(np.uint64)
+        key = np.unique(np.concatenate([src * n + dst, dst * n + src]))
+        key = key[key // n != key % n]
+        off = np.zeros(n + 1, dtype=np.uint64)
+        off[1:] = np.cumsum(np.bincount((key // n).astype(np.int64), minlength=n))
+        suc = (key % n).astype(np.uint32)
+    if kind != "undirected":
+        t = g.transpose()
+        args = (g.offsets, g.successors, t.offsets, t.successors)
+    else:
+        args = (off, suc)
+    for level in ("radius_diameter", "radius"):
+        one = hbo.sum_sweep(*args, level=level)
+        for threads in (3, 8):
+            assert hbo.sum_sweep(*args, level=level, threads=threads) == one, (level, threads)
+
+
 # ---- the device implementation against the oracle ---------------------------
 
 FIELDS = ("diameter", "radius", "diametral_vertex", "radial_vertex", "radius_iterations",

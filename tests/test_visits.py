@@ -68,6 +68,39 @@ def test_oracle_random_graph_matches_test_definition(oracle, hb):
     assert list(d) == correct_dists(off, succ, start)
 
 
+@pytest.mark.parametrize("make", [lambda hb: hb.Graph.weblike(1 << 16, cap=5000, seed=3),
+                                  lambda hb: hb.Graph.rmat(15, 8, seed=2),
+                                  lambda hb: hb.Graph.erdos_renyi(40000, 3, 9)])
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_oracle_parallel_visit_matches_sequential(oracle, hb, make, threads):
+    """The oracle's fair parallel visit (par_fair.rs:226-323 on host threads;
+    levels of 4,096 nodes and more are split among the threads) gives the
+    sequential visit's distances and Known count, valid predecessors, the
+    shared visited set, and the distance filter."""
+    g = make(hb)
+    off, succ = np.asarray(g.offsets), np.asarray(g.successors)
+    seq, par = oracle.OracleVisit(off, succ), oracle.OracleVisit(off, succ)
+    for roots in ([0], [5, 5, 17, 900]):
+        seq.reset()
+        par.reset()
+        on, op, od = seq.visit(roots)
+        pn, pp, pd = par.par_visit(roots, threads=threads)
+        assert sorted(zip(pn.tolist(), pd.tolist())) == sorted(zip(on.tolist(), od.tolist()))
+        assert par.known == seq.known
+        assert np.all(np.diff(pd.astype(np.int64)) >= 0)  # level by level
+        check_events(off, succ, pn, pp, pd, set(roots))
+    # the visited set persists: nothing new from a visited node
+    assert len(par.par_visit([int(pn[-1])], threads=threads)[0]) == 0
+    # the filter: nodes farther than 2 neither reported nor marked
+    seq.reset()
+    par.reset()
+    on, _, od = seq.visit([3], max_distance=2)
+    pn, pp, pd = par.par_visit([3], max_distance=2, threads=threads)
+    assert sorted(zip(pn.tolist(), pd.tolist())) == sorted(zip(on.tolist(), od.tolist()))
+    rest_seq, rest_par = seq.visit([0])[0], par.par_visit([0], threads=threads)[0]
+    assert sorted(rest_seq.tolist()) == sorted(rest_par.tolist())
+
+
 def check_events(off, succ, nodes, preds, dists, roots_set):
     """Every predecessor is one level closer with an arc to the node; roots
     are their own predecessors at distance 0."""
