@@ -99,6 +99,12 @@ def test_oracle_parallel_visit_matches_sequential(oracle, hb, make, threads):
     assert sorted(zip(pn.tolist(), pd.tolist())) == sorted(zip(on.tolist(), od.tolist()))
     rest_seq, rest_par = seq.visit([0])[0], par.par_visit([0], threads=threads)[0]
     assert sorted(rest_seq.tolist()) == sorted(rest_par.tolist())
+    # distance 0: the roots only, no Known events; no roots: no events
+    par.reset()
+    pn, pp, pd = par.par_visit([4, 2, 4], max_distance=0, threads=threads)
+    assert pn.tolist() == [4, 2] and pp.tolist() == [4, 2] and pd.tolist() == [0, 0]
+    assert par.known == 0
+    assert len(par.par_visit([], threads=threads)[0]) == 0 and par.known == 0
 
 
 def check_events(off, succ, nodes, preds, dists, roots_set):
