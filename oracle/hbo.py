@@ -107,6 +107,10 @@ def lib():
                                              _P(ctypes.c_uint64)]),
             "hbo_eccentricities": (None, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
                                           _P(ctypes.c_uint64)]),
+            "hbo_sccs_tarjan": (ctypes.c_uint64, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                                  _P(ctypes.c_uint64)]),
+            "hbo_sccs_symm": (ctypes.c_uint64, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
+                                                _P(ctypes.c_uint64)]),
             "hbo_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, _P(ctypes.c_uint64)]),
             "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
@@ -433,6 +437,20 @@ def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all
     if eff == 0:
         out["backward_eccentricities"] = be[:n].copy()
     return out
+
+
+def sccs(offsets, successors, symmetric=False):
+    """The components ExactSumSweep's restatement uses: Tarjan's numbering
+    (sccs/tarjan.rs) or, for a symmetric graph, symm_seq.rs's. Returns
+    (number of components, component of every node as uint64)."""
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    suc = np.ascontiguousarray(successors, dtype=np.uint32)
+    n = len(off) - 1
+    comp = np.zeros(max(n, 1), dtype=np.uint64)
+    f = lib().hbo_sccs_symm if symmetric else lib().hbo_sccs_tarjan
+    nc = f(n, off.ctypes.data_as(_P(ctypes.c_uint64)), suc.ctypes.data_as(_P(ctypes.c_uint32)),
+           comp.ctypes.data_as(_P(ctypes.c_uint64)))
+    return int(nc), comp[:n].copy()
 
 
 def eccentricities(offsets, successors):

@@ -542,6 +542,24 @@ int hbo_sum_sweep(uint64_t n, const uint64_t* off, const uint32_t* succ, const u
     return hbo_sum_sweep_par(n, off, succ, toff, tsucc, level, radial, fecc, becc, res, 1);
 }
 
+// The components the restatement computes, for the reference's own tests
+// of them (tests/test_sccs.rs): comp[v] for every node; returns their number.
+// hbo_sccs_tarjan: sccs/tarjan.rs numbering; hbo_sccs_symm: sccs/symm_seq.rs
+// numbering (symmetric graphs).
+uint64_t hbo_sccs_tarjan(uint64_t n, const uint64_t* off, const uint32_t* succ, uint64_t* comp) {
+    u64 nc = 0;
+    const std::vector<u64> c = tarjan(Csr{n, off, succ}, nc);
+    std::copy(c.begin(), c.end(), comp);
+    return nc;
+}
+
+uint64_t hbo_sccs_symm(uint64_t n, const uint64_t* off, const uint32_t* succ, uint64_t* comp) {
+    u64 nc = 0;
+    const std::vector<u64> c = symm_components(Csr{n, off, succ}, nc);
+    std::copy(c.begin(), c.end(), comp);
+    return nc;
+}
+
 // Forward eccentricity of every node by one breadth-first visit each (the
 // definition; small graphs only).
 void hbo_eccentricities(uint64_t n, const uint64_t* off, const uint32_t* succ, uint64_t* ecc) {
