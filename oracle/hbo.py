@@ -111,6 +111,8 @@ def lib():
                                                   _P(ctypes.c_uint64)]),
             "hbo_sccs_symm": (ctypes.c_uint64, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint32),
                                                 _P(ctypes.c_uint64)]),
+            "hbo_arg_select": (ctypes.c_uint64, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint64),
+                                                 _P(ctypes.c_uint8), ctypes.c_int]),
             "hbo_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, _P(ctypes.c_uint64)]),
             "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
@@ -437,6 +439,21 @@ def sum_sweep(offsets, successors, t_offsets=None, t_successors=None, level="all
     if eff == 0:
         out["backward_eccentricities"] = be[:n].copy()
     return out
+
+
+def arg_select(values, tie=None, keep=None, maximize=True):
+    """The restatement's argmax / argmin (utils/argmax.rs, argmin.rs): the
+    index of the largest (maximize) or smallest (value, tie) among the kept
+    indices, the first among equals; None when nothing is kept."""
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    n = len(v)
+    t = np.zeros(max(n, 1), dtype=np.uint64) if tie is None else np.ascontiguousarray(tie, dtype=np.uint64)
+    k = np.ones(max(n, 1), dtype=np.uint8) if keep is None else np.ascontiguousarray(keep, dtype=np.uint8)
+    if n == 0:
+        v = np.zeros(1, dtype=np.uint64)
+    r = lib().hbo_arg_select(n, v.ctypes.data_as(_P(ctypes.c_uint64)), t.ctypes.data_as(_P(ctypes.c_uint64)),
+                             k.ctypes.data_as(_P(ctypes.c_uint8)), 1 if maximize else 0)
+    return None if r == 2**64 - 1 else int(r)
 
 
 def sccs(offsets, successors, symmetric=False):

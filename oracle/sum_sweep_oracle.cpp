@@ -183,6 +183,30 @@ void scc_dag(const Csr& g, const Csr& t, const std::vector<u64>& comp, u64 ncomp
     }
 }
 
+// argmax.rs: the largest (value, tie) among the kept indices, the smallest
+// index among equals; NONE when nothing is kept
+template <class V, class T, class F>
+u64 argmax_kept(u64 n, const V& val, const T& tie, F keep) {
+    u64 best = NONE;
+    for (u64 i = 0; i < n; i++) {
+        if (!keep(i)) continue;
+        if (best == NONE || val[i] > val[best] || (val[i] == val[best] && tie[i] > tie[best])) best = i;
+    }
+    return best;
+}
+
+// argmin.rs: the smallest (value, tie) among the kept indices, the smallest
+// index among equals; NONE when nothing is kept
+template <class V, class T, class F>
+u64 argmin_kept(u64 n, const V& val, const T& tie, F keep) {
+    u64 best = NONE;
+    for (u64 i = 0; i < n; i++) {
+        if (!keep(i)) continue;
+        if (best == NONE || val[i] < val[best] || (val[i] == val[best] && tie[i] < tie[best])) best = i;
+    }
+    return best;
+}
+
 enum Output { ALL = 0, ALL_FORWARD = 1, RADIUS_DIAMETER = 2, DIAMETER = 3, RADIUS = 4 };
 
 struct Computer {
@@ -208,25 +232,13 @@ struct Computer {
     bool inc_f(u64 i) const { return forward_low[i] != forward_high[i]; }
     bool inc_b(u64 i) const { return backward_low[i] != backward_high[i]; }
 
-    // argmax.rs: the largest (value, tie), the smallest index among equals
     template <class F>
     u64 argmax_filtered(const std::vector<u64>& val, const std::vector<u64>& tie, F keep) const {
-        u64 best = NONE;
-        for (u64 i = 0; i < n; i++) {
-            if (!keep(i)) continue;
-            if (best == NONE || val[i] > val[best] || (val[i] == val[best] && tie[i] > tie[best])) best = i;
-        }
-        return best;
+        return argmax_kept(n, val, tie, keep);
     }
-    // argmin.rs: the smallest (value, tie), the smallest index among equals
     template <class F>
     u64 argmin_filtered(const std::vector<u64>& val, const std::vector<u64>& tie, F keep) const {
-        u64 best = NONE;
-        for (u64 i = 0; i < n; i++) {
-            if (!keep(i)) continue;
-            if (best == NONE || val[i] < val[best] || (val[i] == val[best] && tie[i] < tie[best])) best = i;
-        }
-        return best;
+        return argmin_kept(n, val, tie, keep);
     }
 
     // computer.rs:487-542
@@ -540,6 +552,15 @@ int hbo_sum_sweep(uint64_t n, const uint64_t* off, const uint32_t* succ, const u
                   const uint32_t* tsucc, int level, const uint8_t* radial, uint64_t* fecc,
                   uint64_t* becc, uint64_t* res) {
     return hbo_sum_sweep_par(n, off, succ, toff, tsucc, level, radial, fecc, becc, res, 1);
+}
+
+// The selections of the restatement, for the reference's own tests of them
+// (tests/test_math.rs): the index of the largest (maximize) or smallest
+// (value, tie) among the indices with keep[i] != 0, the smallest index among
+// equals; ~0 when none is kept.
+uint64_t hbo_arg_select(uint64_t n, const uint64_t* val, const uint64_t* tie, const uint8_t* keep, int maximize) {
+    auto kept = [&](u64 i) { return keep[i] != 0; };
+    return maximize ? argmax_kept(n, val, tie, kept) : argmin_kept(n, val, tie, kept);
 }
 
 // The components the restatement computes, for the reference's own tests

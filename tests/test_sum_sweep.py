@@ -129,6 +129,39 @@ def test_directed_random_against_definition(d):  # test_exact_sum_sweep.rs:292-3
     np.testing.assert_array_equal(r["backward_eccentricities"], hbo.eccentricities(toff, tsuc))
 
 
+# ---- the selections' tie rules (tests/test_math.rs, utils/argmax.rs, argmin.rs) --
+
+def _sel(v, t=None, keep=None, maximize=True):
+    k = None if keep is None else [1 if keep(i, x) else 0 for i, x in enumerate(v)]
+    return hbo.arg_select(v, t, k, maximize)
+
+
+def test_argmax_cases():  # test_math.rs:13-70, argmax.rs doc examples
+    assert _sel([]) is None
+    assert _sel([0]) == 0
+    assert _sel([2, 1, 5, 3]) == 2
+    assert _sel([2, 5, 1, 3, 5]) == 1
+    assert _sel([], [], lambda i, e: True) is None
+    assert _sel([2, 1, 5, 3, 1], [5, 4, 3, 2, 1], lambda i, e: False) is None
+    assert _sel([0], [0], lambda i, e: True) == 0
+    assert _sel([1, 2, 3, 4, 5, 4, 3, 2, 1], list(range(1, 10)), lambda i, e: e < 4) == 6
+    assert _sel([1, 2, 3, 2, 1], [1, 2, 3, 2, 1], lambda i, e: e < 3) == 1
+    assert _sel([1, 2, 5, 2, 1, 2], [1, 2, 3, 4, 5, 2], lambda i, e: e < 4) == 3
+    assert _sel([1, 2, 5, 2, 1, 2], [1, 1, 3, 2, 5, 2], lambda i, e: e < 4) == 3
+
+
+def test_argmin_cases():  # test_math.rs:72-135
+    assert _sel([], maximize=False) is None
+    assert _sel([2**64 - 1], maximize=False) == 0
+    assert _sel([2, 1, 5, 3], maximize=False) == 1
+    assert _sel([2, 1, 5, 3, 1], maximize=False) == 1
+    assert _sel([], [], lambda i, e: True, maximize=False) is None
+    assert _sel([2, 1, 5, 3, 1], [5, 4, 3, 2, 1], lambda i, e: False, maximize=False) is None
+    assert _sel([2**64 - 1], [2**64 - 1], lambda i, e: True, maximize=False) == 0
+    assert _sel([1, 2, 3, 4, 5, 4, 3, 2, 1], list(range(9, 0, -1)), lambda i, e: e > 2, maximize=False) == 6
+    assert _sel([1, 2, 3, 2, 1], [1, 2, 3, 2, 1], lambda i, e: e > 1, maximize=False) == 1
+
+
 # ---- the reference's undirected cases (tests/test_undir_sum_sweep.rs) --------
 
 def sym(arcs):
