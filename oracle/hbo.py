@@ -114,6 +114,8 @@ def lib():
             "hbo_arg_select": (ctypes.c_uint64, [ctypes.c_uint64, _P(ctypes.c_uint64), _P(ctypes.c_uint64),
                                                  _P(ctypes.c_uint8), ctypes.c_int]),
             "hbo_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, _P(ctypes.c_uint64)]),
+            "hbo_par_visit_each": (None, [V, _P(ctypes.c_uint64), ctypes.c_uint64, ctypes.c_uint32,
+                                          _P(ctypes.c_uint64)]),
             "hbo_visit_run": (ctypes.c_uint64, [V, _P(ctypes.c_uint64), ctypes.c_uint64,
                                                 ctypes.c_uint64, _P(ctypes.c_uint64),
                                                 _P(ctypes.c_uint64), _P(ctypes.c_uint64),
@@ -391,6 +393,14 @@ class OracleVisit:
         d = np.zeros(self.n, dtype=np.uint64)
         lib().hbo_visit_each(self._h, r.ctypes.data_as(_P(ctypes.c_uint64)), len(r),
                              d.ctypes.data_as(_P(ctypes.c_uint64)))
+        return d
+
+    def par_visit_each(self, roots, threads=None):
+        r = np.ascontiguousarray(roots, dtype=np.uint64)
+        d = np.zeros(self.n, dtype=np.uint64)
+        th = (os.cpu_count() or 1) if threads is None else max(1, int(threads))
+        lib().hbo_par_visit_each(self._h, r.ctypes.data_as(_P(ctypes.c_uint64)), len(r), th,
+                                 d.ctypes.data_as(_P(ctypes.c_uint64)))
         return d
 
 

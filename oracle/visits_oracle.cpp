@@ -146,4 +146,17 @@ void hbo_visit_each(void* vv, const uint64_t* roots, uint64_t nroots, uint64_t* 
     }
 }
 
+// The parallel visit from each root in order (tests/test_bfv.rs:251-283, the
+// same test run on the parallel visits): dist[node] for every node a visit
+// reaches.
+void hbo_par_visit_each(void* vv, const uint64_t* roots, uint64_t nroots, uint32_t threads, uint64_t* dist) {
+    hbo_visit* v = (hbo_visit*)vv;
+    std::vector<uint64_t> nodes(v->n), preds(v->n), ds(v->n);
+    for (uint64_t i = 0; i < nroots; i++) {
+        const uint64_t k = hbo_par_visit_run(vv, roots + i, 1, UINT64_MAX, threads, nodes.data(), preds.data(),
+                                             ds.data(), v->n, nullptr);
+        for (uint64_t j = 0; j < k; j++) dist[nodes[j]] = ds[j];
+    }
+}
+
 }  // extern "C"

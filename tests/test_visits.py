@@ -107,6 +107,20 @@ def test_oracle_parallel_visit_matches_sequential(oracle, hb, make, threads):
     assert len(par.par_visit([], threads=threads)[0]) == 0 and par.known == 0
 
 
+def test_oracle_parallel_visit_cnr2000_every_root(oracle, hb):
+    """tests/test_bfv.rs:251-283 (the cnr-2000 test of the parallel visits):
+    every root in order from 10,000; the oracle's parallel visit gives the
+    sequential visit's distances."""
+    base = cnr_basename()
+    if base is None:
+        pytest.skip("cnr-2000 not available (run tests/golden/make_fixtures.py)")
+    g = hb.Graph.load_bvgraph(base)
+    roots = (np.arange(g.num_nodes, dtype=np.uint64) + 10000) % g.num_nodes
+    want = oracle.OracleVisit(g.offsets, g.successors).visit_each(roots)
+    got = oracle.OracleVisit(g.offsets, g.successors).par_visit_each(roots, threads=4)
+    np.testing.assert_array_equal(got, want)
+
+
 def check_events(off, succ, nodes, preds, dists, roots_set):
     """Every predecessor is one level closer with an arc to the node; roots
     are their own predecessors at distance 0."""
