@@ -52,6 +52,13 @@ def test_no_device_fails_loudly(hb):
         hb.HyperBallBuilder.new(g, logic).build()
 
 
+def test_missing_library_fails_loudly(hb, tmp_path):
+    """Without the built library the Python mirror raises: it has no other
+    implementation to fall back on."""
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        hb.load_library(str(tmp_path / "libhyperball_gb300.so"))
+
+
 def test_invalid_arguments(hb):
     g = hb.Graph.erdos_renyi(100, 3, 0)
     with pytest.raises(hb.InvalidArgumentError):
